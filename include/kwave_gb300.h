@@ -1,0 +1,142 @@
+/* C ABI of the GB300 k-space first-order time loop (libkwave_gb300.so).
+ *
+ * The library replaces the time loop of k-wave-python's native solver
+ * (kwave/solvers/kspace_solver.py, Simulation.setup :205-241, Simulation.step
+ * :691-747, Simulation.run :749-778), reached from kspaceFirstOrder2D/3D
+ * (kwave/kspaceFirstOrder2D.py:215-218, kwave/kspaceFirstOrder3D.py:208-211)
+ * through kwave/solvers/native.py:6-30 (run_python_backend).
+ *
+ * Conventions: plain host pointers and sizes; grids are C order with axis 0 = x
+ * and the last axis contiguous; all device memory belongs to the plan.  Every
+ * call returns KW_OK (0) or an error code; kw_last_error() gives the
+ * thread-local message of the last failure.
+ */
+#ifndef KWAVE_GB300_H
+#define KWAVE_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  KW_OK = 0,
+  KW_ERR_INVALID = 1,      /* bad argument / descriptor (reference raises ValueError) */
+  KW_ERR_CUDA = 2,         /* CUDA runtime failure */
+  KW_ERR_OOM = 3,          /* device allocation failed */
+  KW_ERR_UNSUPPORTED = 4,  /* e.g. FFT length with a prime factor above 7 */
+  KW_ERR_STATE = 5         /* call out of order (e.g. run before finalize) */
+};
+
+/* Grid, time axis and physics switches.  Mirrors what Simulation.setup derives
+ * (kspace_solver.py:205-241, :363-550). */
+typedef struct kw_grid_desc {
+  int32_t ndim;          /* 2 or 3 */
+  int32_t shape[3];      /* N_x, N_y, N_z (unused entries 1) */
+  int32_t Nt;            /* number of time steps (kgrid.Nt) */
+  int32_t record_start;  /* 0-based first recorded step (sensor.record_start_index - 1) */
+  double spacing[3];     /* d_x, d_y, d_z [m] */
+  double dt;             /* [s] */
+  double c_ref;          /* max(c0), kspace_solver.py:231 */
+  int32_t use_sg;        /* staggered grid shifts (kspace_solver.py:440-447) */
+  int32_t use_kspace;    /* kappa / source_kappa (kspace_solver.py:429-435) */
+  int32_t absorb_mode;   /* 0 none, 1 power law (fractional Laplacian), 2 Stokes (y = 2) */
+  int32_t dispersion;    /* 1: power-law dispersion term enabled (kspace_solver.py:500-524) */
+  int32_t nonlinear;     /* 1: B/A enabled (kspace_solver.py:526-550) */
+  int32_t reserved;
+  double alpha_power;    /* y */
+} kw_grid_desc;
+
+/* Grid-valued inputs.  n == 0 (or host == NULL) selects the scalar. */
+enum {
+  KW_F_C0 = 0,       /* sound speed c0 */
+  KW_F_RHO0 = 1,     /* density rho0 */
+  KW_F_DTRSG0 = 2,   /* dt / rho0 staggered along x (kspace_solver.py:657-666) */
+  KW_F_DTRSG1 = 3,   /* ... along y */
+  KW_F_DTRSG2 = 4,   /* ... along z */
+  KW_F_BONA = 5,     /* B/A */
+  KW_F_TAU = 6,      /* absorption coefficient tau (kspace_solver.py:494-497) */
+  KW_F_ETA = 7,      /* dispersion coefficient eta (kspace_solver.py:522) */
+  KW_F_P0 = 8        /* initial pressure, already smoothed if requested */
+};
+
+/* One-dimensional per-axis tables (length N_axis; complex tables hold 2*N floats
+ * re,im interleaved). */
+enum {
+  KW_T_K = 0,        /* 2 pi fftfreq(N, d) (kspace_solver.py:419) */
+  KW_T_PML = 1,      /* PML, non-staggered (kwave/utils/pml.py:6-64) */
+  KW_T_PMLSG = 2,    /* PML, staggered */
+  KW_T_OPGRAD = 3,   /* i k e^{+i k d/2} (Hermitian part), without kappa (complex) */
+  KW_T_OPDIV = 4,    /* i k e^{-i k d/2} (Hermitian part), without kappa (complex) */
+  KW_T_UNSTAG = 5    /* e^{-i k d/2} (Hermitian part) (kspace_solver.py:677) (complex) */
+};
+
+/* Source slots: KW_S_P0..2 = pressure source injected into rho_x/y/z, already
+ * scaled per axis (kspace_solver.py:597-624); KW_S_U0..2 = velocity sources. */
+enum { KW_S_P0 = 0, KW_S_P1 = 1, KW_S_P2 = 2, KW_S_U0 = 3, KW_S_U1 = 4, KW_S_U2 = 5 };
+/* Source modes (kspace_solver.py:86-114). */
+enum { KW_SRC_DIRICHLET = 0, KW_SRC_ADDITIVE = 1, KW_SRC_ADDITIVE_NC = 2 };
+
+/* Recorded series.  Stored time-major on the device; read back sensor-major. */
+enum {
+  KW_R_P = 0,
+  KW_R_UX_ST = 1, KW_R_UY_ST = 2, KW_R_UZ_ST = 3,  /* staggered u (kspace_solver.py:744-745) */
+  KW_R_UX = 4, KW_R_UY = 5, KW_R_UZ = 6            /* u shifted to the pressure grid (:740-743) */
+};
+/* Fields readable after a run. */
+enum { KW_FLD_P = 0, KW_FLD_U0 = 1, KW_FLD_U1 = 2, KW_FLD_U2 = 3, KW_FLD_RHO0 = 4, KW_FLD_RHO1 = 5, KW_FLD_RHO2 = 6 };
+/* Aggregates over the recorded time axis (kspace_solver.py:824-837). */
+enum { KW_AGG_MAX = 0, KW_AGG_MIN = 1, KW_AGG_RMS = 2 };
+
+typedef struct kw_plan kw_plan;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int32_t kw_version(void);
+/* Thread-local message of the last failing call ("" if none). */
+const char* kw_last_error(void);
+/* Device properties of the current CUDA device. */
+int32_t kw_device_query(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor, uint64_t* free_bytes);
+
+/* Simulation.__init__/setup (kspace_solver.py:135-241): validates the grid and
+ * the FFT lengths. */
+int32_t kw_plan_create(const kw_grid_desc* desc, kw_plan** out);
+/* _expand_to_grid of medium/p0 inputs (kspace_solver.py:48-57, 228-230, 680-687). */
+int32_t kw_plan_set_field(kw_plan* plan, int32_t field, const float* host, int64_t n, float scalar);
+/* _setup_pml / _setup_kspace_operators tables (kspace_solver.py:363-447). */
+int32_t kw_plan_set_table(kw_plan* plan, int32_t table, int32_t axis, const float* host, int64_t n_floats);
+/* _build_source_op (kspace_solver.py:60-114): flat C-order mask indices and the
+ * scaled signal, (n_rows, length) row-major; n_rows == 1 broadcasts. */
+int32_t kw_plan_set_source(kw_plan* plan, int32_t slot, int32_t mode, const int64_t* mask_index, int32_t n_points,
+                           const float* signal, int32_t n_rows, int32_t length);
+/* _setup_sensor_mask (kspace_solver.py:243-326): flat C-order grid indices that
+ * are sampled every recorded step, and which series to record (bit r set =
+ * record series r of KW_R_*). */
+int32_t kw_plan_set_sensor(kw_plan* plan, const int64_t* slot_index, int32_t n_slots, int32_t record_mask);
+/* Cartesian sensors (kspace_solver.py:328-361): point s is
+ * sum_c weight[s*n_corners+c] * sample[slot[s*n_corners+c]]. */
+int32_t kw_plan_set_sensor_interp(kw_plan* plan, int32_t n_points, int32_t n_corners, const int32_t* slot,
+                                  const double* weight);
+/* Allocates device memory, uploads all inputs and resets the state to t = 0. */
+int32_t kw_plan_finalize(kw_plan* plan);
+/* Advances min(nsteps, Nt - t) steps of Simulation.step (kspace_solver.py:691-747)
+ * on `stream` (a cudaStream_t, NULL = default stream); returns after enqueueing. */
+int32_t kw_plan_run(kw_plan* plan, int32_t nsteps, void* stream);
+/* Waits for the plan's work on `stream`. */
+int32_t kw_plan_sync(kw_plan* plan, void* stream);
+/* Current step index t. */
+int32_t kw_plan_time_index(const kw_plan* plan, int32_t* t);
+/* Recorded series, sensor-major (n_points, n_recorded_steps) float32, the layout
+ * of sensor_data[...] in kspace_solver.py:663-668. */
+int32_t kw_plan_read_series(kw_plan* plan, int32_t series, float* host, int64_t n);
+/* Aggregate over recorded steps (max/min/rms), n_points float32. */
+int32_t kw_plan_read_aggregate(kw_plan* plan, int32_t series, int32_t kind, float* host, int64_t n);
+/* Whole field (p, u_i or rho_i), C order, N_total float32. */
+int32_t kw_plan_read_field(kw_plan* plan, int32_t field, float* host, int64_t n);
+/* Device pointer of a field (valid until kw_plan_destroy). */
+int32_t kw_plan_field_device_ptr(kw_plan* plan, int32_t field, void** dptr);
+/* Frees all device memory of the plan. */
+int32_t kw_plan_destroy(kw_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,455 @@
+// Kernels of the k-space first-order time loop (see kw_kernels.cuh).
+//
+// Arithmetic order inside the physics follows kwave/solvers/kspace_solver.py
+// (Simulation.step, :691-747) operation by operation, with explicit
+// round-to-nearest intrinsics so that the compiler does not contract the
+// reference's separate multiplies and adds into FMAs.
+#include "kw_kernels.cuh"
+
+// ---------------------------------------------------------------------------
+// spectral operators (kspace_solver.py:408-447, :811-816)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 axis_op(const AxisParams& P, const AxisJob& J, int x, int c, bool& valid) {
+  int a1, a2 = 0;
+  float kk;
+  const float kx = P.k[0][x];
+  if (P.ndim == 3) {
+    a1 = c / P.Hp;
+    a2 = c - a1 * P.Hp;
+    valid = a2 < P.H;
+    if (!valid) return make_float2(0.f, 0.f);
+    const float ky = P.k[1][a1], kz = P.k[2][a2];
+    kk = __fadd_rn(__fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+  } else {
+    a1 = c;
+    valid = a1 < P.H;
+    if (!valid) return make_float2(0.f, 0.f);
+    const float ky = P.k[1][a1];
+    kk = __fadd_rn(__fmul_rn(kx, kx), __fmul_rn(ky, ky));
+  }
+  const float kmag = sqrtf(kk);
+  const int ai = (J.axis == 0) ? x : (J.axis == 1 ? a1 : a2);
+  float2 v;
+  switch (J.op) {
+    case OP_GRAD:
+    case OP_DIV: {
+      float kappa = 1.f;
+      if (P.use_kspace) {
+        const float arg = P.kcoef * kmag;
+        kappa = (arg == 0.f) ? 1.f : sinf(arg) / arg;
+      }
+      const float2 f = (J.op == OP_GRAD) ? P.fg[J.axis][ai] : P.fd[J.axis][ai];
+      v = make_float2(f.x * kappa, f.y * kappa);
+      break;
+    }
+    case OP_NAB1:
+    case OP_NAB2: {
+      const float e = (J.op == OP_NAB1) ? P.pow1 : P.pow2;
+      v = make_float2(kmag == 0.f ? 0.f : powf(kmag, e), 0.f);
+      break;
+    }
+    case OP_SKAPPA:
+      v = make_float2(P.use_kspace ? cosf(P.kcoef * kmag) : 1.f, 0.f);
+      break;
+    default:
+      v = P.us[J.axis][ai];
+      break;
+  }
+  return make_float2(v.x * P.scale, v.y * P.scale);
+}
+
+// ---------------------------------------------------------------------------
+// strided-axis FFT kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_axis(const __grid_constant__ AxisParams P) {
+  extern __shared__ float4 smem_f4[];
+  float2* sm = reinterpret_cast<float2*>(smem_f4);
+  const int n = P.n, T = P.T;
+  float2* tw = sm;
+  float2* A = sm + n;
+  float2* B = A + (size_t)n * T;
+  float2* C = B + (size_t)n * T;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = P.tw[i];
+  const int c0 = blockIdx.x * T;
+  const int nc = min(T, P.ncols - c0);
+  const long long base = (long long)blockIdx.y * P.os + c0;
+  const int tot = n * T;
+
+  if (P.mode < 2) {
+    float2* buf = P.bufs[P.plain[blockIdx.z]];
+    const bool inv = P.mode == 1;
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int x = i / T, cc = i - x * T;
+      float2 v = make_float2(0.f, 0.f);
+      if (cc < nc) v = buf[base + (long long)x * P.xs + cc];
+      A[i] = inv ? cconj(v) : v;
+    }
+    float2* res = fft_smem<true>(A, B, P.flen, T, T, 1, tw);
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int x = i / T, cc = i - x * T;
+      if (cc < nc) {
+        const float2 v = res[i];
+        buf[base + (long long)x * P.xs + cc] = inv ? cconj(v) : v;
+      }
+    }
+    return;
+  }
+
+  int cur = -1;
+  float2* X = A;
+  for (int j = 0; j < P.njobs; ++j) {
+    const AxisJob J = P.jobs[j];
+    if (J.in != cur) {
+      const float2* in = P.bufs[J.in];
+      for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+        const int x = i / T, cc = i - x * T;
+        A[i] = (cc < nc) ? in[base + (long long)x * P.xs + cc] : make_float2(0.f, 0.f);
+      }
+      X = fft_smem<true>(A, B, P.flen, T, T, 1, tw);
+      cur = J.in;
+    }
+    float2* Y = (X == A) ? B : A;
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int x = i / T, cc = i - x * T;
+      float2 v = make_float2(0.f, 0.f);
+      if (cc < nc) {
+        bool valid;
+        const float2 op = axis_op(P, J, x, c0 + cc, valid);
+        if (valid) v = cconj(cmul(op, X[i]));
+      }
+      Y[i] = v;
+    }
+    float2* res = fft_smem<true>(Y, C, P.flen, T, T, 1, tw);
+    float2* out = P.bufs[J.out];
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int x = i / T, cc = i - x * T;
+      if (cc < nc) out[base + (long long)x * P.xs + cc] = cconj(res[i]);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// row helpers (block-wide)
+// ---------------------------------------------------------------------------
+struct RowSmem {
+  float2* tw;
+  float2* twp;
+  float2* A;
+  float2* B;
+  float* rb[KW_NREAL];
+};
+
+// C2R of R rows of spectral buffer S into rbuf (unnormalised: L * x).
+__device__ void rows_c2r(const RowsParams& P, const RowSmem& s, const float2* __restrict__ S, float* rbuf, int r0,
+                         int nr) {
+  const int M = P.Mfft, L = P.L, R = P.R;
+  const int tot = R * M;
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int row = i / M, k = i - row * M;
+    float2 z = make_float2(0.f, 0.f);
+    if (row < nr) {
+      const float2* sr = S + (long long)(r0 + row) * P.Hp;
+      if (P.even) {
+        const float2 xk = sr[k];
+        const float2 xc = cconj(sr[M - k]);
+        const float2 e = cadd(xk, xc);
+        const float2 o = cmul(csub(xk, xc), cconj(s.twp[k]));
+        z = make_float2(e.x - o.y, e.y + o.x);
+      } else {
+        z = (k < P.H) ? sr[k] : cconj(sr[L - k]);
+      }
+    }
+    s.A[i] = cconj(z);
+  }
+  float2* res = fft_smem<false>(s.A, s.B, P.flen, R, 1, M, s.tw);
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int row = i / M, n = i - row * M;
+    const float2 v = res[i];
+    if (P.even) {
+      rbuf[row * L + 2 * n] = v.x;
+      rbuf[row * L + 2 * n + 1] = -v.y;
+    } else {
+      rbuf[row * L + n] = v.x;
+    }
+  }
+  __syncthreads();
+}
+
+// R2C of rbuf rows into spectral buffer S.
+__device__ void rows_r2c(const RowsParams& P, const RowSmem& s, const float* rbuf, float2* __restrict__ S, int r0,
+                         int nr) {
+  const int M = P.Mfft, L = P.L, R = P.R, H = P.H;
+  const int tot = R * M;
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int row = i / M, n = i - row * M;
+    s.A[i] = P.even ? make_float2(rbuf[row * L + 2 * n], rbuf[row * L + 2 * n + 1]) : make_float2(rbuf[row * L + n], 0.f);
+  }
+  float2* res = fft_smem<false>(s.A, s.B, P.flen, R, 1, M, s.tw);
+  const int toth = R * H;
+  for (int i = threadIdx.x; i < toth; i += blockDim.x) {
+    const int row = i / H, k = i - row * H;
+    if (row >= nr) continue;
+    float2 X;
+    if (P.even) {
+      const float2 zk = res[row * M + (k == M ? 0 : k)];
+      const float2 zc = cconj(res[row * M + (k == 0 ? 0 : M - k)]);
+      const float2 e = cscale(cadd(zk, zc), 0.5f);
+      const float2 d = csub(zk, zc);
+      const float2 o = make_float2(0.5f * d.y, -0.5f * d.x);
+      X = cadd(e, cmul(s.twp[k], o));
+    } else {
+      X = res[row * L + k];
+    }
+    S[(long long)(r0 + row) * P.Hp + k] = X;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ int axis_index(const RowsParams& P, int axis, int grow, int z) {
+  if (axis == P.ndim - 1) return z;
+  if (axis == 0) return (P.ndim == 3) ? grow / P.N1 : grow;
+  return grow % P.N1;  // axis 1 of a 3-D grid
+}
+
+__device__ __forceinline__ float fld(const float* p, float s, long long g) { return p ? p[g] : s; }
+
+// Apply a sparse source to rbuf for the block's rows (kspace_solver.py:86-109).
+__device__ void apply_source(const RowsParams& P, const KwSrcDev& S, float* rbuf, int r0, int nr) {
+  if (!S.active || P.t >= S.len) return;
+  const int e0 = S.row_ptr[r0], e1 = S.row_ptr[r0 + nr];
+  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int4 en = S.ent[e];
+    const float val = S.sig[(long long)P.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+    float& f = rbuf[(en.x - r0) * P.L + en.y];
+    if (S.mode == SRC_DIRICHLET)
+      f = val;
+    else
+      f = __fadd_rn(f, val);
+  }
+}
+
+__device__ void record_samples(const RowsParams& P, const float* rbuf, float* rec, int r0, int nr) {
+  if (rec == nullptr || P.rec_row < 0 || P.sens_row_ptr == nullptr) return;
+  const int e0 = P.sens_row_ptr[r0], e1 = P.sens_row_ptr[r0 + nr];
+  float* out = rec + (long long)P.rec_row * P.nslots;
+  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int4 en = P.sens_ent[e];
+    out[en.z] = rbuf[(en.x - r0) * P.L + en.y];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// row stage kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams P) {
+  extern __shared__ float4 smem_f4[];
+  const int M = P.Mfft, L = P.L, R = P.R;
+  RowSmem s;
+  s.tw = reinterpret_cast<float2*>(smem_f4);
+  s.twp = s.tw + M;
+  s.A = s.twp + (L / 2 + 1);
+  s.B = s.A + (size_t)R * M;
+  float* rb = reinterpret_cast<float*>(s.B + (size_t)R * M);
+  for (int q = 0; q < KW_NREAL; ++q) s.rb[q] = rb + (size_t)q * R * L;
+  for (int i = threadIdx.x; i < M; i += blockDim.x) s.tw[i] = P.tw[i];
+  if (P.even)
+    for (int i = threadIdx.x; i <= L / 2; i += blockDim.x) s.twp[i] = P.twpost[i];
+  __syncthreads();  // rows_c2r reads twp before its first FFT barrier
+
+  const int r0 = blockIdx.x * R;
+  const int nr = min(R, P.nrows - r0);
+  const int tot = R * L;
+  const int D = P.ndim;
+
+  if (P.stage == ST_INIT) {
+    // t = 0 with p0: p = p0, rho_i = p0 / (c0^2 D) (kspace_solver.py:729-733)
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = i / L, z = i - row * L;
+      if (row >= nr) continue;
+      const long long g = (long long)(r0 + row) * L + z;
+      const float pv = P.p0[g];
+      const float c = fld(P.c0, P.c0_s, g);
+      const float c2 = __fmul_rn(c, c);
+      const float r = __fdiv_rn(pv, __fmul_rn(c2, (float)D));
+      for (int a = 0; a < D; ++a) P.rho[a][g] = r;
+      if (P.write_p) P.p[g] = pv;
+      s.rb[0][i] = pv;
+    }
+    __syncthreads();
+    record_samples(P, s.rb[0], P.rec[0], r0, nr);
+    rows_r2c(P, s, s.rb[0], P.S[3], r0, nr);
+    return;
+  }
+
+  if (P.stage == ST_U) {
+    // momentum: u_i = pml_sg (pml_sg u_i - dt/rho_sg g_i) (kspace_solver.py:703-707)
+    for (int a = 0; a < D; ++a) {
+      rows_c2r(P, s, P.S[a], s.rb[0], r0, nr);
+      float* u = P.u[a];
+      for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+        const int row = i / L, z = i - row * L;
+        if (row >= nr) continue;
+        const long long g = (long long)(r0 + row) * L + z;
+        const float gr = s.rb[0][i];
+        const float dtr = fld(P.dtrsg[a], P.dtrsg_s[a], g);
+        float nu;
+        if (P.init) {
+          nu = __fmul_rn(__fmul_rn(dtr, 0.5f), gr);
+        } else {
+          const float sg = P.pmlsg[a][axis_index(P, a, r0 + row, z)];
+          nu = __fmul_rn(sg, __fsub_rn(__fmul_rn(sg, u[g]), __fmul_rn(dtr, gr)));
+        }
+        s.rb[0][i] = nu;
+      }
+      __syncthreads();
+      if (!P.init) apply_source(P, P.src[3 + a], s.rb[0], r0, nr);
+      __syncthreads();
+      for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+        const int row = i / L, z = i - row * L;
+        if (row >= nr) continue;
+        u[(long long)(r0 + row) * L + z] = s.rb[0][i];
+      }
+      record_samples(P, s.rb[0], P.rec[1 + a], r0, nr);
+      if (!P.init) rows_r2c(P, s, s.rb[0], P.S[a], r0, nr);
+      __syncthreads();
+    }
+    return;
+  }
+
+  if (P.stage == ST_RHO) {
+    // mass conservation with split density (kspace_solver.py:709-717)
+    for (int a = 0; a < D; ++a) rows_c2r(P, s, P.S[a], s.rb[a], r0, nr);
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = i / L, z = i - row * L;
+      if (row >= nr) continue;
+      const long long g = (long long)(r0 + row) * L + z;
+      const float r0v = fld(P.rho0, P.rho0_s, g);
+      float nl = 1.f;
+      if (P.nonlin) {
+        float sr = P.rho[0][g];
+        for (int a = 1; a < D; ++a) sr = __fadd_rn(sr, P.rho[a][g]);
+        nl = __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr), r0v), r0v);
+      }
+      float div = 0.f;
+      const float dtr0 = __fmul_rn(P.dt, r0v);
+      for (int a = 0; a < D; ++a) {
+        const float du = s.rb[a][i];
+        div = __fadd_rn(div, du);
+        const float pm = P.pml[a][axis_index(P, a, r0 + row, z)];
+        const float term = __fmul_rn(__fmul_rn(dtr0, du), nl);
+        s.rb[a][i] = __fmul_rn(pm, __fsub_rn(__fmul_rn(pm, P.rho[a][g]), term));
+      }
+      s.rb[3][i] = div;
+    }
+    __syncthreads();
+    for (int a = 0; a < D; ++a) apply_source(P, P.src[a], s.rb[a], r0, nr);
+    __syncthreads();
+    const bool powerlaw = P.absorb == 1;
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = i / L, z = i - row * L;
+      if (row >= nr) continue;
+      const long long g = (long long)(r0 + row) * L + z;
+      float rs = s.rb[0][i];
+      P.rho[0][g] = rs;
+      for (int a = 1; a < D; ++a) {
+        const float ra = s.rb[a][i];
+        P.rho[a][g] = ra;
+        rs = __fadd_rn(rs, ra);
+      }
+      const float div = s.rb[3][i];
+      const float r0v = fld(P.rho0, P.rho0_s, g);
+      if (powerlaw) {
+        P.rho_sum[g] = rs;
+        s.rb[0][i] = __fmul_rn(r0v, div);
+        s.rb[1][i] = rs;
+      } else {
+        // equation of state without fractional Laplacians (kspace_solver.py:719-723)
+        const float c = fld(P.c0, P.c0_s, g);
+        const float c2 = __fmul_rn(c, c);
+        float acc = rs;
+        if (P.absorb == 2) acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(fld(P.tau, P.tau_s, g), r0v), div));
+        if (P.nonlin) {
+          const float nlt = __fdiv_rn(__fmul_rn(fld(P.bona, P.bona_s, g), __fmul_rn(rs, rs)), __fmul_rn(2.f, r0v));
+          acc = __fadd_rn(acc, nlt);
+        }
+        const float pv = __fmul_rn(c2, acc);
+        if (P.write_p) P.p[g] = pv;
+        s.rb[0][i] = pv;
+      }
+    }
+    __syncthreads();
+    if (powerlaw) {
+      rows_r2c(P, s, s.rb[0], P.S[0], r0, nr);
+      if (P.disp) rows_r2c(P, s, s.rb[1], P.S[1], r0, nr);
+    } else {
+      record_samples(P, s.rb[0], P.rec[0], r0, nr);
+      rows_r2c(P, s, s.rb[0], P.S[3], r0, nr);
+    }
+    return;
+  }
+
+  // ST_EOS: p = c0^2 (rho + tau F^-1[nabla1 F[rho0 div]] - eta F^-1[nabla2 F[rho]] + B/A rho^2 / (2 rho0))
+  rows_c2r(P, s, P.S[0], s.rb[0], r0, nr);
+  if (P.disp) rows_c2r(P, s, P.S[1], s.rb[1], r0, nr);
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int row = i / L, z = i - row * L;
+    if (row >= nr) continue;
+    const long long g = (long long)(r0 + row) * L + z;
+    const float rs = P.rho_sum[g];
+    const float c = fld(P.c0, P.c0_s, g);
+    const float c2 = __fmul_rn(c, c);
+    float acc = __fadd_rn(rs, __fmul_rn(fld(P.tau, P.tau_s, g), s.rb[0][i]));
+    if (P.disp) acc = __fsub_rn(acc, __fmul_rn(fld(P.eta, P.eta_s, g), s.rb[1][i]));
+    if (P.nonlin) {
+      const float r0v = fld(P.rho0, P.rho0_s, g);
+      const float nlt = __fdiv_rn(__fmul_rn(fld(P.bona, P.bona_s, g), __fmul_rn(rs, rs)), __fmul_rn(2.f, r0v));
+      acc = __fadd_rn(acc, nlt);
+    }
+    const float pv = __fmul_rn(c2, acc);
+    if (P.write_p) P.p[g] = pv;
+    s.rb[0][i] = pv;
+  }
+  __syncthreads();
+  record_samples(P, s.rb[0], P.rec[0], r0, nr);
+  rows_r2c(P, s, s.rb[0], P.S[3], r0, nr);
+}
+
+// ---------------------------------------------------------------------------
+// recorder post-processing (kspace_solver.py:335-359, :824-837)
+// ---------------------------------------------------------------------------
+// out[pt][t] = sum_c w[pt][c] * rec[t][slot[pt][c]]  (ncorner == 0: out[pt][t] = rec[t][pt])
+__global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
+                                const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out) {
+  const long long tot = (long long)npts * nrec;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int pt = (int)(i / nrec), t = (int)(i - (long long)pt * nrec);
+    if (ncorner == 0) {
+      out[i] = rec[(long long)t * nslots + pt];
+    } else {
+      double acc = 0.0;
+      for (int c = 0; c < ncorner; ++c)
+        acc += w[(long long)pt * ncorner + c] * (double)rec[(long long)t * nslots + slot[(long long)pt * ncorner + c]];
+      out[i] = (float)acc;
+    }
+  }
+}
+
+__global__ void k_series_reduce(const float* __restrict__ series, int npts, int nrec, int kind, float* __restrict__ out) {
+  const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pt >= npts) return;
+  const float* s = series + (long long)pt * nrec;
+  if (kind == 2) {
+    double acc = 0.0;
+    for (int t = 0; t < nrec; ++t) {
+      const float v = s[t];
+      const float v2 = v * v;
+      acc += (double)v2;
+    }
+    out[pt] = sqrtf((float)(acc / nrec));
+  } else {
+    float m = s[0];
+    for (int t = 1; t < nrec; ++t) m = (kind == 0) ? fmaxf(m, s[t]) : fminf(m, s[t]);
+    out[pt] = m;
+  }
+}

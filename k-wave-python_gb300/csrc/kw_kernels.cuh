@@ -1,0 +1,110 @@
+// Kernels of the k-space first-order time loop.
+//
+// Spectral layout.  A real field of shape (N0[, N1], L), C order, is held in
+// "row spectra": every row of L reals along the last axis becomes H = L/2 + 1
+// complex values (numpy rfft convention), stored with a row stride Hp = H
+// rounded up to an even count (16-byte aligned rows).  The other axes are then
+// transformed in place as complex sequences.
+//
+// Two kernel families:
+//   * k_axis  : complex FFT along a strided axis (axis 0, or axis 1 of a 3-D
+//               grid), in place.  In "ops" mode it runs forward FFT, multiplies
+//               by a spectral operator, runs the inverse FFT and stores, for
+//               one or more (input, output, operator) jobs.  The operators
+//               (gradient, divergence, fractional Laplacian, source kappa,
+//               unstagger shift) are evaluated on the fly from 1-D tables.
+//   * k_rows  : one stage of the time step on whole rows along the last axis:
+//               C2R of the stage's inputs, the real-space physics of that
+//               stage (velocity update, split-density update, equation of
+//               state, sources, sensor sampling), and R2C of the outputs.
+#pragma once
+#include "kw_fft.cuh"
+
+#define KW_NBUF 8
+#define KW_MAX_JOBS 8
+#define KW_NREAL 4
+
+enum KwStage { ST_INIT = 0, ST_U = 1, ST_RHO = 2, ST_EOS = 3 };
+enum KwOp { OP_GRAD = 0, OP_DIV = 1, OP_NAB1 = 2, OP_NAB2 = 3, OP_SKAPPA = 4, OP_UNSTAG = 5 };
+enum KwSrcMode { SRC_DIRICHLET = 0, SRC_ADDITIVE = 1, SRC_ADDITIVE_NC = 2 };
+
+struct KwSrcDev {
+  int active;            // 0 = no source in this slot
+  int mode;              // KwSrcMode
+  int nsig;              // signal rows (1 = broadcast)
+  int len;               // signal length in steps
+  const int* row_ptr;    // per grid row: first entry (nrows + 1)
+  const int4* ent;       // (row, pos, point, 0) sorted by row
+  const float* sig;      // time-major [len][nsig], pre-scaled
+};
+
+struct RowsParams {
+  int stage, init;
+  int ndim, N0, N1, L, H, Hp, Mfft, even;
+  int nrows, R;
+  int t, rec_row, write_p;
+  float2* S[4];          // spectral work buffers S0..S2 and P (index 3)
+  float* u[3];
+  float* rho[3];
+  float* p;
+  float* rho_sum;
+  const float* p0;
+  const float* c0;
+  float c0_s;
+  const float* rho0;
+  float rho0_s;
+  const float* dtrsg[3];
+  float dtrsg_s[3];
+  const float* bona;
+  float bona_s;
+  const float* tau;
+  float tau_s;
+  const float* eta;
+  float eta_s;
+  int absorb, disp, nonlin;
+  float dt;
+  const float* pml[3];
+  const float* pmlsg[3];
+  const float2* tw;       // Mfft twiddles
+  const float2* twpost;   // exp(-2 pi i k / L), k <= L/2 (even L)
+  KwFftLen flen;
+  KwSrcDev src[6];        // p into rho_0..2, then u_0..2
+  const int* sens_row_ptr;
+  const int4* sens_ent;   // (row, pos, slot, 0)
+  int nslots;
+  float* rec[7];
+};
+
+struct AxisJob {
+  int in, out, op, axis;
+};
+
+struct AxisParams {
+  float2* bufs[KW_NBUF];
+  int n;
+  long long xs;   // element stride along the axis
+  long long os;   // stride between outer blocks (blockIdx.y)
+  int ncols;      // contiguous positions per outer block
+  int T;          // positions per tile
+  int mode;       // 0 plain forward, 1 plain inverse, 2 ops
+  int plain[KW_NBUF];
+  int njobs;
+  AxisJob jobs[KW_MAX_JOBS];
+  KwFftLen flen;
+  const float2* tw;
+  int ndim, H, Hp;
+  const float* k[3];
+  const float2* fg[3];
+  const float2* fd[3];
+  const float2* us[3];
+  float kcoef;    // c_ref * dt / 2
+  int use_kspace;
+  float pow1, pow2;
+  float scale;    // 1 / N_total
+};
+
+__global__ void k_axis(const __grid_constant__ AxisParams P);
+__global__ void k_rows(const __grid_constant__ RowsParams P);
+__global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
+                                const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out);
+__global__ void k_series_reduce(const float* __restrict__ series, int npts, int nrec, int kind, float* __restrict__ out);

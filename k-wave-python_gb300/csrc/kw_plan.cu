@@ -1,0 +1,712 @@
+// Host side of libkwave_gb300: plan objects, uploads, the launch sequence of
+// one time step, and the extern "C" entry points declared in
+// include/kwave_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/kwave_gb300.h"
+#include "kw_kernels.cuh"
+
+#define KW_VERSION 100  // 0.1.0
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(e_ == cudaErrorMemoryAllocation ? KW_ERR_OOM : KW_ERR_CUDA, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                         \
+  } while (0)
+
+static const int kThreads = 256;
+
+struct HostSrc {
+  bool set = false;
+  int mode = 0;
+  std::vector<long long> idx;
+  std::vector<float> sig;  // (nrows, len) row-major as given
+  int nrows = 0, len = 0;
+};
+
+struct kw_plan {
+  kw_grid_desc g{};
+  int D = 0;
+  int N[3] = {1, 1, 1};
+  long long ntot = 0;
+  int L = 0, H = 0, Hp = 0, Mfft = 0, even = 0, nrows = 0, R = 1;
+  long long spec_elems = 0;
+  bool finalized = false;
+  int t = 0;
+  // staged host inputs
+  std::vector<float> hfield[9];
+  float hscalar[9] = {0};
+  std::vector<float> htab[6][3];
+  HostSrc hsrc[6];
+  std::vector<long long> sens_idx;
+  int record_mask = 0;
+  int interp_npts = 0, interp_nc = 0;
+  std::vector<int> interp_slot;
+  std::vector<double> interp_w;
+  // device
+  std::vector<void*> allocs;
+  float* d_u[3] = {nullptr, nullptr, nullptr};
+  float* d_rho[3] = {nullptr, nullptr, nullptr};
+  float* d_p = nullptr;
+  float* d_rhosum = nullptr;
+  float2* d_S[4] = {nullptr, nullptr, nullptr, nullptr};
+  float* d_field[9] = {nullptr};
+  float* d_tab[6][3] = {{nullptr}};
+  float2* d_tw_axis[3] = {nullptr, nullptr, nullptr};
+  KwFftLen flen_axis[3];
+  float2* d_tw_row = nullptr;
+  float2* d_twpost = nullptr;
+  KwFftLen flen_row;
+  KwSrcDev src[6];
+  int* d_sens_rowptr = nullptr;
+  int4* d_sens_ent = nullptr;
+  int nslots = 0;
+  float* d_rec[7] = {nullptr};
+  int nrec = 0;
+  int* d_islot = nullptr;
+  double* d_iw = nullptr;
+  size_t smem_rows = 0, smem_axis_plain[3] = {0, 0, 0}, smem_axis_ops = 0;
+  int T_axis[3] = {1, 1, 1};
+};
+
+static bool factor_len(int n, KwFftLen& f) {
+  f.n = n;
+  f.nst = 0;
+  int m = n;
+  const int rs[5] = {4, 2, 3, 5, 7};
+  for (int r : rs) {
+    while (m % r == 0 && m > 1) {
+      if (f.nst >= KW_MAX_STAGES) return false;
+      f.radix[f.nst++] = r;
+      m /= r;
+    }
+  }
+  return m == 1;
+}
+
+template <typename T>
+static int dalloc(kw_plan* p, T** out, size_t count) {
+  void* ptr = nullptr;
+  size_t bytes = count * sizeof(T);
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&ptr, bytes);
+  if (e != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? KW_ERR_OOM : KW_ERR_CUDA, "cudaMalloc(%zu): %s", bytes,
+                cudaGetErrorString(e));
+  p->allocs.push_back(ptr);
+  *out = static_cast<T*>(ptr);
+  return KW_OK;
+}
+
+template <typename T>
+static int upload(kw_plan* p, T** out, const T* host, size_t count) {
+  int rc = dalloc(p, out, count);
+  if (rc) return rc;
+  if (count) CK(cudaMemcpy(*out, host, count * sizeof(T), cudaMemcpyHostToDevice));
+  return KW_OK;
+}
+
+static std::vector<float2> twiddles(int n, int count) {
+  std::vector<float2> w(count);
+  for (int j = 0; j < count; ++j) {
+    const double a = -2.0 * M_PI * (double)j / (double)n;
+    w[j] = make_float2((float)cos(a), (float)sin(a));
+  }
+  return w;
+}
+
+extern "C" {
+
+int32_t kw_version(void) { return KW_VERSION; }
+
+const char* kw_last_error(void) { return g_err.c_str(); }
+
+int32_t kw_device_query(int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor, uint64_t* free_bytes) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, dev));
+  if (sm_count) *sm_count = prop.multiProcessorCount;
+  if (cc_major) *cc_major = prop.major;
+  if (cc_minor) *cc_minor = prop.minor;
+  if (free_bytes) {
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    *free_bytes = fr;
+  }
+  return KW_OK;
+}
+
+int32_t kw_plan_create(const kw_grid_desc* desc, kw_plan** out) {
+  if (!desc || !out) return fail(KW_ERR_INVALID, "kw_plan_create: null argument");
+  if (desc->ndim != 2 && desc->ndim != 3) return fail(KW_ERR_UNSUPPORTED, "only 2-D and 3-D grids are supported (ndim=%d)", desc->ndim);
+  if (desc->Nt < 1) return fail(KW_ERR_INVALID, "Nt must be >= 1 (got %d)", desc->Nt);
+  if (desc->record_start < 0 || desc->record_start >= desc->Nt)
+    return fail(KW_ERR_INVALID, "record start %d outside [0, Nt)", desc->record_start);
+  kw_plan* p = new kw_plan();
+  p->g = *desc;
+  p->D = desc->ndim;
+  p->ntot = 1;
+  for (int a = 0; a < p->D; ++a) {
+    p->N[a] = desc->shape[a];
+    if (p->N[a] < 2 || p->N[a] > 4096) {
+      delete p;
+      return fail(KW_ERR_UNSUPPORTED, "grid size %d along axis %d outside [2, 4096]", desc->shape[a], a);
+    }
+    p->ntot *= p->N[a];
+  }
+  p->L = p->N[p->D - 1];
+  p->H = p->L / 2 + 1;
+  p->Hp = (p->H + 1) & ~1;
+  p->even = (p->L % 2) == 0;
+  p->Mfft = p->even ? p->L / 2 : p->L;
+  p->nrows = (int)(p->ntot / p->L);
+  p->spec_elems = (long long)p->nrows * p->Hp;
+  for (int a = 0; a < p->D - 1; ++a) {
+    if (!factor_len(p->N[a], p->flen_axis[a])) {
+      int n = p->N[a];
+      delete p;
+      return fail(KW_ERR_UNSUPPORTED, "FFT length %d (axis %d) has a prime factor above 7", n, a);
+    }
+  }
+  if (!factor_len(p->Mfft, p->flen_row)) {
+    int n = p->L;
+    delete p;
+    return fail(KW_ERR_UNSUPPORTED, "FFT length %d (last axis) has a prime factor above 7", n);
+  }
+  for (int i = 0; i < 9; ++i) p->hscalar[i] = 0.f;
+  *out = p;
+  return KW_OK;
+}
+
+int32_t kw_plan_set_field(kw_plan* p, int32_t field, const float* host, int64_t n, float scalar) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (field < 0 || field > KW_F_P0) return fail(KW_ERR_INVALID, "unknown field id %d", field);
+  if (host && n > 0) {
+    if (n != p->ntot) return fail(KW_ERR_INVALID, "field %d has %lld values, grid has %lld", field, (long long)n, p->ntot);
+    p->hfield[field].assign(host, host + n);
+  } else {
+    p->hfield[field].clear();
+  }
+  p->hscalar[field] = scalar;
+  return KW_OK;
+}
+
+int32_t kw_plan_set_table(kw_plan* p, int32_t table, int32_t axis, const float* host, int64_t n_floats) {
+  if (!p || !host) return fail(KW_ERR_INVALID, "null argument");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (table < 0 || table > KW_T_UNSTAG || axis < 0 || axis >= p->D) return fail(KW_ERR_INVALID, "bad table %d / axis %d", table, axis);
+  const bool cplx = table >= KW_T_OPGRAD;
+  const long long want = (long long)p->N[axis] * (cplx ? 2 : 1);
+  if (n_floats != want) return fail(KW_ERR_INVALID, "table %d axis %d: %lld floats, expected %lld", table, axis, (long long)n_floats, want);
+  p->htab[table][axis].assign(host, host + n_floats);
+  return KW_OK;
+}
+
+int32_t kw_plan_set_source(kw_plan* p, int32_t slot, int32_t mode, const int64_t* mask_index, int32_t n_points,
+                           const float* signal, int32_t n_rows, int32_t length) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (slot < 0 || slot > KW_S_U2) return fail(KW_ERR_INVALID, "unknown source slot %d", slot);
+  if ((slot % 3) >= p->D) return fail(KW_ERR_INVALID, "source slot %d beyond ndim", slot);
+  if (mode < 0 || mode > KW_SRC_ADDITIVE_NC) return fail(KW_ERR_INVALID, "Unknown source mode: %d", mode);
+  if (n_points <= 0 || !mask_index || !signal || length <= 0) return fail(KW_ERR_INVALID, "empty source");
+  if (n_rows != 1 && n_rows != n_points)
+    return fail(KW_ERR_INVALID, "source signal has %d rows for %d mask points", n_rows, n_points);
+  HostSrc& s = p->hsrc[slot];
+  s.set = true;
+  s.mode = mode;
+  s.idx.assign(mask_index, mask_index + n_points);
+  for (long long v : s.idx)
+    if (v < 0 || v >= p->ntot) return fail(KW_ERR_INVALID, "source index %lld outside grid", v);
+  for (size_t i = 1; i < s.idx.size(); ++i)
+    if (s.idx[i] <= s.idx[i - 1]) return fail(KW_ERR_INVALID, "source mask indices must be strictly increasing (C order)");
+  s.sig.assign(signal, signal + (size_t)n_rows * length);
+  s.nrows = n_rows;
+  s.len = length;
+  return KW_OK;
+}
+
+int32_t kw_plan_set_sensor(kw_plan* p, const int64_t* slot_index, int32_t n_slots, int32_t record_mask) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (n_slots < 0 || (n_slots > 0 && !slot_index)) return fail(KW_ERR_INVALID, "bad sensor slots");
+  p->sens_idx.assign(slot_index, slot_index + n_slots);
+  for (long long v : p->sens_idx)
+    if (v < 0 || v >= p->ntot) return fail(KW_ERR_INVALID, "sensor index %lld outside grid", v);
+  for (size_t i = 1; i < p->sens_idx.size(); ++i)
+    if (p->sens_idx[i] <= p->sens_idx[i - 1]) return fail(KW_ERR_INVALID, "sensor slot indices must be strictly increasing");
+  if (record_mask & ~0x7f) return fail(KW_ERR_INVALID, "bad record mask 0x%x", record_mask);
+  for (int a = p->D; a < 3; ++a)
+    if (record_mask & ((1 << (1 + a)) | (1 << (4 + a)))) return fail(KW_ERR_INVALID, "velocity record beyond ndim");
+  p->record_mask = record_mask;
+  return KW_OK;
+}
+
+int32_t kw_plan_set_sensor_interp(kw_plan* p, int32_t n_points, int32_t n_corners, const int32_t* slot,
+                                  const double* weight) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (n_points <= 0 || n_corners <= 0 || !slot || !weight) return fail(KW_ERR_INVALID, "bad interpolation table");
+  p->interp_npts = n_points;
+  p->interp_nc = n_corners;
+  p->interp_slot.assign(slot, slot + (size_t)n_points * n_corners);
+  p->interp_w.assign(weight, weight + (size_t)n_points * n_corners);
+  return KW_OK;
+}
+
+static int build_csr(kw_plan* p, const std::vector<long long>& idx, int** d_rowptr, int4** d_ent) {
+  std::vector<int> rowptr(p->nrows + 1, 0);
+  std::vector<int4> ent(idx.size());
+  for (size_t i = 0; i < idx.size(); ++i) {
+    const int row = (int)(idx[i] / p->L);
+    const int pos = (int)(idx[i] % p->L);
+    ent[i] = make_int4(row, pos, (int)i, 0);
+    rowptr[row + 1]++;
+  }
+  for (int r = 0; r < p->nrows; ++r) rowptr[r + 1] += rowptr[r];
+  int rc = upload(p, d_rowptr, rowptr.data(), rowptr.size());
+  if (rc) return rc;
+  return upload(p, d_ent, ent.data(), ent.size());
+}
+
+int32_t kw_plan_finalize(kw_plan* p) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  const int D = p->D;
+  int rc;
+  // required tables
+  for (int a = 0; a < D; ++a) {
+    for (int tb : {KW_T_K, KW_T_PML, KW_T_PMLSG, KW_T_OPGRAD, KW_T_OPDIV})
+      if (p->htab[tb][a].empty()) return fail(KW_ERR_INVALID, "table %d for axis %d not set", tb, a);
+  }
+  if (p->g.absorb_mode == 1 && !p->g.use_kspace && false) return KW_ERR_INVALID;
+  for (int sl = 0; sl < 6; ++sl)
+    if (p->hsrc[sl].set && p->hsrc[sl].mode == KW_SRC_ADDITIVE)
+      return fail(KW_ERR_UNSUPPORTED, "k-space corrected additive sources are not implemented yet");
+  if (p->record_mask & (0x70))
+    return fail(KW_ERR_UNSUPPORTED, "non-staggered velocity recording is not implemented yet");
+
+  // state and work buffers
+  for (int a = 0; a < D; ++a) {
+    if ((rc = dalloc(p, &p->d_u[a], p->ntot))) return rc;
+    if ((rc = dalloc(p, &p->d_rho[a], p->ntot))) return rc;
+  }
+  if ((rc = dalloc(p, &p->d_p, p->ntot))) return rc;
+  if (p->g.absorb_mode == 1)
+    if ((rc = dalloc(p, &p->d_rhosum, p->ntot))) return rc;
+  for (int b = 0; b < 4; ++b) {
+    if (b < D || b == 3 || (b < 2 && p->g.absorb_mode == 1)) {
+      if ((rc = dalloc(p, &p->d_S[b], p->spec_elems))) return rc;
+    }
+  }
+  // medium fields
+  for (int f = 0; f < 9; ++f)
+    if (!p->hfield[f].empty())
+      if ((rc = upload(p, &p->d_field[f], p->hfield[f].data(), p->hfield[f].size()))) return rc;
+  // tables
+  for (int tb = 0; tb < 6; ++tb)
+    for (int a = 0; a < D; ++a)
+      if (!p->htab[tb][a].empty())
+        if ((rc = upload(p, &p->d_tab[tb][a], p->htab[tb][a].data(), p->htab[tb][a].size()))) return rc;
+  // twiddles
+  for (int a = 0; a < D - 1; ++a) {
+    std::vector<float2> w = twiddles(p->N[a], p->N[a]);
+    if ((rc = upload(p, &p->d_tw_axis[a], w.data(), w.size()))) return rc;
+  }
+  {
+    std::vector<float2> w = twiddles(p->Mfft, p->Mfft);
+    if ((rc = upload(p, &p->d_tw_row, w.data(), w.size()))) return rc;
+    std::vector<float2> wp = twiddles(p->L, p->L / 2 + 1);
+    if ((rc = upload(p, &p->d_twpost, wp.data(), wp.size()))) return rc;
+  }
+  // sources
+  for (int sl = 0; sl < 6; ++sl) {
+    KwSrcDev& s = p->src[sl];
+    memset(&s, 0, sizeof(s));
+    const HostSrc& h = p->hsrc[sl];
+    if (!h.set) continue;
+    s.active = 1;
+    s.mode = h.mode;
+    s.nsig = h.nrows;
+    s.len = h.len;
+    int* rp;
+    int4* en;
+    if ((rc = build_csr(p, h.idx, &rp, &en))) return rc;
+    s.row_ptr = rp;
+    s.ent = en;
+    std::vector<float> tm((size_t)h.len * h.nrows);
+    for (int r = 0; r < h.nrows; ++r)
+      for (int t = 0; t < h.len; ++t) tm[(size_t)t * h.nrows + r] = h.sig[(size_t)r * h.len + t];
+    float* ds;
+    if ((rc = upload(p, &ds, tm.data(), tm.size()))) return rc;
+    s.sig = ds;
+  }
+  // sensor
+  p->nslots = (int)p->sens_idx.size();
+  p->nrec = p->g.Nt - p->g.record_start;
+  if (p->nslots > 0) {
+    if ((rc = build_csr(p, p->sens_idx, &p->d_sens_rowptr, &p->d_sens_ent))) return rc;
+    for (int s = 0; s < 7; ++s)
+      if (p->record_mask & (1 << s)) {
+        if ((rc = dalloc(p, &p->d_rec[s], (size_t)p->nrec * p->nslots))) return rc;
+        CK(cudaMemset(p->d_rec[s], 0, (size_t)p->nrec * p->nslots * sizeof(float)));
+      }
+  }
+  if (p->interp_npts > 0) {
+    for (int v : p->interp_slot)
+      if (v < 0 || v >= p->nslots) return fail(KW_ERR_INVALID, "interpolation slot %d outside [0, %d)", v, p->nslots);
+    if ((rc = upload(p, &p->d_islot, p->interp_slot.data(), p->interp_slot.size()))) return rc;
+    if ((rc = upload(p, &p->d_iw, p->interp_w.data(), p->interp_w.size()))) return rc;
+  }
+  // zero state
+  for (int a = 0; a < D; ++a) {
+    CK(cudaMemset(p->d_u[a], 0, p->ntot * sizeof(float)));
+    CK(cudaMemset(p->d_rho[a], 0, p->ntot * sizeof(float)));
+  }
+  CK(cudaMemset(p->d_p, 0, p->ntot * sizeof(float)));
+  for (int b = 0; b < 4; ++b)
+    if (p->d_S[b]) CK(cudaMemset(p->d_S[b], 0, p->spec_elems * sizeof(float2)));
+
+  // launch geometry
+  p->R = (p->L >= 2048) ? 1 : 2048 / p->L;
+  if (p->R > 16) p->R = 16;
+  p->smem_rows = sizeof(float2) * ((size_t)p->Mfft + p->L / 2 + 1 + 2 * (size_t)p->R * p->Mfft) +
+                 sizeof(float) * (size_t)KW_NREAL * p->R * p->L;
+  for (int a = 0; a < D - 1; ++a) {
+    int n = p->N[a];
+    int T = 16;
+    while (T > 1 && (size_t)3 * n * T * sizeof(float2) > 100 * 1024) T /= 2;
+    p->T_axis[a] = T;
+    p->smem_axis_plain[a] = sizeof(float2) * ((size_t)n + 2 * (size_t)n * T);
+    size_t ops = sizeof(float2) * ((size_t)n + 3 * (size_t)n * T);
+    if (a == 0) p->smem_axis_ops = ops;
+  }
+  CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  CK(cudaFuncSetAttribute(k_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  CK(cudaDeviceSynchronize());
+  p->finalized = true;
+  p->t = 0;
+  return KW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// launch sequence
+// ---------------------------------------------------------------------------
+static void fill_rows(const kw_plan* p, RowsParams& P) {
+  memset(&P, 0, sizeof(P));
+  P.ndim = p->D;
+  P.N0 = p->N[0];
+  P.N1 = p->D == 3 ? p->N[1] : 1;
+  P.L = p->L;
+  P.H = p->H;
+  P.Hp = p->Hp;
+  P.Mfft = p->Mfft;
+  P.even = p->even;
+  P.nrows = p->nrows;
+  P.R = p->R;
+  for (int b = 0; b < 4; ++b) P.S[b] = p->d_S[b];
+  for (int a = 0; a < 3; ++a) {
+    P.u[a] = p->d_u[a];
+    P.rho[a] = p->d_rho[a];
+    P.pml[a] = p->d_tab[KW_T_PML][a];
+    P.pmlsg[a] = p->d_tab[KW_T_PMLSG][a];
+    P.dtrsg[a] = p->d_field[KW_F_DTRSG0 + a];
+    P.dtrsg_s[a] = p->hscalar[KW_F_DTRSG0 + a];
+  }
+  P.p = p->d_p;
+  P.rho_sum = p->d_rhosum;
+  P.p0 = p->d_field[KW_F_P0];
+  P.c0 = p->d_field[KW_F_C0];
+  P.c0_s = p->hscalar[KW_F_C0];
+  P.rho0 = p->d_field[KW_F_RHO0];
+  P.rho0_s = p->hscalar[KW_F_RHO0];
+  P.bona = p->d_field[KW_F_BONA];
+  P.bona_s = p->hscalar[KW_F_BONA];
+  P.tau = p->d_field[KW_F_TAU];
+  P.tau_s = p->hscalar[KW_F_TAU];
+  P.eta = p->d_field[KW_F_ETA];
+  P.eta_s = p->hscalar[KW_F_ETA];
+  P.absorb = p->g.absorb_mode;
+  P.disp = p->g.dispersion;
+  P.nonlin = p->g.nonlinear;
+  P.dt = (float)p->g.dt;
+  P.tw = p->d_tw_row;
+  P.twpost = p->d_twpost;
+  P.flen = p->flen_row;
+  for (int s = 0; s < 6; ++s) P.src[s] = p->src[s];
+  P.sens_row_ptr = p->d_sens_rowptr;
+  P.sens_ent = p->d_sens_ent;
+  P.nslots = p->nslots;
+  for (int s = 0; s < 7; ++s) P.rec[s] = p->d_rec[s];
+}
+
+static int launch_rows(const kw_plan* p, int stage, int init, int t, int write_p, cudaStream_t st) {
+  RowsParams P;
+  fill_rows(p, P);
+  P.stage = stage;
+  P.init = init;
+  P.t = t;
+  P.rec_row = (t >= p->g.record_start) ? t - p->g.record_start : -1;
+  P.write_p = write_p;
+  const int grid = (p->nrows + p->R - 1) / p->R;
+  k_rows<<<grid, kThreads, p->smem_rows, st>>>(P);
+  CK(cudaGetLastError());
+  return KW_OK;
+}
+
+static void fill_axis_geom(const kw_plan* p, int axis, AxisParams& A) {
+  memset(&A, 0, sizeof(A));
+  for (int b = 0; b < 4; ++b) A.bufs[b] = p->d_S[b];
+  A.n = p->N[axis];
+  A.flen = p->flen_axis[axis];
+  A.tw = p->d_tw_axis[axis];
+  A.T = p->T_axis[axis];
+  A.ndim = p->D;
+  A.H = p->H;
+  A.Hp = p->Hp;
+  if (p->D == 3) {
+    if (axis == 0) {
+      A.xs = (long long)p->N[1] * p->Hp;
+      A.os = 0;
+      A.ncols = p->N[1] * p->Hp;
+    } else {
+      A.xs = p->Hp;
+      A.os = (long long)p->N[1] * p->Hp;
+      A.ncols = p->Hp;
+    }
+  } else {
+    A.xs = p->Hp;
+    A.os = 0;
+    A.ncols = p->Hp;
+  }
+}
+
+static int launch_axis_plain(const kw_plan* p, int axis, int inv, const int* bufs, int nb, cudaStream_t st) {
+  AxisParams A;
+  fill_axis_geom(p, axis, A);
+  A.mode = inv ? 1 : 0;
+  for (int i = 0; i < nb; ++i) A.plain[i] = bufs[i];
+  const int nouter = (p->D == 3 && axis == 1) ? p->N[0] : 1;
+  dim3 grid((A.ncols + A.T - 1) / A.T, nouter, nb);
+  k_axis<<<grid, kThreads, p->smem_axis_plain[axis], st>>>(A);
+  CK(cudaGetLastError());
+  return KW_OK;
+}
+
+static int launch_axis_ops(const kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t st) {
+  AxisParams A;
+  fill_axis_geom(p, 0, A);
+  A.mode = 2;
+  A.njobs = nj;
+  for (int i = 0; i < nj; ++i) A.jobs[i] = jobs[i];
+  for (int a = 0; a < p->D; ++a) {
+    A.k[a] = p->d_tab[KW_T_K][a];
+    A.fg[a] = reinterpret_cast<const float2*>(p->d_tab[KW_T_OPGRAD][a]);
+    A.fd[a] = reinterpret_cast<const float2*>(p->d_tab[KW_T_OPDIV][a]);
+    A.us[a] = reinterpret_cast<const float2*>(p->d_tab[KW_T_UNSTAG][a]);
+  }
+  A.kcoef = (float)(p->g.c_ref * p->g.dt / 2.0);
+  A.use_kspace = p->g.use_kspace;
+  A.pow1 = (float)(p->g.alpha_power - 2.0);
+  A.pow2 = (float)(p->g.alpha_power - 1.0);
+  A.scale = (float)(1.0 / (double)p->ntot);
+  dim3 grid((A.ncols + A.T - 1) / A.T, 1, 1);
+  k_axis<<<grid, kThreads, p->smem_axis_ops, st>>>(A);
+  CK(cudaGetLastError());
+  return KW_OK;
+}
+
+static int enqueue_step(kw_plan* p, int t, bool last, cudaStream_t st) {
+  const int D = p->D;
+  const bool three = D == 3;
+  int rc;
+  const int SB[3] = {0, 1, 2};
+  const int PB[1] = {3};
+  AxisJob jobs[KW_MAX_JOBS];
+  const bool has_p0 = !p->hfield[KW_F_P0].empty();
+  if (t == 0 && has_p0) {
+    // initial condition override (kspace_solver.py:725-733)
+    if ((rc = launch_rows(p, ST_INIT, 0, t, 1, st))) return rc;
+    if (three && (rc = launch_axis_plain(p, 1, 0, PB, 1, st))) return rc;
+    for (int a = 0; a < D; ++a) jobs[a] = AxisJob{3, a, OP_GRAD, a};
+    if ((rc = launch_axis_ops(p, jobs, D, st))) return rc;
+    if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) return rc;
+    return launch_rows(p, ST_U, 1, t, 0, st);
+  }
+  // momentum
+  for (int a = 0; a < D; ++a) jobs[a] = AxisJob{3, a, OP_GRAD, a};
+  if ((rc = launch_axis_ops(p, jobs, D, st))) return rc;
+  if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) return rc;
+  if ((rc = launch_rows(p, ST_U, 0, t, 0, st))) return rc;
+  // mass conservation
+  if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) return rc;
+  for (int a = 0; a < D; ++a) jobs[a] = AxisJob{a, a, OP_DIV, a};
+  if ((rc = launch_axis_ops(p, jobs, D, st))) return rc;
+  if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) return rc;
+  const bool powerlaw = p->g.absorb_mode == 1;
+  if ((rc = launch_rows(p, ST_RHO, 0, t, (!powerlaw && last) ? 1 : 0, st))) return rc;
+  if (powerlaw) {
+    const int nb = p->g.dispersion ? 2 : 1;
+    if (three && (rc = launch_axis_plain(p, 1, 0, SB, nb, st))) return rc;
+    jobs[0] = AxisJob{0, 0, OP_NAB1, 0};
+    jobs[1] = AxisJob{1, 1, OP_NAB2, 0};
+    if ((rc = launch_axis_ops(p, jobs, nb, st))) return rc;
+    if (three && (rc = launch_axis_plain(p, 1, 1, SB, nb, st))) return rc;
+    if ((rc = launch_rows(p, ST_EOS, 0, t, last ? 1 : 0, st))) return rc;
+  }
+  if (three && (rc = launch_axis_plain(p, 1, 0, PB, 1, st))) return rc;
+  return KW_OK;
+}
+
+int32_t kw_plan_run(kw_plan* p, int32_t nsteps, void* stream) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_run before kw_plan_finalize");
+  if (nsteps < 0) return fail(KW_ERR_INVALID, "nsteps < 0");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int end = std::min(p->g.Nt, p->t + nsteps);
+  for (int t = p->t; t < end; ++t) {
+    int rc = enqueue_step(p, t, t == end - 1, st);
+    if (rc) return rc;
+  }
+  p->t = end;
+  return KW_OK;
+}
+
+int32_t kw_plan_sync(kw_plan* p, void* stream) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  CK(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
+  return KW_OK;
+}
+
+int32_t kw_plan_time_index(const kw_plan* p, int32_t* t) {
+  if (!p || !t) return fail(KW_ERR_INVALID, "null argument");
+  *t = p->t;
+  return KW_OK;
+}
+
+static int series_device(kw_plan* p, int series, float** out_dev, int* npts) {
+  if (series < 0 || series > 6 || !p->d_rec[series]) return fail(KW_ERR_INVALID, "series %d was not recorded", series);
+  const int np = p->interp_npts > 0 ? p->interp_npts : p->nslots;
+  float* buf;
+  int rc = dalloc(p, &buf, (size_t)np * p->nrec);
+  if (rc) return rc;
+  const long long tot = (long long)np * p->nrec;
+  int grid = (int)std::min<long long>((tot + kThreads - 1) / kThreads, 65535);
+  if (grid < 1) grid = 1;
+  k_series_gather<<<grid, kThreads>>>(p->d_rec[series], p->nrec, p->nslots, np, p->interp_nc, p->d_islot, p->d_iw, buf);
+  CK(cudaGetLastError());
+  *out_dev = buf;
+  *npts = np;
+  return KW_OK;
+}
+
+static void dfree_last(kw_plan* p, void* ptr) {
+  for (size_t i = 0; i < p->allocs.size(); ++i)
+    if (p->allocs[i] == ptr) {
+      cudaFree(ptr);
+      p->allocs.erase(p->allocs.begin() + i);
+      return;
+    }
+}
+
+int32_t kw_plan_read_series(kw_plan* p, int32_t series, float* host, int64_t n) {
+  if (!p || !host) return fail(KW_ERR_INVALID, "null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "plan not finalized");
+  float* buf;
+  int np;
+  int rc = series_device(p, series, &buf, &np);
+  if (rc) return rc;
+  if (n != (long long)np * p->nrec) {
+    dfree_last(p, buf);
+    return fail(KW_ERR_INVALID, "series buffer has %lld values, expected %lld", (long long)n, (long long)np * p->nrec);
+  }
+  cudaError_t e = cudaMemcpy(host, buf, n * sizeof(float), cudaMemcpyDeviceToHost);
+  dfree_last(p, buf);
+  if (e != cudaSuccess) return fail(KW_ERR_CUDA, "read_series: %s", cudaGetErrorString(e));
+  return KW_OK;
+}
+
+int32_t kw_plan_read_aggregate(kw_plan* p, int32_t series, int32_t kind, float* host, int64_t n) {
+  if (!p || !host) return fail(KW_ERR_INVALID, "null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "plan not finalized");
+  if (kind < 0 || kind > 2) return fail(KW_ERR_INVALID, "unknown aggregate %d", kind);
+  float* buf;
+  int np;
+  int rc = series_device(p, series, &buf, &np);
+  if (rc) return rc;
+  if (n != np) {
+    dfree_last(p, buf);
+    return fail(KW_ERR_INVALID, "aggregate buffer has %lld values, expected %d", (long long)n, np);
+  }
+  float* agg;
+  if ((rc = dalloc(p, &agg, np))) {
+    dfree_last(p, buf);
+    return rc;
+  }
+  k_series_reduce<<<(np + 255) / 256, 256>>>(buf, np, p->nrec, kind, agg);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(host, agg, n * sizeof(float), cudaMemcpyDeviceToHost);
+  dfree_last(p, agg);
+  dfree_last(p, buf);
+  if (e != cudaSuccess) return fail(KW_ERR_CUDA, "read_aggregate: %s", cudaGetErrorString(e));
+  return KW_OK;
+}
+
+static float* field_ptr(kw_plan* p, int field) {
+  if (field == KW_FLD_P) return p->d_p;
+  if (field >= KW_FLD_U0 && field <= KW_FLD_U2) return p->d_u[field - KW_FLD_U0];
+  if (field >= KW_FLD_RHO0 && field <= KW_FLD_RHO2) return p->d_rho[field - KW_FLD_RHO0];
+  return nullptr;
+}
+
+int32_t kw_plan_read_field(kw_plan* p, int32_t field, float* host, int64_t n) {
+  if (!p || !host) return fail(KW_ERR_INVALID, "null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "plan not finalized");
+  float* d = field_ptr(p, field);
+  if (!d) return fail(KW_ERR_INVALID, "unknown field %d", field);
+  if (n != p->ntot) return fail(KW_ERR_INVALID, "field buffer has %lld values, grid has %lld", (long long)n, p->ntot);
+  CK(cudaMemcpy(host, d, n * sizeof(float), cudaMemcpyDeviceToHost));
+  return KW_OK;
+}
+
+int32_t kw_plan_field_device_ptr(kw_plan* p, int32_t field, void** dptr) {
+  if (!p || !dptr) return fail(KW_ERR_INVALID, "null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "plan not finalized");
+  float* d = field_ptr(p, field);
+  if (!d) return fail(KW_ERR_INVALID, "unknown field %d", field);
+  *dptr = d;
+  return KW_OK;
+}
+
+int32_t kw_plan_destroy(kw_plan* p) {
+  if (!p) return KW_OK;
+  for (void* a : p->allocs) cudaFree(a);
+  delete p;
+  return KW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,14 @@
+"""kwave_gb300: the k-space first-order time loop of k-wave-python on one GB300.
+
+Entry points:
+  * ``backend.install()`` + ``backend.execution_options()`` — select the GPU
+    time loop from the legacy ``kspaceFirstOrder2D/3D`` call;
+  * ``backend.run_gb300_backend`` — the bridge itself (the counterpart of
+    ``kwave.solvers.native.run_python_backend``);
+  * ``solver.Simulation`` — the counterpart of
+    ``kwave.solvers.kspace_solver.Simulation``.
+"""
+__version__ = "0.1.0"
+
+from .backend import BACKEND, execution_options, install, run_gb300_backend, uninstall  # noqa: F401
+from .solver import Simulation, run_problem  # noqa: F401

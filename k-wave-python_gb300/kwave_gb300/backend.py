@@ -1,0 +1,122 @@
+"""Drop-in boundary: the ``"gb300"`` backend behind kspaceFirstOrder2D/3D.
+
+The legacy entry points (kwave/kspaceFirstOrder2D.py:215-218,
+kwave/kspaceFirstOrder3D.py:208-211) import
+``kwave.solvers.native.run_python_backend`` at call time when
+``execution_options.is_python_backend`` is true.  ``install()`` replaces that
+attribute with a dispatcher: execution options whose backend is ``"gb300"``
+go to :func:`run_gb300_backend`, everything else to the original function.
+
+The reference's option setter accepts only None/"OMP"/"CUDA"/"python"
+(kwave/options/simulation_execution_options.py:114-119), so
+:func:`execution_options` builds a subclass that also accepts ``"gb300"`` and
+reports ``is_python_backend`` (the switch the legacy functions test).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .precompute import grid_of
+from .solver import Simulation
+
+BACKEND = "gb300"
+
+
+def is_gb300(execution_options) -> bool:
+    return getattr(execution_options, "backend", None) == BACKEND
+
+
+def _per_axis(val, dim, default, cast):
+    """native.py:9-18, plus broadcasting of a length-1 sequence (the form that
+    SimulationOptions stores a scalar pml_size in, simulation_options.py:178-179)."""
+    if val is None:
+        return (default,) * dim
+    if not hasattr(val, "__len__"):
+        return (cast(val),) * dim
+    seq = [cast(v) for v in np.asarray(val).ravel()]
+    if len(seq) == 1:
+        seq = seq * dim
+    if len(seq) != dim:
+        raise ValueError(f"expected {dim} per-axis values, got {len(seq)}")
+    return tuple(seq)
+
+
+def run_gb300_backend(kgrid, medium, source, sensor, simulation_options, execution_options=None):
+    """GB300 counterpart of ``run_python_backend`` (kwave/solvers/native.py:6-30).
+
+    Same defaults as the reference bridge: PML size 20 and alpha 2.0 per axis
+    when unset, ``use_sg``/``use_kspace``/``smooth_p0`` from the simulation
+    options.  Differences: the computation is float32 (the reference bridge
+    always runs float64 because it never passes ``data_cast``), and a scalar
+    ``pml_size`` is broadcast instead of failing with IndexError.
+    """
+    dim = len(grid_of(kgrid)[0])
+    pml_size = _per_axis(getattr(simulation_options, "pml_size", None), dim, 20, int)
+    pml_alpha = _per_axis(getattr(simulation_options, "pml_alpha", None), dim, 2.0, float)
+    sim = Simulation(
+        kgrid, medium, source, sensor, device="gpu",
+        use_sg=getattr(simulation_options, "use_sg", True),
+        use_kspace=getattr(simulation_options, "use_kspace", True),
+        smooth_p0=getattr(simulation_options, "smooth_p0", True),
+        pml_size=pml_size, pml_alpha=pml_alpha, quiet=True,
+    )
+    try:
+        return sim.run()
+    finally:
+        sim.close()
+
+
+_installed = {}
+
+
+def install():
+    """Route ``backend="gb300"`` through the legacy kspaceFirstOrder2D/3D calls.
+
+    Requires the reference package (``kwave``) to be importable.  Idempotent.
+    """
+    import kwave.solvers.native as native
+
+    if getattr(native.run_python_backend, "_gb300_dispatch", False):
+        return native.run_python_backend
+    original = native.run_python_backend
+
+    def run_python_backend(kgrid, medium, source, sensor, simulation_options, execution_options):
+        if is_gb300(execution_options):
+            return run_gb300_backend(kgrid, medium, source, sensor, simulation_options, execution_options)
+        return original(kgrid, medium, source, sensor, simulation_options, execution_options)
+
+    run_python_backend._gb300_dispatch = True
+    run_python_backend._original = original
+    native.run_python_backend = run_python_backend
+    _installed["native"] = (native, original)
+    return run_python_backend
+
+
+def uninstall():
+    if "native" in _installed:
+        native, original = _installed.pop("native")
+        native.run_python_backend = original
+
+
+def execution_options(**kwargs):
+    """SimulationExecutionOptions with ``backend="gb300"`` (needs ``kwave``)."""
+    from kwave.options.simulation_execution_options import SimulationExecutionOptions
+
+    class GB300ExecutionOptions(SimulationExecutionOptions):
+        @property
+        def backend(self):
+            return self._backend
+
+        @backend.setter
+        def backend(self, value):
+            if value not in (None, "OMP", "CUDA", "python", BACKEND):
+                raise ValueError(f"Backend must be one of [None, 'OMP', 'CUDA', 'python', '{BACKEND}'], got '{value}'")
+            self._backend = value
+
+        @property
+        def is_python_backend(self):
+            return self._backend in ("python", BACKEND)
+
+    kwargs.setdefault("backend", BACKEND)
+    kwargs.setdefault("is_gpu_simulation", True)
+    return GB300ExecutionOptions(**kwargs)

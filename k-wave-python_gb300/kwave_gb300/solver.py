@@ -1,0 +1,258 @@
+"""GB300 counterpart of ``kwave.solvers.kspace_solver.Simulation``.
+
+Same constructor arguments, same ``setup() / step() / run()`` split and the
+same result dictionary as the reference class (kwave/solvers/kspace_solver.py
+:122-778); the time loop runs on the GPU through libkwave_gb300 (ctypes).  The
+arithmetic type is float32; the sensor series and running aggregates stay on
+the device until ``run()`` returns.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+
+import numpy as np
+
+from . import _lib as K
+from .precompute import AXES, Setup, build_setup, problem_from_kwave
+
+_TABLES = {"k": K.KW_T_K, "pml": K.KW_T_PML, "pml_sg": K.KW_T_PMLSG, "op_grad": K.KW_T_OPGRAD,
+           "op_div": K.KW_T_OPDIV, "unstag": K.KW_T_UNSTAG}
+_FIELDS = {"c0": K.KW_F_C0, "rho0": K.KW_F_RHO0, "dtrsg0": K.KW_F_DTRSG0, "dtrsg1": K.KW_F_DTRSG1,
+           "dtrsg2": K.KW_F_DTRSG2, "BonA": K.KW_F_BONA, "tau": K.KW_F_TAU, "eta": K.KW_F_ETA, "p0": K.KW_F_P0}
+
+
+def _series_id(key, ndim):
+    if key == "p":
+        return K.KW_R_P
+    for i, a in enumerate(AXES[:ndim]):
+        if key == f"u{a}_staggered":
+            return K.KW_R_UX_ST + i
+        if key == f"u{a}":
+            return K.KW_R_UX + i
+    return None
+
+
+class DevicePlan:
+    """Owns one kw_plan (device state of one simulation)."""
+
+    def __init__(self, S: Setup, stream=None):
+        lib = K.lib()
+        K.require_device()
+        self.S = S
+        self.lib = lib
+        self.stream = stream
+        d = K.KwGridDesc()
+        d.ndim = S.ndim
+        for a in range(3):
+            d.shape[a] = S.shape[a] if a < S.ndim else 1
+            d.spacing[a] = S.spacing[a] if a < S.ndim else 1.0
+        d.Nt = S.Nt
+        d.record_start = S.record_start
+        d.dt = S.dt
+        d.c_ref = S.c_ref
+        d.use_sg = int(S.use_sg)
+        d.use_kspace = int(S.use_kspace)
+        d.absorb_mode = S.absorb_mode
+        d.dispersion = S.dispersion
+        d.nonlinear = S.nonlinear
+        d.alpha_power = S.alpha_power
+        self._h = C.c_void_p()
+        K.check(lib.kw_plan_create(C.byref(d), C.byref(self._h)))
+        try:
+            self._upload()
+            K.check(lib.kw_plan_finalize(self._h))
+        except BaseException:
+            lib.kw_plan_destroy(self._h)
+            self._h = None
+            raise
+
+    def _upload(self):
+        S, lib, h = self.S, self.lib, self._h
+        for name, fid in _FIELDS.items():
+            v = S.fields.get(name)
+            if v is None:
+                continue
+            if isinstance(v, float):
+                K.check(lib.kw_plan_set_field(h, fid, None, 0, C.c_float(v)))
+            else:
+                a = np.ascontiguousarray(v, dtype=np.float32).ravel()
+                K.check(lib.kw_plan_set_field(h, fid, K.ptr(a), a.size, C.c_float(0.0)))
+        for (name, axis), tb in S.tables.items():
+            a = np.ascontiguousarray(tb, dtype=np.float32)
+            K.check(lib.kw_plan_set_table(h, _TABLES[name], axis, K.ptr(a), a.size))
+        for src in S.sources:
+            idx = np.ascontiguousarray(src.index, dtype=np.int64)
+            sig = np.ascontiguousarray(src.signal, dtype=np.float32)
+            K.check(lib.kw_plan_set_source(h, src.slot, K.SRC_MODES[src.mode], K.ptr(idx), idx.size, K.ptr(sig),
+                                           sig.shape[0], sig.shape[1]))
+        mask = 0
+        for key in S.record:
+            sid = _series_id(key, S.ndim)
+            if sid is not None:
+                mask |= 1 << sid
+        slots = np.ascontiguousarray(S.slots, dtype=np.int64)
+        self.record_mask = mask
+        K.check(lib.kw_plan_set_sensor(h, K.ptr(slots), slots.size, mask))
+        if S.sensor_kind == "cartesian":
+            sl = np.ascontiguousarray(S.interp_slot, dtype=np.int32)
+            w = np.ascontiguousarray(S.interp_w, dtype=np.float64)
+            K.check(lib.kw_plan_set_sensor_interp(h, sl.shape[0], sl.shape[1], K.ptr(sl), K.ptr(w)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def run(self, nsteps):
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        K.check(self.lib.kw_plan_run(self._h, int(nsteps), st))
+
+    def sync(self):
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        K.check(self.lib.kw_plan_sync(self._h, st))
+
+    def time_index(self):
+        t = C.c_int32()
+        K.check(self.lib.kw_plan_time_index(self._h, C.byref(t)))
+        return t.value
+
+    def read_series(self, sid):
+        n_rec = self.S.Nt - self.S.record_start
+        out = np.empty((self.S.n_points, n_rec), np.float32)
+        K.check(self.lib.kw_plan_read_series(self._h, sid, K.ptr(out), out.size))
+        return out
+
+    def read_aggregate(self, sid, kind):
+        out = np.empty(self.S.n_points, np.float32)
+        K.check(self.lib.kw_plan_read_aggregate(self._h, sid, kind, K.ptr(out), out.size))
+        return out
+
+    def read_field(self, fid):
+        out = np.empty(self.S.shape, np.float32)
+        K.check(self.lib.kw_plan_read_field(self._h, fid, K.ptr(out), out.size))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kw_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Simulation:
+    """GB300 k-space pseudospectral propagator with the reference's interface.
+
+    ``Simulation(kgrid, medium, source, sensor, *, device, use_sg, use_kspace,
+    smooth_p0, pml_size, pml_alpha, quiet, dtype).run()`` mirrors
+    kwave/solvers/kspace_solver.py:135-203; ``device`` is accepted for
+    signature compatibility and must be "gpu" (there is no CPU path).
+    """
+
+    def __init__(self, kgrid, medium, source, sensor, *, device="gpu", use_sg=True, use_kspace=True, smooth_p0=True,
+                 pml_size=None, pml_alpha=None, quiet=False, dtype=None, stream=None):
+        if device not in ("gpu", "cuda", "auto"):
+            raise ValueError(f"Unknown device {device!r}. The GB300 backend runs on the GPU only.")
+        if dtype is not None and np.dtype(dtype) != np.float32:
+            raise NotImplementedError("the GB300 backend computes in float32 (dtype=np.float32)")
+        if pml_size is None and hasattr(kgrid, "N"):
+            warnings.warn("Simulation received a kWaveGrid without explicit pml_size; PML will be disabled.",
+                          UserWarning, stacklevel=2)
+        self.prob = problem_from_kwave(kgrid, medium, source, sensor, pml_size=pml_size, pml_alpha=pml_alpha,
+                                       use_sg=use_sg, use_kspace=use_kspace, smooth_p0=smooth_p0)
+        self.quiet = quiet
+        self.stream = stream
+        self._plan = None
+        self.t = 0
+
+    @classmethod
+    def from_problem(cls, prob, stream=None):
+        obj = cls.__new__(cls)
+        obj.prob = dict(prob)
+        obj.quiet = True
+        obj.stream = stream
+        obj._plan = None
+        obj.t = 0
+        return obj
+
+    # -- setup / stepping ---------------------------------------------------
+    def setup(self):
+        self.S = build_setup(self.prob)
+        unsupported = [k for k in self.S.record if k.startswith("I") or k in ("ux", "uy", "uz")]
+        if unsupported:
+            raise NotImplementedError(f"recording {sorted(unsupported)} is not available on the GB300 backend yet")
+        self._plan = DevicePlan(self.S, stream=self.stream)
+        self.t = 0
+        return self
+
+    @property
+    def Nt(self):
+        return self.S.Nt
+
+    def step(self):
+        if self._plan is None:
+            self.setup()
+        if self.t < self.S.Nt:
+            self._plan.run(1)
+            self.t = self._plan.time_index()
+        return self
+
+    def run(self):
+        if self._plan is None:
+            self.setup()
+        self._plan.run(self.S.Nt - self.t)
+        self._plan.sync()
+        self.t = self._plan.time_index()
+        return self.results()
+
+    # -- fields (host copies) -------------------------------------------------
+    @property
+    def p(self):
+        return self._plan.read_field(K.KW_FLD_P)
+
+    @property
+    def u(self):
+        return [self._plan.read_field(K.KW_FLD_U0 + i) for i in range(self.S.ndim)]
+
+    @property
+    def rho_split(self):
+        return [self._plan.read_field(K.KW_FLD_RHO0 + i) for i in range(self.S.ndim)]
+
+    # -- results (kspace_solver.py:763-778) --------------------------------------
+    def results(self):
+        S, plan = self.S, self._plan
+        out = {}
+        for key in sorted(S.record):
+            sid = _series_id(key, S.ndim)
+            if sid is None:
+                continue
+            if key in S.requested:
+                out[key] = plan.read_series(sid)
+            for suf, kind in (("_max", K.KW_AGG_MAX), ("_min", K.KW_AGG_MIN), ("_rms", K.KW_AGG_RMS)):
+                if key + suf in S.requested:
+                    out[key + suf] = plan.read_aggregate(sid, kind)
+        interior = tuple(slice(s, N - s if s else None) for s, N in zip(S.pml_sizes, S.shape))
+        if "p_final" in S.requested:
+            out["p_final"] = plan.read_field(K.KW_FLD_P)[interior].copy()
+        for i, a in enumerate(AXES[: S.ndim]):
+            if f"u{a}_final" in S.requested:
+                out[f"u{a}_final"] = plan.read_field(K.KW_FLD_U0 + i)[interior].copy()
+        return {k: v for k, v in out.items() if k in S.requested}
+
+    def close(self):
+        if self._plan is not None:
+            self._plan.close()
+            self._plan = None
+
+
+def run_problem(prob, stream=None):
+    """Set up, run and close one simulation described by a plain problem dict."""
+    sim = Simulation.from_problem(prob, stream=stream)
+    try:
+        return sim.run()
+    finally:
+        sim.close()
