@@ -1,6 +1,53 @@
-"""Benchmark: k-space first-order time loop on one GB300 (placeholder; generators only)."""
+"""Benchmark of the GB300 k-space first-order time loop.
+
+Workload (the headline configuration): 3-D heterogeneous absorbing IVP on a
+256^3 grid including a 10-point PML, dx = 0.1 mm, power-law absorption
+(0.75 dB/(MHz^y cm), y = 1.5), B/A = 6, 8 random ellipsoids, 20 Gaussian p0
+blobs, a binary sensor on the z = 20 plane recording p and p_max; seeded
+synthetic inputs of those shapes.
+
+A bench "step" is one time step of that simulation over the whole grid
+(16.8 M cells).  ``value`` = cells x timed steps / device time (CUDA events on
+the launching stream), state resident in HBM.  ``e2e`` = the same metric
+through the public bridge (``run_gb300_backend``, the kspaceFirstOrder3D
+path) for a full 1000-step simulation from host numpy inputs to host results,
+host set-up and host<->device copies included.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the reference's CPU implementation of the same
+workload (the oracle restatement, bit-identical to kwave's native NumPy
+solver) on a bounded sample of time steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+from types import SimpleNamespace
+
 import numpy as np
 
+ROOT = Path(__file__).resolve().parent
+for _p in (str(ROOT), str(ROOT / "k-wave-python_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Mcell-steps/s vs native solver; time to 1% p0 error, learned+adjoint vs plain"
+UNIT = "Mcell-steps/s"
+WORKLOAD = ("3-D heterogeneous absorbing IVP, 256^3 incl. 10-pt PML, dx=0.1 mm, 1000 steps, "
+            "power law 0.75 dB/(MHz^y cm) y=1.5, B/A=6, 8 ellipsoids, 20 p0 blobs, z=20 plane sensor p+p_max")
+A_MODEL_BYTES_PER_CELL_STEP = 168  # algorithmic bytes per cell-step of this configuration
+
+
+# ---------------------------------------------------------------------------
+# synthetic workloads
+# ---------------------------------------------------------------------------
 
 def _random_rotation(rng):
     q, r = np.linalg.qr(rng.standard_normal((3, 3)))
@@ -55,3 +102,310 @@ def config2_problem(n=256, nt=1000, seed=0, plane_z=20, pml=10):
                 alpha_coeff=0.75, alpha_power=1.5, BonA=6.0, p0=p0, smooth_p0=True,
                 sensor_mask=mask, record=("p", "p_max"), pml_size=(pml,) * 3, pml_alpha=(2.0,) * 3,
                 use_sg=True, use_kspace=True)
+
+
+def kwave_objects(prob):
+    """The same problem as the objects the legacy kspaceFirstOrder3D call takes."""
+    kgrid = SimpleNamespace(N=np.array(prob["shape"]), spacing=np.array(prob["spacing"]), Nt=prob["Nt"], dt=prob["dt"],
+                            dim=len(prob["shape"]))
+    medium = SimpleNamespace(sound_speed=prob["sound_speed"], density=prob["density"], alpha_coeff=prob["alpha_coeff"],
+                             alpha_power=prob["alpha_power"], alpha_mode=None, BonA=prob["BonA"])
+    source = SimpleNamespace(p0=prob["p0"])
+    sensor = SimpleNamespace(mask=prob["sensor_mask"], record=prob["record"], record_start_index=1)
+    opts = SimpleNamespace(pml_size=prob["pml_size"], pml_alpha=prob["pml_alpha"], use_sg=True, use_kspace=True,
+                           smooth_p0=prob["smooth_p0"])
+    return kgrid, medium, source, sensor, opts
+
+
+# ---------------------------------------------------------------------------
+# measurement helpers
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+        return False
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def launch_bytes(S):
+    """Algorithmic bytes per launch of each kernel class for a set-up problem:
+    every array a launch must read or write, counted once (fp32 reals, complex64
+    half spectra)."""
+    D = S.ndim
+    ntot = int(np.prod(S.shape))
+    L = S.shape[-1]
+    H = L // 2 + 1
+    Hp = H + (H & 1)
+    spec = (ntot // L) * Hp * 8
+    real = ntot * 4
+    grid = lambda name: isinstance(S.fields.get(name), np.ndarray)  # noqa: E731
+    powerlaw = S.absorb_mode == 1
+    nb = 1 + S.dispersion
+    by = {}
+    # axis passes with operators: grad (1 in, D out), div (D in, D out), fractional Laplacians (nb in/out)
+    ops = [(1 + D) * spec, 2 * D * spec] + ([2 * nb * spec] if powerlaw else [])
+    by["axis_ops"] = sum(ops) / len(ops)
+    plain = [2 * D * spec, 2 * D * spec, 2 * D * spec] + ([2 * nb * spec, 2 * nb * spec] if powerlaw else []) + [2 * spec]
+    by["axis_plain"] = sum(plain) / len(plain) if D == 3 else 0.0
+    by["rows_u"] = D * (2 * spec + 2 * real) + sum(real for a in range(D) if grid(f"dtrsg{a}"))
+    rho = D * (spec + 2 * real) + (real if grid("rho0") else 0)
+    if powerlaw:
+        rho += real + nb * spec
+    else:
+        rho += spec + (real if grid("c0") else 0) + (real if grid("BonA") else 0)
+    by["rows_rho"] = rho
+    eos = nb * spec + real + spec
+    for name in ("c0", "tau", "eta", "rho0", "BonA"):
+        if grid(name) and (name != "eta" or S.dispersion) and (name not in ("rho0", "BonA") or S.nonlinear):
+            eos += real
+    by["rows_eos"] = eos if powerlaw else 0.0
+    return by
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline_sample(n=256, steps=1):
+    """Oracle (the reference's CPU implementation, restated) on the same
+    workload: set-up and the t=0 step untimed, then ``steps`` timed steps."""
+    from oracle.kspace_oracle import OracleSimulation
+
+    prob = config2_problem(n=n, nt=1 + steps)
+    sim = OracleSimulation(prob, dtype=np.float32).setup()
+    sim.step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    dt = time.perf_counter() - t0
+    return n ** 3 * steps / dt / 1e6, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    steps = max(1, min(args.steps, 3))
+    value, secs = cpu_baseline_sample(args.n, steps)
+    cpu = {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+           "sample": f"{steps} time step(s) of the 256^3 workload after set-up and the t=0 step ({secs:.1f} s); "
+                     "NumPy pocketfft is single-threaded, so the reference path uses one core "
+                     f"(host has {os.cpu_count()})"}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+            "warmup": 1, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, shapes of the named workload)",
+            "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "l2": "inputs larger than L2"},
+            "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300 import _lib as K
+    from kwave_gb300.backend import run_gb300_backend
+    from kwave_gb300.precompute import build_setup
+    from kwave_gb300.solver import DevicePlan
+
+    n = args.n
+    K_steps, W = args.steps, args.warmup
+    nt = max(1000, K_steps + W)
+    prob = config2_problem(n=n, nt=nt, seed=rank)
+    S = build_setup(prob)
+    stream = torch.cuda.current_stream()
+    plan = DevicePlan(S, stream=stream.cuda_stream)
+    lib = K.lib()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # warm-up (includes the t = 0 initial-condition step)
+    plan.run(W)
+    torch.cuda.synchronize()
+    cnt0 = C_int64()
+    lib.kw_plan_launch_count(plan.handle, ctypes.byref(cnt0))
+    K.check(lib.kw_plan_set_timing(plan.handle, 1))
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        plan.run(K_steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    cnt1 = C_int64()
+    lib.kw_plan_launch_count(plan.handle, ctypes.byref(cnt1))
+    kms = (ctypes.c_double * 6)()
+    kcnt = (ctypes.c_int64 * 6)()
+    K.check(lib.kw_plan_read_timing(plan.handle, kms, kcnt))
+    K.check(lib.kw_plan_set_timing(plan.handle, 0))
+    ms_max = ms
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(t.item())
+    cells = int(np.prod(S.shape))
+    value = ws * cells * K_steps / (ms_max / 1e3) / 1e6
+
+    # roofline of the dominant kernel class (algorithmic bytes / average launch time)
+    names = K.KW_K_NAMES
+    by = launch_bytes(S)
+    dom = max(range(6), key=lambda i: kms[i])
+    avg_ms = kms[dom] / max(kcnt[dom], 1)
+    peak, peak_kind = measured_peaks()
+    achieved = by.get(names[dom], 0.0) / (avg_ms / 1e3) / 1e9
+    kernels = {names[i]: {"launches": int(kcnt[i]), "ms_total": kms[i], "share": kms[i] / max(sum(kms), 1e-30),
+                          "alg_bytes_per_launch": by.get(names[i], 0.0),
+                          "gbs": (by.get(names[i], 0.0) / (kms[i] / max(kcnt[i], 1) / 1e3) / 1e9) if kcnt[i] else None}
+               for i in range(6) if kcnt[i]}
+    step_gbs = A_MODEL_BYTES_PER_CELL_STEP * cells * K_steps / (ms / 1e3) / 1e9
+    plan.close()
+    del plan
+
+    # end to end through the public bridge (host inputs -> host results), one full simulation
+    e2e = None
+    if not args.no_e2e:
+        prob_e2e = config2_problem(n=n, nt=1000, seed=rank)
+        kg, med, src, sen, opts = kwave_objects(prob_e2e)
+        from kwave_gb300.solver import STATS
+
+        torch.cuda.synchronize()
+        barrier()
+        STATS["d2h_bytes"] = 0
+        t0 = time.perf_counter()
+        res = run_gb300_backend(kg, med, src, sen, opts)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        assert set(res) == {"p", "p_max"}
+        h2d, d2h = STATS["h2d_bytes"], STATS["d2h_bytes"]
+        e2e = {"value": cells * 1000 / (t1 - t0) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d / 1000,
+               "d2h_bytes_per_step": d2h / 1000, "seconds": t1 - t0}
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline:
+        cv, secs = cpu_baseline_sample(256, 1)
+        cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"1 time step of the 256^3 workload after set-up and the t=0 step ({secs:.1f} s), "
+                         "oracle restatement (bit-identical to kwave's native NumPy solver), single-threaded"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K_steps, "warmup": W,
+        "ms_per_step": ms_max / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded ellipsoids and Gaussian blobs with the named shapes and ranges)",
+        "config": {"workload": WORKLOAD, "grid": list(S.shape), "nt": nt, "timed_steps": f"{W}..{W + K_steps - 1}",
+                   "l2": "inputs larger than L2 (state + medium ~1.1 GB per step)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
+        "step_roofline": {"model_bytes_per_cell_step": A_MODEL_BYTES_PER_CELL_STEP, "achieved": step_gbs,
+                          "peak": peak, "frac": step_gbs / peak, "unit": "GB/s"},
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk.summary(),
+        "gpu_launches": int(cnt1.value - cnt0.value),
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+import ctypes  # noqa: E402
+
+C_int64 = ctypes.c_int64
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="grid edge (the headline workload is 256)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

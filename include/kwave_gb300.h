@@ -133,6 +133,21 @@ int32_t kw_plan_read_aggregate(kw_plan* plan, int32_t series, int32_t kind, floa
 int32_t kw_plan_read_field(kw_plan* plan, int32_t field, float* host, int64_t n);
 /* Device pointer of a field (valid until kw_plan_destroy). */
 int32_t kw_plan_field_device_ptr(kw_plan* plan, int32_t field, void** dptr);
+/* Zeroes the state and the recorded series and rewinds to t = 0, keeping the
+ * uploaded medium, sources and sensor (a fresh Simulation.setup()). */
+int32_t kw_plan_reset(kw_plan* plan);
+/* Launch classes for timing: axis pass with operators, plain axis pass, and
+ * the row stages INIT, U, RHO, EOS. */
+enum { KW_K_AXIS_OPS = 0, KW_K_AXIS_PLAIN = 1, KW_K_ROWS_INIT = 2, KW_K_ROWS_U = 3, KW_K_ROWS_RHO = 4,
+       KW_K_ROWS_EOS = 5, KW_K_NCLASS = 6 };
+/* enable != 0: bracket every launch with CUDA events on its stream (clears
+ * previous timings). */
+int32_t kw_plan_set_timing(kw_plan* plan, int32_t enable);
+/* Synchronises and returns, per launch class, the summed kernel time [ms] and
+ * the number of launches since timing was enabled (arrays of KW_K_NCLASS). */
+int32_t kw_plan_read_timing(kw_plan* plan, double* ms, int64_t* count);
+/* Number of kernels the plan has launched since creation. */
+int32_t kw_plan_launch_count(const kw_plan* plan, int64_t* count);
 /* Frees all device memory of the plan. */
 int32_t kw_plan_destroy(kw_plan* plan);
 

@@ -89,7 +89,37 @@ struct kw_plan {
   double* d_iw = nullptr;
   size_t smem_rows = 0, smem_axis_plain[3] = {0, 0, 0}, smem_axis_ops = 0;
   int T_axis[3] = {1, 1, 1};
+  // launch accounting / timing
+  long long launches = 0;
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, size_t>> ev_used;  // (class, index of start event)
+  size_t ev_next = 0;
 };
+
+// Bracket a launch with events when timing is on.
+static int ev_begin(kw_plan* p, cudaStream_t st, size_t* slot) {
+  if (!p->timing) return KW_OK;
+  if (p->ev_next + 2 > p->ev_pool.size()) {
+    for (int i = 0; i < 256; ++i) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      p->ev_pool.push_back(e);
+    }
+  }
+  *slot = p->ev_next;
+  p->ev_next += 2;
+  CK(cudaEventRecord(p->ev_pool[*slot], st));
+  return KW_OK;
+}
+
+static int ev_end(kw_plan* p, cudaStream_t st, int cls, size_t slot) {
+  p->launches++;
+  if (!p->timing) return KW_OK;
+  CK(cudaEventRecord(p->ev_pool[slot + 1], st));
+  p->ev_used.push_back({cls, slot});
+  return KW_OK;
+}
 
 static bool factor_len(int n, KwFftLen& f) {
   f.n = n;
@@ -293,6 +323,19 @@ static int build_csr(kw_plan* p, const std::vector<long long>& idx, int** d_rowp
   return upload(p, d_ent, ent.data(), ent.size());
 }
 
+static int zero_state(kw_plan* p) {
+  for (int a = 0; a < p->D; ++a) {
+    CK(cudaMemset(p->d_u[a], 0, p->ntot * sizeof(float)));
+    CK(cudaMemset(p->d_rho[a], 0, p->ntot * sizeof(float)));
+  }
+  CK(cudaMemset(p->d_p, 0, p->ntot * sizeof(float)));
+  for (int b = 0; b < 4; ++b)
+    if (p->d_S[b]) CK(cudaMemset(p->d_S[b], 0, p->spec_elems * sizeof(float2)));
+  for (int s = 0; s < 7; ++s)
+    if (p->d_rec[s]) CK(cudaMemset(p->d_rec[s], 0, (size_t)p->nrec * p->nslots * sizeof(float)));
+  return KW_OK;
+}
+
 int32_t kw_plan_finalize(kw_plan* p) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");
   if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
@@ -382,14 +425,7 @@ int32_t kw_plan_finalize(kw_plan* p) {
     if ((rc = upload(p, &p->d_islot, p->interp_slot.data(), p->interp_slot.size()))) return rc;
     if ((rc = upload(p, &p->d_iw, p->interp_w.data(), p->interp_w.size()))) return rc;
   }
-  // zero state
-  for (int a = 0; a < D; ++a) {
-    CK(cudaMemset(p->d_u[a], 0, p->ntot * sizeof(float)));
-    CK(cudaMemset(p->d_rho[a], 0, p->ntot * sizeof(float)));
-  }
-  CK(cudaMemset(p->d_p, 0, p->ntot * sizeof(float)));
-  for (int b = 0; b < 4; ++b)
-    if (p->d_S[b]) CK(cudaMemset(p->d_S[b], 0, p->spec_elems * sizeof(float2)));
+  if ((rc = zero_state(p))) return rc;
 
   // launch geometry
   p->R = (p->L >= 2048) ? 1 : 2048 / p->L;
@@ -464,7 +500,7 @@ static void fill_rows(const kw_plan* p, RowsParams& P) {
   for (int s = 0; s < 7; ++s) P.rec[s] = p->d_rec[s];
 }
 
-static int launch_rows(const kw_plan* p, int stage, int init, int t, int write_p, cudaStream_t st) {
+static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cudaStream_t st) {
   RowsParams P;
   fill_rows(p, P);
   P.stage = stage;
@@ -473,9 +509,12 @@ static int launch_rows(const kw_plan* p, int stage, int init, int t, int write_p
   P.rec_row = (t >= p->g.record_start) ? t - p->g.record_start : -1;
   P.write_p = write_p;
   const int grid = (p->nrows + p->R - 1) / p->R;
+  size_t slot = 0;
+  int rc = ev_begin(p, st, &slot);
+  if (rc) return rc;
   k_rows<<<grid, kThreads, p->smem_rows, st>>>(P);
   CK(cudaGetLastError());
-  return KW_OK;
+  return ev_end(p, st, KW_K_ROWS_INIT + stage, slot);
 }
 
 static void fill_axis_geom(const kw_plan* p, int axis, AxisParams& A) {
@@ -505,19 +544,22 @@ static void fill_axis_geom(const kw_plan* p, int axis, AxisParams& A) {
   }
 }
 
-static int launch_axis_plain(const kw_plan* p, int axis, int inv, const int* bufs, int nb, cudaStream_t st) {
+static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int nb, cudaStream_t st) {
   AxisParams A;
   fill_axis_geom(p, axis, A);
   A.mode = inv ? 1 : 0;
   for (int i = 0; i < nb; ++i) A.plain[i] = bufs[i];
   const int nouter = (p->D == 3 && axis == 1) ? p->N[0] : 1;
   dim3 grid((A.ncols + A.T - 1) / A.T, nouter, nb);
+  size_t slot = 0;
+  int rc = ev_begin(p, st, &slot);
+  if (rc) return rc;
   k_axis<<<grid, kThreads, p->smem_axis_plain[axis], st>>>(A);
   CK(cudaGetLastError());
-  return KW_OK;
+  return ev_end(p, st, KW_K_AXIS_PLAIN, slot);
 }
 
-static int launch_axis_ops(const kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t st) {
+static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t st) {
   AxisParams A;
   fill_axis_geom(p, 0, A);
   A.mode = 2;
@@ -535,9 +577,12 @@ static int launch_axis_ops(const kw_plan* p, const AxisJob* jobs, int nj, cudaSt
   A.pow2 = (float)(p->g.alpha_power - 1.0);
   A.scale = (float)(1.0 / (double)p->ntot);
   dim3 grid((A.ncols + A.T - 1) / A.T, 1, 1);
+  size_t slot = 0;
+  int rc = ev_begin(p, st, &slot);
+  if (rc) return rc;
   k_axis<<<grid, kThreads, p->smem_axis_ops, st>>>(A);
   CK(cudaGetLastError());
-  return KW_OK;
+  return ev_end(p, st, KW_K_AXIS_OPS, slot);
 }
 
 static int enqueue_step(kw_plan* p, int t, bool last, cudaStream_t st) {
@@ -702,8 +747,50 @@ int32_t kw_plan_field_device_ptr(kw_plan* p, int32_t field, void** dptr) {
   return KW_OK;
 }
 
+int32_t kw_plan_reset(kw_plan* p) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (!p->finalized) return fail(KW_ERR_STATE, "plan not finalized");
+  CK(cudaDeviceSynchronize());
+  int rc = zero_state(p);
+  if (rc) return rc;
+  CK(cudaDeviceSynchronize());
+  p->t = 0;
+  return KW_OK;
+}
+
+int32_t kw_plan_set_timing(kw_plan* p, int32_t enable) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  p->timing = enable != 0;
+  p->ev_used.clear();
+  p->ev_next = 0;
+  return KW_OK;
+}
+
+int32_t kw_plan_read_timing(kw_plan* p, double* ms, int64_t* count) {
+  if (!p || !ms || !count) return fail(KW_ERR_INVALID, "null argument");
+  for (int c = 0; c < KW_K_NCLASS; ++c) {
+    ms[c] = 0.0;
+    count[c] = 0;
+  }
+  if (!p->ev_used.empty()) CK(cudaEventSynchronize(p->ev_pool[p->ev_used.back().second + 1]));
+  for (auto& u : p->ev_used) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, p->ev_pool[u.second], p->ev_pool[u.second + 1]));
+    ms[u.first] += t;
+    count[u.first] += 1;
+  }
+  return KW_OK;
+}
+
+int32_t kw_plan_launch_count(const kw_plan* p, int64_t* count) {
+  if (!p || !count) return fail(KW_ERR_INVALID, "null argument");
+  *count = p->launches;
+  return KW_OK;
+}
+
 int32_t kw_plan_destroy(kw_plan* p) {
   if (!p) return KW_OK;
+  for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   for (void* a : p->allocs) cudaFree(a);
   delete p;
   return KW_OK;

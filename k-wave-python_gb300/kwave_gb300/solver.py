@@ -33,6 +33,9 @@ def _series_id(key, ndim):
     return None
 
 
+STATS = {"h2d_bytes": 0, "d2h_bytes": 0}
+
+
 class DevicePlan:
     """Owns one kw_plan (device state of one simulation)."""
 
@@ -69,6 +72,7 @@ class DevicePlan:
 
     def _upload(self):
         S, lib, h = self.S, self.lib, self._h
+        nbytes = 0
         for name, fid in _FIELDS.items():
             v = S.fields.get(name)
             if v is None:
@@ -77,13 +81,16 @@ class DevicePlan:
                 K.check(lib.kw_plan_set_field(h, fid, None, 0, C.c_float(v)))
             else:
                 a = np.ascontiguousarray(v, dtype=np.float32).ravel()
+                nbytes += a.nbytes
                 K.check(lib.kw_plan_set_field(h, fid, K.ptr(a), a.size, C.c_float(0.0)))
         for (name, axis), tb in S.tables.items():
             a = np.ascontiguousarray(tb, dtype=np.float32)
+            nbytes += a.nbytes
             K.check(lib.kw_plan_set_table(h, _TABLES[name], axis, K.ptr(a), a.size))
         for src in S.sources:
             idx = np.ascontiguousarray(src.index, dtype=np.int64)
             sig = np.ascontiguousarray(src.signal, dtype=np.float32)
+            nbytes += idx.nbytes + sig.nbytes
             K.check(lib.kw_plan_set_source(h, src.slot, K.SRC_MODES[src.mode], K.ptr(idx), idx.size, K.ptr(sig),
                                            sig.shape[0], sig.shape[1]))
         mask = 0
@@ -92,12 +99,16 @@ class DevicePlan:
             if sid is not None:
                 mask |= 1 << sid
         slots = np.ascontiguousarray(S.slots, dtype=np.int64)
+        nbytes += slots.nbytes
         self.record_mask = mask
         K.check(lib.kw_plan_set_sensor(h, K.ptr(slots), slots.size, mask))
         if S.sensor_kind == "cartesian":
             sl = np.ascontiguousarray(S.interp_slot, dtype=np.int32)
             w = np.ascontiguousarray(S.interp_w, dtype=np.float64)
+            nbytes += sl.nbytes + w.nbytes
             K.check(lib.kw_plan_set_sensor_interp(h, sl.shape[0], sl.shape[1], K.ptr(sl), K.ptr(w)))
+        self.h2d_bytes = nbytes
+        STATS["h2d_bytes"] = nbytes
 
     @property
     def handle(self):
@@ -120,16 +131,19 @@ class DevicePlan:
         n_rec = self.S.Nt - self.S.record_start
         out = np.empty((self.S.n_points, n_rec), np.float32)
         K.check(self.lib.kw_plan_read_series(self._h, sid, K.ptr(out), out.size))
+        STATS["d2h_bytes"] += out.nbytes
         return out
 
     def read_aggregate(self, sid, kind):
         out = np.empty(self.S.n_points, np.float32)
         K.check(self.lib.kw_plan_read_aggregate(self._h, sid, kind, K.ptr(out), out.size))
+        STATS["d2h_bytes"] += out.nbytes
         return out
 
     def read_field(self, fid):
         out = np.empty(self.S.shape, np.float32)
         K.check(self.lib.kw_plan_read_field(self._h, fid, K.ptr(out), out.size))
+        STATS["d2h_bytes"] += out.nbytes
         return out
 
     def close(self):
