@@ -148,6 +148,26 @@ int32_t kw_plan_set_timing(kw_plan* plan, int32_t enable);
 int32_t kw_plan_read_timing(kw_plan* plan, double* ms, int64_t* count);
 /* Number of kernels the plan has launched since creation. */
 int32_t kw_plan_launch_count(const kw_plan* plan, int64_t* count);
+/* Spectral derivative along `axis` without any device allocation (no
+ * counterpart in the reference; it computes what Simulation._diff(f,
+ * op_grad_list[axis]) computes, kwave/solvers/kspace_solver.py:781-796 with the
+ * operator of :440-447):
+ *     out = Re F^-1[ kappa(|k|) (i k_a e^{+i k_a d_a/2}) F[f] ],
+ *     kappa = sin(kappa_coef |k|) / (kappa_coef |k|)  (kappa_coef = c_ref dt / 2; 0 gives kappa = 1),
+ * with the shift factor dropped when use_sg == 0.  f and out are caller-owned
+ * device buffers of N_total float32 (C order).
+ * For callers that cannot let a library allocate device memory: custom
+ * operators of frameworks that own all device memory (PyTorch, JAX/XLA,
+ * TensorRT plugins) and real-time pipelines that forbid allocation once
+ * running.  The half-spectrum scratch is a static 16 MiB device array
+ * (2,097,152 complex values; about 2040^2 in 2-D or 128^3 in 3-D), held by every
+ * GPU that loads the library until exit; larger grids return
+ * KW_ERR_UNSUPPORTED.  The first call on a device resolves the array's address
+ * and sets kernel attributes (make it before any stream capture).  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised
+ * by the caller.  Work is enqueued on `stream` (NULL = default stream). */
+int32_t kw_gradient_noalloc(const float* f, float* out, int32_t ndim, const int32_t* shape, const double* spacing,
+                            int32_t axis, double kappa_coef, int32_t use_sg, void* stream);
 /* Frees all device memory of the plan. */
 int32_t kw_plan_destroy(kw_plan* plan);
 

@@ -28,6 +28,9 @@ static int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+// Lets other translation units of the library report through kw_last_error().
+int kw_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+
 #define CK(call)                                                                              \
   do {                                                                                        \
     cudaError_t e_ = (call);                                                                  \

@@ -84,6 +84,7 @@ _PROTOS = {
     "kw_plan_set_timing": (C.c_int32, [_P, C.c_int32]),
     "kw_plan_read_timing": (C.c_int32, [_P, _P, _P]),
     "kw_plan_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
+    "kw_gradient_noalloc": (C.c_int32, [_P, _P, C.c_int32, _P, _P, C.c_int32, C.c_double, C.c_int32, _P]),
     "kw_plan_destroy": (C.c_int32, [_P]),
 }
 KW_K_NAMES = ("axis_ops", "axis_plain", "rows_init", "rows_u", "rows_rho", "rows_eos")
