@@ -1,0 +1,373 @@
+// Persistent, warp-specialised strided-axis FFT pass (power-of-two lengths).
+//
+// One CTA per SM.  Warp 8 is the producer: its elected lane streams tiles of
+// T columns x N points of a spectral buffer into a ring of NST shared-memory
+// stages with TMA (cp.async.bulk.tensor, box T x min(N,256)), completion
+// tracked by "full" mbarriers.  Warps 0-7 are consumers: they copy a stage
+// into registers, release it on its "empty" mbarrier, run the register FFT
+// (kw_regfft.cuh), apply the spectral operators and store the results with
+// coalesced global stores.  Loads therefore run NST tiles ahead of compute.
+//
+// Work units: in operator mode one unit is a tile and its items are the
+// distinct input buffers of the jobs; in plain mode one unit is (buffer,
+// outer index, tile).  Producer and consumers walk the same unit/item sequence.
+//
+// All mbarrier waits are bounded (2 s).  A timeout sets g_kw_device_error,
+// the consumers agree on it through a reducing barrier and leave together,
+// and thread 0 waits (bounded) for loads still in flight before the CTA exits.
+#include <cstdlib>
+
+#include "kw_kernels.cuh"
+#include "kw_regfft.cuh"
+#include "kw_tma.cuh"
+
+__device__ int g_kw_device_error;
+
+namespace {
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+struct TmaMaps {
+  CUtensorMap m[4];  // one per spectral buffer S0, S1, S2, P for the pass's axis
+};
+
+struct TmaWork {
+  int ntile;   // column tiles per outer block
+  int nouter;  // outer blocks (x planes for the 3-D y pass)
+  int nunits;
+  int nitems;  // items per unit
+  int inp[4];  // operator mode: distinct input buffers in job order
+};
+
+__device__ __forceinline__ bool consumers_any(bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, 1, 256, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred)
+      : "memory");
+  return r != 0;
+}
+
+__device__ __forceinline__ float kappa_of(const AxisParams& A, float kmag) {
+  if (!A.use_kspace) return 1.f;
+  return kwreg::sinc_taylor(A.kcoef * kmag);
+}
+
+__device__ __forceinline__ float kmag_of(const AxisParams& A, int x, const ColK& g) {
+  const float kx = A.k[0][x];
+  float kk = __fadd_rn(__fmul_rn(kx, kx), g.ky2);
+  if (A.ndim == 3) kk = __fadd_rn(kk, g.kz2);
+  return sqrtf(kk);
+}
+
+}  // namespace
+
+template <int E, int P, int NST, int MINB>
+__global__ void __launch_bounds__(288, MINB)
+    k_axis_tma(const __grid_constant__ AxisParams A, const __grid_constant__ TmaMaps maps, const TmaWork W) {
+  constexpr int N = E * P, T = 256 / P, RS = N + E + 1;
+  constexpr uint32_t kStageBytes = N * T * sizeof(float2);
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float2* stages = reinterpret_cast<float2*>(smem_raw);  // NST * N * T
+  float2* ex = stages + (size_t)NST * N * T;             // T * RS
+  float2* tw = ex + (size_t)T * RS;                      // N
+  uint64_t* full = reinterpret_cast<uint64_t*>(tw + N);
+  uint64_t* empty = full + NST;
+  int* counters = reinterpret_cast<int*>(empty + NST);  // [0] issued, [1] consumed
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      kwtma::mbar_init(&full[s], 1);
+      kwtma::mbar_init(&empty[s], 8);
+    }
+    counters[0] = counters[1] = 0;
+    kwtma::fence_barrier_init();
+  }
+  for (int i = tid; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  __syncthreads();
+
+  const bool plain = A.mode < 2;
+  if (warp == 8) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; u < W.nunits && ok; u += gridDim.x) {
+        const int tile = u % W.ntile;
+        const int rest = u / W.ntile;
+        const int outer = rest % W.nouter;
+        const int b = rest / W.nouter;
+        for (int q = 0; q < W.nitems; ++q, ++it) {
+          const int buf = plain ? A.plain[b] : W.inp[q];
+          const uint32_t s = it % NST, k = it / NST;
+          if (k > 0 && !kwtma::mbar_wait(&empty[s], (k - 1) & 1, kWaitLimitNs)) {
+            atomicExch(&g_kw_device_error, 1);
+            ok = false;
+            break;
+          }
+          kwtma::mbar_arrive_expect_tx(&full[s], kStageBytes);
+          float2* dst = stages + (size_t)s * N * T;
+#pragma unroll
+          for (int n0 = 0; n0 < N; n0 += 256) kwtma::tma_load_3d(dst + n0 * T, &maps.m[buf], tile * T, n0, outer, &full[s]);
+        }
+      }
+      counters[0] = (int)it;
+    }
+  } else {
+    // ---------------- consumers ----------------
+    const int cc = tid % T, t = tid / T;
+    auto sync = [] __device__() { kwtma::named_sync(256); };
+    uint32_t it = 0;
+    bool aborted = false;
+    for (int u = blockIdx.x; u < W.nunits && !aborted; u += gridDim.x) {
+      const int tile = u % W.ntile;
+      const int rest = u / W.ntile;
+      const int outer = rest % W.nouter;
+      const int b = rest / W.nouter;
+      const int c0 = tile * T;
+      const bool act = cc < A.ncols - c0;
+      const long long base = (long long)outer * A.os + c0 + cc;
+      const long long xs = A.xs;
+      ColK g;
+      float kap[E];
+      if (!plain) {
+        g = col_geometry(A, act ? c0 + cc : c0);
+        bool need = false;
+        for (int j = 0; j < A.njobs; ++j) need |= (A.jobs[j].op == OP_GRAD || A.jobs[j].op == OP_DIV);
+        if (need) {
+#pragma unroll
+          for (int m = 0; m < E / P; ++m)
+#pragma unroll
+            for (int k2 = 0; k2 < P; ++k2) kap[m * P + k2] = kappa_of(A, kmag_of(A, t + P * m + E * k2, g));
+        }
+      }
+      for (int q = 0; q < W.nitems; ++q, ++it) {
+        const uint32_t s = it % NST, k = it / NST;
+        const bool got = kwtma::mbar_wait(&full[s], k & 1, kWaitLimitNs);
+        if (consumers_any(!got)) {
+          if (tid == 0) atomicExch(&g_kw_device_error, 2);
+          aborted = true;
+          break;
+        }
+        const float2* st = stages + (size_t)s * N * T;
+        float2 v[E];
+        if (plain && A.mode == 1) {
+#pragma unroll
+          for (int m = 0; m < E / P; ++m)
+#pragma unroll
+            for (int k2 = 0; k2 < P; ++k2) v[m * P + k2] = cconj(st[(t + P * m + E * k2) * T + cc]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < E; ++j) v[j] = st[(t + P * j) * T + cc];
+        }
+        __syncwarp();
+        if (lane == 0) kwtma::mbar_arrive(&empty[s]);
+
+        if (plain) {
+          float2* buf = A.bufs[A.plain[b]];
+          if (A.mode == 0) {
+            kwreg::Reg<E, P>::fwd(v, t, ex + cc * RS, 1, tw, sync);
+            if (act) {
+#pragma unroll
+              for (int m = 0; m < E / P; ++m)
+#pragma unroll
+                for (int k2 = 0; k2 < P; ++k2) buf[base + (t + P * m + E * k2) * xs] = v[m * P + k2];
+            }
+          } else {
+            kwreg::Reg<E, P>::rev(v, t, ex + cc * RS, 1, tw, sync);
+            if (act) {
+#pragma unroll
+              for (int j = 0; j < E; ++j) buf[base + (t + P * j) * xs] = cconj(v[j]);
+            }
+          }
+          continue;
+        }
+        // operator mode: forward FFT of this input, then every job reading it
+        kwreg::Reg<E, P>::fwd(v, t, ex + cc * RS, 1, tw, sync);
+        const int in = W.inp[q];
+        for (int jj = 0; jj < A.njobs; ++jj) {
+          const AxisJob J = A.jobs[jj];
+          if (J.in != in) continue;
+          float2 y[E];
+#pragma unroll
+          for (int m = 0; m < E / P; ++m)
+#pragma unroll
+            for (int k2 = 0; k2 < P; ++k2) {
+              const int x = t + P * m + E * k2;
+              const int r = m * P + k2;
+              float2 op;
+              const int ai = (J.axis == 0) ? x : (J.axis == 1 ? g.a1 : g.a2);
+              switch (J.op) {
+                case OP_GRAD:
+                case OP_DIV: {
+                  const float2 f = (J.op == OP_GRAD) ? A.fg[J.axis][ai] : A.fd[J.axis][ai];
+                  const float kp = kap[r];
+                  op = make_float2(f.x * kp, f.y * kp);
+                  break;
+                }
+                case OP_NAB1:
+                case OP_NAB2: {
+                  const float km = kmag_of(A, x, g);
+                  op = make_float2(km == 0.f ? 0.f : powf(km, J.op == OP_NAB1 ? A.pow1 : A.pow2), 0.f);
+                  break;
+                }
+                case OP_SKAPPA:
+                  op = make_float2(A.use_kspace ? cosf(A.kcoef * kmag_of(A, x, g)) : 1.f, 0.f);
+                  break;
+                default:
+                  op = A.us[J.axis][ai];
+                  break;
+              }
+              op = make_float2(op.x * A.scale, op.y * A.scale);
+              y[r] = (act && g.valid) ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
+            }
+          kwreg::Reg<E, P>::rev(y, t, ex + cc * RS, 1, tw, sync);
+          if (act) {
+            float2* out = A.bufs[J.out];
+#pragma unroll
+            for (int j = 0; j < E; ++j) out[base + (t + P * j) * xs] = cconj(y[j]);
+          }
+        }
+      }
+    }
+    if (tid == 0) counters[1] = (int)it;
+  }
+  __syncthreads();
+  // loads issued but never consumed (only after a timeout): wait for them, bounded
+  if (tid == 0) {
+    for (int i = counters[1]; i < counters[0]; ++i) {
+      const uint32_t s = (uint32_t)i % NST, k = (uint32_t)i / NST;
+      if (!kwtma::mbar_wait(&full[s], k & 1, kWaitLimitNs)) break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// Two variants: 4 stages at one CTA per SM, or (lengths <= 256) 2 stages at
+// two CTAs per SM.
+static int g_axis_variant = -1;
+static int axis_variant() {
+  if (g_axis_variant < 0) {
+    const char* e = getenv("KWAVE_GB300_AXIS_2CTA");
+    g_axis_variant = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_axis_variant;
+}
+static int stages_for(int n) { return (n <= 256 && !axis_variant()) ? 4 : 2; }
+
+static size_t tma_smem(int n, int E, int P) {
+  const int T = 256 / P, RS = n + E + 1;
+  return sizeof(float2) * ((size_t)stages_for(n) * n * T + (size_t)T * RS + n) + 2 * 4 * sizeof(uint64_t) + 16;
+}
+
+// Tensor-map storage for one plan: 2 axes x 4 buffers.
+struct KwTmaPlan {
+  TmaMaps maps[2];
+};
+
+void* kw_tma_plan_create() { return new KwTmaPlan(); }
+void kw_tma_plan_destroy(void* h) { delete static_cast<KwTmaPlan*>(h); }
+
+// Describe buffer `b` for a pass along `axis`: a 3-D tensor of 8-byte elements
+// (ncols contiguous, n along the axis with stride xs, nouter with stride os).
+bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long long xs, int nouter, long long os,
+                   int P) {
+  KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || !base) return false;
+  const int T = 256 / P;
+  cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)n, (cuuint64_t)nouter};
+  cuuint64_t strides[2] = {(cuuint64_t)xs * 8, (cuuint64_t)(nouter > 1 ? os : xs * n) * 8};
+  cuuint32_t box[3] = {(cuuint32_t)T, (cuuint32_t)(n < 256 ? n : 256), 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(&tp->maps[axis].m[b], CU_TENSOR_MAP_DATA_TYPE_INT64, 3, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+bool kw_tma_supported(int n) {
+  int E, P;
+  return encode_fn() != nullptr && kw_reg_shape(n, &E, &P);
+}
+
+#define KW_TMA_SWITCH(n, CALL)                                        \
+  switch (n) {                                                        \
+    case 64: return axis_variant() ? CALL(16, 4, 2, 2) : CALL(16, 4, 4, 1);    \
+    case 128: return axis_variant() ? CALL(16, 8, 2, 2) : CALL(16, 8, 4, 1);   \
+    case 256: return axis_variant() ? CALL(16, 16, 2, 2) : CALL(16, 16, 4, 1); \
+    case 512: return CALL(32, 16, 2, 1);                              \
+    case 1024: return CALL(32, 32, 2, 1);                             \
+    default: return cudaErrorInvalidValue;                            \
+  }
+
+cudaError_t kw_tma_attr(int n) {
+  int E, P;
+  if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
+  const int smem = (int)tma_smem(n, E, P);
+#define KW_T(E_, P_, S_, B_) \
+  cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+  KW_TMA_SWITCH(n, KW_T)
+#undef KW_T
+}
+
+// Launch one persistent pass along `axis` (0: operator or plain pass along x;
+// 1: plain pass along y of a 3-D grid) over `nb` plain buffers or A's jobs.
+cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A) {
+  KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
+  int E, P;
+  if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
+  const int T = 256 / P;
+  TmaWork W;
+  W.ntile = (A.ncols + T - 1) / T;
+  W.nouter = nouter;
+  if (A.mode < 2) {
+    W.nitems = 1;
+    W.nunits = W.ntile * nouter * nb;
+  } else {
+    int ni = 0;
+    for (int j = 0; j < A.njobs; ++j) {
+      bool seen = false;
+      for (int q = 0; q < ni; ++q) seen |= (W.inp[q] == A.jobs[j].in);
+      if (!seen) W.inp[ni++] = A.jobs[j].in;
+    }
+    W.nitems = ni;
+    W.nunits = W.ntile * nouter;
+  }
+  const int per_sm = (n <= 256 && axis_variant()) ? 2 : 1;
+  const int grid = W.nunits < nsm * per_sm ? W.nunits : nsm * per_sm;
+  const size_t smem = tma_smem(n, E, P);
+#define KW_T(E_, P_, S_, B_) (k_axis_tma<E_, P_, S_, B_><<<grid, 288, smem, st>>>(A, tp->maps[axis], W), cudaGetLastError())
+  KW_TMA_SWITCH(n, KW_T)
+#undef KW_T
+}
+
+int kw_device_error_take() {
+  int v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_kw_device_error, sizeof(int)) != cudaSuccess) return -1;
+  if (v) cudaMemcpyToSymbol(g_kw_device_error, &z, sizeof(int));
+  return v;
+}

@@ -5,6 +5,7 @@
 // round-to-nearest intrinsics so that the compiler does not contract the
 // reference's separate multiplies and adds into FMAs.
 #include "kw_kernels.cuh"
+#include "kw_regfft.cuh"
 
 // ---------------------------------------------------------------------------
 // spectral operators (kspace_solver.py:408-447, :811-816)
@@ -240,23 +241,24 @@ __device__ void record_samples(const RowsParams& P, const float* rbuf, float* re
 }
 
 // ---------------------------------------------------------------------------
-// row stage kernel
+// row stage kernels: one physics body, two row-FFT implementations
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams P) {
-  extern __shared__ float4 smem_f4[];
-  const int M = P.Mfft, L = P.L, R = P.R;
+// Row transforms through the shared-memory Stockham stages (any 2,3,5,7-smooth length).
+struct GenericRowFFT {
   RowSmem s;
-  s.tw = reinterpret_cast<float2*>(smem_f4);
-  s.twp = s.tw + M;
-  s.A = s.twp + (L / 2 + 1);
-  s.B = s.A + (size_t)R * M;
-  float* rb = reinterpret_cast<float*>(s.B + (size_t)R * M);
-  for (int q = 0; q < KW_NREAL; ++q) s.rb[q] = rb + (size_t)q * R * L;
-  for (int i = threadIdx.x; i < M; i += blockDim.x) s.tw[i] = P.tw[i];
-  if (P.even)
-    for (int i = threadIdx.x; i <= L / 2; i += blockDim.x) s.twp[i] = P.twpost[i];
-  __syncthreads();  // rows_c2r reads twp before its first FFT barrier
+  __device__ void c2r(const RowsParams& P, const float2* S, float* rbuf, int r0, int nr) const {
+    rows_c2r(P, s, S, rbuf, r0, nr);
+  }
+  __device__ void r2c(const RowsParams& P, const float* rbuf, float2* S, int r0, int nr) const {
+    rows_r2c(P, s, rbuf, S, r0, nr);
+  }
+};
 
+// The stage physics of one block of R rows; rb[q] are R*L real buffers in
+// shared memory.  Every rf call starts and ends with a block-wide barrier.
+template <class RF>
+__device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, float* const* rb) {
+  const int L = P.L, R = P.R;
   const int r0 = blockIdx.x * R;
   const int nr = min(R, P.nrows - r0);
   const int tot = R * L;
@@ -274,24 +276,24 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
       const float r = __fdiv_rn(pv, __fmul_rn(c2, (float)D));
       for (int a = 0; a < D; ++a) P.rho[a][g] = r;
       if (P.write_p) P.p[g] = pv;
-      s.rb[0][i] = pv;
+      rb[0][i] = pv;
     }
     __syncthreads();
-    record_samples(P, s.rb[0], P.rec[0], r0, nr);
-    rows_r2c(P, s, s.rb[0], P.S[3], r0, nr);
+    record_samples(P, rb[0], P.rec[0], r0, nr);
+    rf.r2c(P, rb[0], P.S[3], r0, nr);
     return;
   }
 
   if (P.stage == ST_U) {
     // momentum: u_i = pml_sg (pml_sg u_i - dt/rho_sg g_i) (kspace_solver.py:703-707)
     for (int a = 0; a < D; ++a) {
-      rows_c2r(P, s, P.S[a], s.rb[0], r0, nr);
+      rf.c2r(P, P.S[a], rb[0], r0, nr);
       float* u = P.u[a];
       for (int i = threadIdx.x; i < tot; i += blockDim.x) {
         const int row = i / L, z = i - row * L;
         if (row >= nr) continue;
         const long long g = (long long)(r0 + row) * L + z;
-        const float gr = s.rb[0][i];
+        const float gr = rb[0][i];
         const float dtr = fld(P.dtrsg[a], P.dtrsg_s[a], g);
         float nu;
         if (P.init) {
@@ -300,18 +302,18 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
           const float sg = P.pmlsg[a][axis_index(P, a, r0 + row, z)];
           nu = __fmul_rn(sg, __fsub_rn(__fmul_rn(sg, u[g]), __fmul_rn(dtr, gr)));
         }
-        s.rb[0][i] = nu;
+        rb[0][i] = nu;
       }
       __syncthreads();
-      if (!P.init) apply_source(P, P.src[3 + a], s.rb[0], r0, nr);
+      if (!P.init) apply_source(P, P.src[3 + a], rb[0], r0, nr);
       __syncthreads();
       for (int i = threadIdx.x; i < tot; i += blockDim.x) {
         const int row = i / L, z = i - row * L;
         if (row >= nr) continue;
-        u[(long long)(r0 + row) * L + z] = s.rb[0][i];
+        u[(long long)(r0 + row) * L + z] = rb[0][i];
       }
-      record_samples(P, s.rb[0], P.rec[1 + a], r0, nr);
-      if (!P.init) rows_r2c(P, s, s.rb[0], P.S[a], r0, nr);
+      record_samples(P, rb[0], P.rec[1 + a], r0, nr);
+      if (!P.init) rf.r2c(P, rb[0], P.S[a], r0, nr);
       __syncthreads();
     }
     return;
@@ -319,7 +321,7 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
 
   if (P.stage == ST_RHO) {
     // mass conservation with split density (kspace_solver.py:709-717)
-    for (int a = 0; a < D; ++a) rows_c2r(P, s, P.S[a], s.rb[a], r0, nr);
+    for (int a = 0; a < D; ++a) rf.c2r(P, P.S[a], rb[a], r0, nr);
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
       const int row = i / L, z = i - row * L;
       if (row >= nr) continue;
@@ -334,35 +336,35 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
       float div = 0.f;
       const float dtr0 = __fmul_rn(P.dt, r0v);
       for (int a = 0; a < D; ++a) {
-        const float du = s.rb[a][i];
+        const float du = rb[a][i];
         div = __fadd_rn(div, du);
         const float pm = P.pml[a][axis_index(P, a, r0 + row, z)];
         const float term = __fmul_rn(__fmul_rn(dtr0, du), nl);
-        s.rb[a][i] = __fmul_rn(pm, __fsub_rn(__fmul_rn(pm, P.rho[a][g]), term));
+        rb[a][i] = __fmul_rn(pm, __fsub_rn(__fmul_rn(pm, P.rho[a][g]), term));
       }
-      s.rb[3][i] = div;
+      rb[3][i] = div;
     }
     __syncthreads();
-    for (int a = 0; a < D; ++a) apply_source(P, P.src[a], s.rb[a], r0, nr);
+    for (int a = 0; a < D; ++a) apply_source(P, P.src[a], rb[a], r0, nr);
     __syncthreads();
     const bool powerlaw = P.absorb == 1;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
       const int row = i / L, z = i - row * L;
       if (row >= nr) continue;
       const long long g = (long long)(r0 + row) * L + z;
-      float rs = s.rb[0][i];
+      float rs = rb[0][i];
       P.rho[0][g] = rs;
       for (int a = 1; a < D; ++a) {
-        const float ra = s.rb[a][i];
+        const float ra = rb[a][i];
         P.rho[a][g] = ra;
         rs = __fadd_rn(rs, ra);
       }
-      const float div = s.rb[3][i];
+      const float div = rb[3][i];
       const float r0v = fld(P.rho0, P.rho0_s, g);
       if (powerlaw) {
         P.rho_sum[g] = rs;
-        s.rb[0][i] = __fmul_rn(r0v, div);
-        s.rb[1][i] = rs;
+        rb[0][i] = __fmul_rn(r0v, div);
+        rb[1][i] = rs;
       } else {
         // equation of state without fractional Laplacians (kspace_solver.py:719-723)
         const float c = fld(P.c0, P.c0_s, g);
@@ -375,23 +377,23 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
         }
         const float pv = __fmul_rn(c2, acc);
         if (P.write_p) P.p[g] = pv;
-        s.rb[0][i] = pv;
+        rb[0][i] = pv;
       }
     }
     __syncthreads();
     if (powerlaw) {
-      rows_r2c(P, s, s.rb[0], P.S[0], r0, nr);
-      if (P.disp) rows_r2c(P, s, s.rb[1], P.S[1], r0, nr);
+      rf.r2c(P, rb[0], P.S[0], r0, nr);
+      if (P.disp) rf.r2c(P, rb[1], P.S[1], r0, nr);
     } else {
-      record_samples(P, s.rb[0], P.rec[0], r0, nr);
-      rows_r2c(P, s, s.rb[0], P.S[3], r0, nr);
+      record_samples(P, rb[0], P.rec[0], r0, nr);
+      rf.r2c(P, rb[0], P.S[3], r0, nr);
     }
     return;
   }
 
   // ST_EOS: p = c0^2 (rho + tau F^-1[nabla1 F[rho0 div]] - eta F^-1[nabla2 F[rho]] + B/A rho^2 / (2 rho0))
-  rows_c2r(P, s, P.S[0], s.rb[0], r0, nr);
-  if (P.disp) rows_c2r(P, s, P.S[1], s.rb[1], r0, nr);
+  rf.c2r(P, P.S[0], rb[0], r0, nr);
+  if (P.disp) rf.c2r(P, P.S[1], rb[1], r0, nr);
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
     const int row = i / L, z = i - row * L;
     if (row >= nr) continue;
@@ -399,8 +401,8 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
     const float rs = P.rho_sum[g];
     const float c = fld(P.c0, P.c0_s, g);
     const float c2 = __fmul_rn(c, c);
-    float acc = __fadd_rn(rs, __fmul_rn(fld(P.tau, P.tau_s, g), s.rb[0][i]));
-    if (P.disp) acc = __fsub_rn(acc, __fmul_rn(fld(P.eta, P.eta_s, g), s.rb[1][i]));
+    float acc = __fadd_rn(rs, __fmul_rn(fld(P.tau, P.tau_s, g), rb[0][i]));
+    if (P.disp) acc = __fsub_rn(acc, __fmul_rn(fld(P.eta, P.eta_s, g), rb[1][i]));
     if (P.nonlin) {
       const float r0v = fld(P.rho0, P.rho0_s, g);
       const float nlt = __fdiv_rn(__fmul_rn(fld(P.bona, P.bona_s, g), __fmul_rn(rs, rs)), __fmul_rn(2.f, r0v));
@@ -408,12 +410,178 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
     }
     const float pv = __fmul_rn(c2, acc);
     if (P.write_p) P.p[g] = pv;
-    s.rb[0][i] = pv;
+    rb[0][i] = pv;
   }
   __syncthreads();
-  record_samples(P, s.rb[0], P.rec[0], r0, nr);
-  rows_r2c(P, s, s.rb[0], P.S[3], r0, nr);
+  record_samples(P, rb[0], P.rec[0], r0, nr);
+  rf.r2c(P, rb[0], P.S[3], r0, nr);
 }
+
+__global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams P) {
+  extern __shared__ float4 smem_f4[];
+  const int M = P.Mfft, L = P.L, R = P.R;
+  GenericRowFFT rf;
+  RowSmem& s = rf.s;
+  s.tw = reinterpret_cast<float2*>(smem_f4);
+  s.twp = s.tw + M;
+  s.A = s.twp + (L / 2 + 1);
+  s.B = s.A + (size_t)R * M;
+  float* rbase = reinterpret_cast<float*>(s.B + (size_t)R * M);
+  for (int q = 0; q < KW_NREAL; ++q) s.rb[q] = rbase + (size_t)q * R * L;
+  for (int i = threadIdx.x; i < M; i += blockDim.x) s.tw[i] = P.tw[i];
+  if (P.even)
+    for (int i = threadIdx.x; i <= L / 2; i += blockDim.x) s.twp[i] = P.twpost[i];
+  __syncthreads();  // the row transforms read twp before their first barrier
+  rows_body(P, rf, s.rb);
+}
+
+// ---------------------------------------------------------------------------
+// register-FFT variants for power-of-two lengths (kw_regfft.cuh)
+// ---------------------------------------------------------------------------
+// Spectral operator value at x-frequency index x of a column (register axis pass).
+__device__ __forceinline__ float2 col_op(const AxisParams& A, const AxisJob& J, int x, const ColK& g) {
+  const float kx = A.k[0][x];
+  float kk = __fadd_rn(__fmul_rn(kx, kx), g.ky2);
+  if (A.ndim == 3) kk = __fadd_rn(kk, g.kz2);
+  const float kmag = sqrtf(kk);
+  const int ai = (J.axis == 0) ? x : (J.axis == 1 ? g.a1 : g.a2);
+  float2 v;
+  switch (J.op) {
+    case OP_GRAD:
+    case OP_DIV: {
+      float kappa = 1.f;
+      if (A.use_kspace) {
+        const float arg = A.kcoef * kmag;
+        kappa = (arg == 0.f) ? 1.f : sinf(arg) / arg;
+      }
+      const float2 f = (J.op == OP_GRAD) ? A.fg[J.axis][ai] : A.fd[J.axis][ai];
+      v = make_float2(f.x * kappa, f.y * kappa);
+      break;
+    }
+    case OP_NAB1:
+    case OP_NAB2: {
+      const float e = (J.op == OP_NAB1) ? A.pow1 : A.pow2;
+      v = make_float2(kmag == 0.f ? 0.f : powf(kmag, e), 0.f);
+      break;
+    }
+    case OP_SKAPPA:
+      v = make_float2(A.use_kspace ? cosf(A.kcoef * kmag) : 1.f, 0.f);
+      break;
+    default:
+      v = A.us[J.axis][ai];
+      break;
+  }
+  return make_float2(v.x * A.scale, v.y * A.scale);
+}
+
+// Strided axis: T = 256 / P columns per block, P threads per column.
+template <int E, int P>
+__global__ void __launch_bounds__(256) k_axis_reg(const __grid_constant__ AxisParams A) {
+  constexpr int N = E * P, T = 256 / P, RS = N + E + 1;
+  extern __shared__ float4 smem_f4[];
+  float2* tw = reinterpret_cast<float2*>(smem_f4);
+  float2* ex = tw + N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  __syncthreads();
+  const int cc = threadIdx.x % T, t = threadIdx.x / T;
+  const int c0 = blockIdx.x * T;
+  const bool act = cc < A.ncols - c0;
+  const long long base = (long long)blockIdx.y * A.os + c0 + cc;
+  const long long xs = A.xs;
+  float2* sm = ex + cc * RS;
+  auto sync = [] __device__() { __syncthreads(); };
+  if (A.mode < 2) {
+    float2* buf = A.bufs[A.plain[blockIdx.z]];
+    float2 v[E];
+    if (A.mode == 0) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) v[j] = act ? buf[base + (t + P * j) * xs] : make_float2(0.f, 0.f);
+      kwreg::Reg<E, P>::fwd(v, t, sm, 1, tw, sync);
+      if (act) {
+#pragma unroll
+        for (int m = 0; m < E / P; ++m)
+#pragma unroll
+          for (int k2 = 0; k2 < P; ++k2) buf[base + (t + P * m + E * k2) * xs] = v[m * P + k2];
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < E / P; ++m)
+#pragma unroll
+        for (int k2 = 0; k2 < P; ++k2)
+          v[m * P + k2] = act ? cconj(buf[base + (t + P * m + E * k2) * xs]) : make_float2(0.f, 0.f);
+      kwreg::Reg<E, P>::rev(v, t, sm, 1, tw, sync);
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < E; ++j) buf[base + (t + P * j) * xs] = cconj(v[j]);
+      }
+    }
+    return;
+  }
+  const ColK g = col_geometry(A, act ? c0 + cc : c0);
+  int cur = -1;
+  float2 X[E];
+  for (int jj = 0; jj < A.njobs; ++jj) {
+    const AxisJob J = A.jobs[jj];
+    if (J.in != cur) {
+      const float2* in = A.bufs[J.in];
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = act ? in[base + (t + P * j) * xs] : make_float2(0.f, 0.f);
+      kwreg::Reg<E, P>::fwd(X, t, sm, 1, tw, sync);
+      cur = J.in;
+    }
+    float2 Y[E];
+#pragma unroll
+    for (int m = 0; m < E / P; ++m)
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) {
+        float2 y = make_float2(0.f, 0.f);
+        if (act && g.valid) y = cconj(cmul(col_op(A, J, t + P * m + E * k2, g), X[m * P + k2]));
+        Y[m * P + k2] = y;
+      }
+    kwreg::Reg<E, P>::rev(Y, t, sm, 1, tw, sync);
+    if (act) {
+      float2* out = A.bufs[J.out];
+#pragma unroll
+      for (int j = 0; j < E; ++j) out[base + (t + P * j) * xs] = cconj(Y[j]);
+    }
+  }
+}
+
+// Host-side dispatch of the register kernels (launched from this translation
+// unit, where the templates are instantiated).
+bool kw_reg_shape(int n, int* E, int* P) {
+  switch (n) {
+    case 64: *E = 16; *P = 4; return true;
+    case 128: *E = 16; *P = 8; return true;
+    case 256: *E = 16; *P = 16; return true;
+    case 512: *E = 32; *P = 16; return true;
+    case 1024: *E = 32; *P = 32; return true;
+    default: return false;
+  }
+}
+
+#define KW_REG_SWITCH(n, CALL)             \
+  switch (n) {                             \
+    case 64: return CALL(16, 4);           \
+    case 128: return CALL(16, 8);          \
+    case 256: return CALL(16, 16);         \
+    case 512: return CALL(32, 16);         \
+    case 1024: return CALL(32, 32);        \
+    default: return cudaErrorInvalidValue; \
+  }
+
+cudaError_t kw_axis_reg_attr(int n) {
+#define KW_A(E, P) cudaFuncSetAttribute(k_axis_reg<E, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
+  KW_REG_SWITCH(n, KW_A)
+#undef KW_A
+}
+
+cudaError_t kw_axis_reg_launch(int n, dim3 grid, size_t smem, cudaStream_t st, const AxisParams& A) {
+#define KW_A(E, P) (k_axis_reg<E, P><<<grid, 256, smem, st>>>(A), cudaGetLastError())
+  KW_REG_SWITCH(n, KW_A)
+#undef KW_A
+}
+
 
 // ---------------------------------------------------------------------------
 // recorder post-processing (kspace_solver.py:335-359, :824-837)

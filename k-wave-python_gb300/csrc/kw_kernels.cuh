@@ -43,6 +43,7 @@ struct RowsParams {
   int ndim, N0, N1, L, H, Hp, Mfft, even;
   int nrows, R;
   int t, rec_row, write_p;
+  int ex_stride;         // register-FFT rows: exchange region per row (complex values)
   float2* S[4];          // spectral work buffers S0..S2 and P (index 3)
   float* u[3];
   float* rho[3];
@@ -103,7 +104,53 @@ struct AxisParams {
   float scale;    // 1 / N_total
 };
 
+// Spectral operator for one column (ky, kz fixed) of the axis-0 pass.
+struct ColK {
+  int a1, a2;
+  bool valid;
+  float ky2, kz2;
+};
+
+__device__ __forceinline__ ColK col_geometry(const AxisParams& A, int c) {
+  ColK g;
+  if (A.ndim == 3) {
+    g.a1 = c / A.Hp;
+    g.a2 = c - g.a1 * A.Hp;
+    g.valid = g.a2 < A.H;
+    const float ky = A.k[1][g.a1];
+    const float kz = g.valid ? A.k[2][g.a2] : 0.f;
+    g.ky2 = __fmul_rn(ky, ky);
+    g.kz2 = __fmul_rn(kz, kz);
+  } else {
+    g.a1 = c;
+    g.a2 = 0;
+    g.valid = c < A.H;
+    const float ky = g.valid ? A.k[1][c] : 0.f;
+    g.ky2 = __fmul_rn(ky, ky);
+    g.kz2 = 0.f;
+  }
+  return g;
+}
+
 __global__ void k_axis(const __grid_constant__ AxisParams P);
+// Register-FFT variants for power-of-two lengths 64..1024, launched through
+// these host helpers (defined next to the template instantiations).
+bool kw_reg_shape(int n, int* E, int* P);
+cudaError_t kw_axis_reg_attr(int n);
+cudaError_t kw_rows_v2_attr(int m);
+cudaError_t kw_axis_reg_launch(int n, dim3 grid, size_t smem, cudaStream_t st, const AxisParams& A);
+// register-resident row stages (kw_rows_reg.cu), 128 threads per block
+cudaError_t kw_rows_v2_launch(int m, int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q);
+
+// Persistent TMA-fed axis passes (kw_axis_tma.cu), power-of-two lengths 64..1024.
+void* kw_tma_plan_create();
+void kw_tma_plan_destroy(void* h);
+bool kw_tma_supported(int n);
+bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long long xs, int nouter, long long os, int P);
+cudaError_t kw_tma_attr(int n);
+cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A);
+// Returns and clears the device error word (nonzero: a bounded device wait timed out).
+int kw_device_error_take();
 __global__ void k_rows(const __grid_constant__ RowsParams P);
 __global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
                                 const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out);

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -92,6 +93,16 @@ struct kw_plan {
   double* d_iw = nullptr;
   size_t smem_rows = 0, smem_axis_plain[3] = {0, 0, 0}, smem_axis_ops = 0;
   int T_axis[3] = {1, 1, 1};
+  // register-FFT dispatch (power-of-two lengths 64..1024)
+  bool generic_only = false;
+  bool axis_reg[3] = {false, false, false};
+  int axis_regP[3] = {0, 0, 0}, axis_regE[3] = {0, 0, 0};
+  bool rows_reg = false;
+  // persistent TMA axis passes
+  void* tma = nullptr;
+  bool tma_axis[3] = {false, false, false};
+  int nsm = 0;
+  int rows_regP = 0, rows_regE = 0, rows_R = 0, rows_RS = 0;
   // launch accounting / timing
   long long launches = 0;
   bool timing = false;
@@ -446,6 +457,54 @@ int32_t kw_plan_finalize(kw_plan* p) {
   }
   CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   CK(cudaFuncSetAttribute(k_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  {
+    const char* env = getenv("KWAVE_GB300_GENERIC_FFT");
+    p->generic_only = env && env[0] == '1';
+  }
+  {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  if (!p->generic_only) {
+    const char* env = getenv("KWAVE_GB300_NO_TMA");
+    const bool no_tma = env && env[0] == '1';
+    for (int a = 0; a < D - 1 && !no_tma; ++a) {
+      if (!kw_tma_supported(p->N[a])) continue;
+      if (!p->tma) p->tma = kw_tma_plan_create();
+      int E, Pt;
+      kw_reg_shape(p->N[a], &E, &Pt);
+      bool ok = true;
+      for (int b = 0; b < 4; ++b) {
+        if (!p->d_S[b]) continue;
+        if (D == 3 && a == 0)
+          ok &= kw_tma_encode(p->tma, 0, b, p->d_S[b], p->N[1] * p->Hp, p->N[0], (long long)p->N[1] * p->Hp, 1, 0, Pt);
+        else if (D == 3)
+          ok &= kw_tma_encode(p->tma, 1, b, p->d_S[b], p->Hp, p->N[1], p->Hp, p->N[0], (long long)p->N[1] * p->Hp, Pt);
+        else
+          ok &= kw_tma_encode(p->tma, 0, b, p->d_S[b], p->Hp, p->N[0], p->Hp, 1, 0, Pt);
+      }
+      if (ok) {
+        CK(kw_tma_attr(p->N[a]));
+        p->tma_axis[a] = true;
+      }
+    }
+    for (int a = 0; a < D - 1; ++a) {
+      p->axis_reg[a] = kw_reg_shape(p->N[a], &p->axis_regE[a], &p->axis_regP[a]);
+      if (p->axis_reg[a]) CK(kw_axis_reg_attr(p->N[a]));
+    }
+    if (p->even) {
+      p->rows_reg = kw_reg_shape(p->Mfft, &p->rows_regE, &p->rows_regP);
+      if (p->rows_reg) {
+        p->rows_R = 128 / p->rows_regP;
+        const int target = p->rows_regP == 4 ? 4 : (p->rows_regP == 8 ? 8 : 0);
+        int rs = p->Mfft + p->rows_regE;
+        while (rs % 16 != target) ++rs;
+        p->rows_RS = rs;
+        CK(kw_rows_v2_attr(p->Mfft));
+      }
+    }
+  }
   CK(cudaDeviceSynchronize());
   p->finalized = true;
   p->t = 0;
@@ -511,11 +570,19 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   P.t = t;
   P.rec_row = (t >= p->g.record_start) ? t - p->g.record_start : -1;
   P.write_p = write_p;
-  const int grid = (p->nrows + p->R - 1) / p->R;
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
-  k_rows<<<grid, kThreads, p->smem_rows, st>>>(P);
+  if (p->rows_reg) {
+    P.R = p->rows_R;
+    P.ex_stride = p->rows_RS;
+    const size_t smem = sizeof(float2) * (2 * (size_t)p->Mfft + 1 + (size_t)p->rows_R * p->rows_RS);
+    const int grid = (p->nrows + p->rows_R - 1) / p->rows_R;
+    CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
+  } else {
+    const int grid = (p->nrows + p->R - 1) / p->R;
+    k_rows<<<grid, kThreads, p->smem_rows, st>>>(P);
+  }
   CK(cudaGetLastError());
   return ev_end(p, st, KW_K_ROWS_INIT + stage, slot);
 }
@@ -553,11 +620,19 @@ static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int
   A.mode = inv ? 1 : 0;
   for (int i = 0; i < nb; ++i) A.plain[i] = bufs[i];
   const int nouter = (p->D == 3 && axis == 1) ? p->N[0] : 1;
-  dim3 grid((A.ncols + A.T - 1) / A.T, nouter, nb);
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
-  k_axis<<<grid, kThreads, p->smem_axis_plain[axis], st>>>(A);
+  if (p->tma_axis[axis]) {
+    CK(kw_tma_launch(p->tma, axis, p->N[axis], nouter, nb, p->nsm, st, A));
+  } else if (p->axis_reg[axis]) {
+    const int E = p->axis_regE[axis], Pt = p->axis_regP[axis], T = 256 / Pt, n = p->N[axis];
+    dim3 grid((A.ncols + T - 1) / T, nouter, nb);
+    CK(kw_axis_reg_launch(n, grid, sizeof(float2) * ((size_t)n + (size_t)T * (n + E + 1)), st, A));
+  } else {
+    dim3 grid((A.ncols + A.T - 1) / A.T, nouter, nb);
+    k_axis<<<grid, kThreads, p->smem_axis_plain[axis], st>>>(A);
+  }
   CK(cudaGetLastError());
   return ev_end(p, st, KW_K_AXIS_PLAIN, slot);
 }
@@ -579,11 +654,19 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
   A.pow1 = (float)(p->g.alpha_power - 2.0);
   A.pow2 = (float)(p->g.alpha_power - 1.0);
   A.scale = (float)(1.0 / (double)p->ntot);
-  dim3 grid((A.ncols + A.T - 1) / A.T, 1, 1);
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
-  k_axis<<<grid, kThreads, p->smem_axis_ops, st>>>(A);
+  if (p->tma_axis[0]) {
+    CK(kw_tma_launch(p->tma, 0, p->N[0], 1, 0, p->nsm, st, A));
+  } else if (p->axis_reg[0]) {
+    const int E = p->axis_regE[0], Pt = p->axis_regP[0], T = 256 / Pt, n = p->N[0];
+    dim3 grid((A.ncols + T - 1) / T, 1, 1);
+    CK(kw_axis_reg_launch(n, grid, sizeof(float2) * ((size_t)n + (size_t)T * (n + E + 1)), st, A));
+  } else {
+    dim3 grid((A.ncols + A.T - 1) / A.T, 1, 1);
+    k_axis<<<grid, kThreads, p->smem_axis_ops, st>>>(A);
+  }
   CK(cudaGetLastError());
   return ev_end(p, st, KW_K_AXIS_OPS, slot);
 }
@@ -644,10 +727,17 @@ int32_t kw_plan_run(kw_plan* p, int32_t nsteps, void* stream) {
   return KW_OK;
 }
 
+static int check_device_error() {
+  const int e = kw_device_error_take();
+  if (e > 0) return fail(KW_ERR_CUDA, "a bounded device wait timed out (code %d); results of this run are invalid", e);
+  if (e < 0) return fail(KW_ERR_CUDA, "could not read the device error word");
+  return KW_OK;
+}
+
 int32_t kw_plan_sync(kw_plan* p, void* stream) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");
   CK(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
-  return KW_OK;
+  return check_device_error();
 }
 
 int32_t kw_plan_time_index(const kw_plan* p, int32_t* t) {
@@ -794,6 +884,7 @@ int32_t kw_plan_launch_count(const kw_plan* p, int64_t* count) {
 int32_t kw_plan_destroy(kw_plan* p) {
   if (!p) return KW_OK;
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  if (p->tma) kw_tma_plan_destroy(p->tma);
   for (void* a : p->allocs) cudaFree(a);
   delete p;
   return KW_OK;

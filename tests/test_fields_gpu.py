@@ -8,7 +8,10 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(16, 15), (15, 16), (16, 16), (8, 8), (2, 4), (12, 20), (30, 18), (8, 6, 10), (9, 5, 7), (6, 10, 12)]
+# generic shared-memory transforms (any 2,3,5,7-smooth length) ...
+SHAPES = [(16, 15), (15, 16), (16, 16), (8, 8), (2, 4), (12, 20), (30, 18), (8, 6, 10), (9, 5, 7), (6, 10, 12),
+          # ... and register transforms (power-of-two lengths 64..1024 along x/y, 128..2048 along the last axis)
+          (128, 128), (64, 512), (512, 128), (1024, 120), (64, 128, 256), (16, 64, 2048), (20, 256, 30)]
 
 
 def rel_max(a, b):
