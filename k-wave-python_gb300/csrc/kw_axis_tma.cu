@@ -57,11 +57,61 @@ __device__ __forceinline__ float kappa_of(const AxisParams& A, float kmag) {
   return kwreg::sinc_taylor(A.kcoef * kmag);
 }
 
-__device__ __forceinline__ float kmag_of(const AxisParams& A, int x, const ColK& g) {
-  const float kx = A.k[0][x];
+__device__ __forceinline__ float kmag_of(const float* k0s, int ndim, int x, const ColK& g) {
+  const float kx = k0s[x];
   float kk = __fadd_rn(__fmul_rn(kx, kx), g.ky2);
-  if (A.ndim == 3) kk = __fadd_rn(kk, g.kz2);
+  if (ndim == 3) kk = __fadd_rn(kk, g.kz2);
   return sqrtf(kk);
+}
+
+// The x-axis operator tables (shared or global memory).
+struct TabX {
+  const float2* grad;
+  const float2* div;
+  const float2* unstag;
+};
+
+// Operator of job J at x-frequency index x of column g.  fcol is the job's
+// 1-D factor when it acts along y or z (constant over the column).  With
+// full == false only the 1-D factor of a gradient/divergence is returned
+// (kappa and 1/N already folded into the spectrum).
+__device__ __forceinline__ float2 op_value(const AxisParams& A, const AxisJob& J, int x, const ColK& g,
+                                           const float* k0s, const TabX& f0s, float2 fcol, bool full) {
+  float2 op;
+  switch (J.op) {
+    case OP_GRAD:
+    case OP_DIV: {
+      const float2 f = (J.axis == 0) ? (J.op == OP_GRAD ? f0s.grad[x] : f0s.div[x]) : fcol;
+      if (!full) return f;
+      const float kp = kappa_of(A, kmag_of(k0s, A.ndim, x, g)) * A.scale;
+      return make_float2(f.x * kp, f.y * kp);
+    }
+    case OP_NAB1:
+    case OP_NAB2: {
+      const float km = kmag_of(k0s, A.ndim, x, g);
+      op = make_float2(km == 0.f ? 0.f : powf(km, J.op == OP_NAB1 ? A.pow1 : A.pow2), 0.f);
+      break;
+    }
+    case OP_SKAPPA:
+      op = make_float2(A.use_kspace ? cosf(A.kcoef * kmag_of(k0s, A.ndim, x, g)) : 1.f, 0.f);
+      break;
+    default:
+      op = (J.axis == 0) ? f0s.unstag[x] : fcol;
+      break;
+  }
+  return make_float2(op.x * A.scale, op.y * A.scale);
+}
+
+// The column-constant 1-D factor of job J (axis 1 or 2).
+__device__ __forceinline__ float2 col_factor(const AxisParams& A, const AxisJob& J, const ColK& g) {
+  if (J.axis == 0 || !g.valid) return make_float2(0.f, 0.f);
+  const int ai = (J.axis == 1) ? g.a1 : g.a2;
+  switch (J.op) {
+    case OP_GRAD: return A.fg[J.axis][ai];
+    case OP_DIV: return A.fd[J.axis][ai];
+    case OP_UNSTAG: return A.us[J.axis][ai];
+    default: return make_float2(0.f, 0.f);
+  }
 }
 
 }  // namespace
@@ -75,7 +125,12 @@ __global__ void __launch_bounds__(288, MINB)
   float2* stages = reinterpret_cast<float2*>(smem_raw);  // NST * N * T
   float2* ex = stages + (size_t)NST * N * T;             // T * RS
   float2* tw = ex + (size_t)T * RS;                      // N
-  uint64_t* full = reinterpret_cast<uint64_t*>(tw + N);
+  // x-axis tables (k, op_grad, op_div, unstag) in shared memory when they fit
+  constexpr bool kTablesInSmem = N <= 512;
+  constexpr int NT = kTablesInSmem ? N : 0;
+  float* k0t = reinterpret_cast<float*>(tw + N);
+  float2* f0t = reinterpret_cast<float2*>(k0t + NT);
+  uint64_t* full = reinterpret_cast<uint64_t*>(f0t + 3 * NT);
   uint64_t* empty = full + NST;
   int* counters = reinterpret_cast<int*>(empty + NST);  // [0] issued, [1] consumed
 
@@ -88,8 +143,18 @@ __global__ void __launch_bounds__(288, MINB)
     counters[0] = counters[1] = 0;
     kwtma::fence_barrier_init();
   }
-  for (int i = tid; i < N; i += blockDim.x) tw[i] = A.tw[i];
+  for (int i = tid; i < N; i += blockDim.x) {
+    tw[i] = A.tw[i];
+    if (kTablesInSmem && A.mode == 2) {
+      k0t[i] = A.k[0][i];
+      f0t[i] = A.fg[0][i];
+      f0t[N + i] = A.fd[0][i];
+      f0t[2 * N + i] = A.us[0] ? A.us[0][i] : make_float2(0.f, 0.f);
+    }
+  }
   __syncthreads();
+  const float* k0s = kTablesInSmem ? k0t : A.k[0];
+  const TabX f0s{kTablesInSmem ? f0t : A.fg[0], kTablesInSmem ? f0t + N : A.fd[0], kTablesInSmem ? f0t + 2 * N : A.us[0]};
 
   const bool plain = A.mode < 2;
   if (warp == 8) {
@@ -113,6 +178,7 @@ __global__ void __launch_bounds__(288, MINB)
           kwtma::mbar_arrive_expect_tx(&full[s], kStageBytes);
           float2* dst = stages + (size_t)s * N * T;
 #pragma unroll
+#pragma unroll
           for (int n0 = 0; n0 < N; n0 += 256) kwtma::tma_load_3d(dst + n0 * T, &maps.m[buf], tile * T, n0, outer, &full[s]);
         }
       }
@@ -134,18 +200,7 @@ __global__ void __launch_bounds__(288, MINB)
       const long long base = (long long)outer * A.os + c0 + cc;
       const long long xs = A.xs;
       ColK g;
-      float kap[E];
-      if (!plain) {
-        g = col_geometry(A, act ? c0 + cc : c0);
-        bool need = false;
-        for (int j = 0; j < A.njobs; ++j) need |= (A.jobs[j].op == OP_GRAD || A.jobs[j].op == OP_DIV);
-        if (need) {
-#pragma unroll
-          for (int m = 0; m < E / P; ++m)
-#pragma unroll
-            for (int k2 = 0; k2 < P; ++k2) kap[m * P + k2] = kappa_of(A, kmag_of(A, t + P * m + E * k2, g));
-        }
-      }
+      if (!plain) g = col_geometry(A, act ? c0 + cc : c0);
       for (int q = 0; q < W.nitems; ++q, ++it) {
         const uint32_t s = it % NST, k = it / NST;
         const bool got = kwtma::mbar_wait(&full[s], k & 1, kWaitLimitNs);
@@ -190,40 +245,55 @@ __global__ void __launch_bounds__(288, MINB)
         // operator mode: forward FFT of this input, then every job reading it
         kwreg::Reg<E, P>::fwd(v, t, ex + cc * RS, 1, tw, sync);
         const int in = W.inp[q];
+        int nj = 0, jlast = 0;
+        bool all_kappa = true;
+        for (int jj = 0; jj < A.njobs; ++jj)
+          if (A.jobs[jj].in == in) {
+            ++nj;
+            jlast = jj;
+            all_kappa &= (A.jobs[jj].op == OP_GRAD || A.jobs[jj].op == OP_DIV);
+          }
+        if (nj == 1) {
+          // one job: multiply in place
+          const AxisJob J = A.jobs[jlast];
+          const float2 fcol = col_factor(A, J, g);
+#pragma unroll
+          for (int m = 0; m < E / P; ++m)
+#pragma unroll
+            for (int k2 = 0; k2 < P; ++k2) {
+              const int r = m * P + k2;
+              const float2 op = op_value(A, J, t + P * m + E * k2, g, k0s, f0s, fcol, true);
+              v[r] = (act && g.valid) ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
+            }
+          kwreg::Reg<E, P>::rev(v, t, ex + cc * RS, 1, tw, sync);
+          if (act) {
+            float2* out = A.bufs[J.out];
+#pragma unroll
+            for (int j = 0; j < E; ++j) out[base + (t + P * j) * xs] = cconj(v[j]);
+          }
+          continue;
+        }
+        if (all_kappa) {
+          // the jobs share kappa(|k|) / N: fold it into the spectrum once
+#pragma unroll
+          for (int m = 0; m < E / P; ++m)
+#pragma unroll
+            for (int k2 = 0; k2 < P; ++k2) {
+              const float kp = kappa_of(A, kmag_of(k0s, A.ndim, t + P * m + E * k2, g)) * A.scale;
+              v[m * P + k2] = make_float2(v[m * P + k2].x * kp, v[m * P + k2].y * kp);
+            }
+        }
         for (int jj = 0; jj < A.njobs; ++jj) {
           const AxisJob J = A.jobs[jj];
           if (J.in != in) continue;
+          const float2 fcol = col_factor(A, J, g);
           float2 y[E];
 #pragma unroll
           for (int m = 0; m < E / P; ++m)
 #pragma unroll
             for (int k2 = 0; k2 < P; ++k2) {
-              const int x = t + P * m + E * k2;
               const int r = m * P + k2;
-              float2 op;
-              const int ai = (J.axis == 0) ? x : (J.axis == 1 ? g.a1 : g.a2);
-              switch (J.op) {
-                case OP_GRAD:
-                case OP_DIV: {
-                  const float2 f = (J.op == OP_GRAD) ? A.fg[J.axis][ai] : A.fd[J.axis][ai];
-                  const float kp = kap[r];
-                  op = make_float2(f.x * kp, f.y * kp);
-                  break;
-                }
-                case OP_NAB1:
-                case OP_NAB2: {
-                  const float km = kmag_of(A, x, g);
-                  op = make_float2(km == 0.f ? 0.f : powf(km, J.op == OP_NAB1 ? A.pow1 : A.pow2), 0.f);
-                  break;
-                }
-                case OP_SKAPPA:
-                  op = make_float2(A.use_kspace ? cosf(A.kcoef * kmag_of(A, x, g)) : 1.f, 0.f);
-                  break;
-                default:
-                  op = A.us[J.axis][ai];
-                  break;
-              }
-              op = make_float2(op.x * A.scale, op.y * A.scale);
+              const float2 op = op_value(A, J, t + P * m + E * k2, g, k0s, f0s, fcol, !all_kappa);
               y[r] = (act && g.valid) ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
             }
           kwreg::Reg<E, P>::rev(y, t, ex + cc * RS, 1, tw, sync);
@@ -280,7 +350,9 @@ static int stages_for(int n) { return (n <= 256 && !axis_variant()) ? 4 : 2; }
 
 static size_t tma_smem(int n, int E, int P) {
   const int T = 256 / P, RS = n + E + 1;
-  return sizeof(float2) * ((size_t)stages_for(n) * n * T + (size_t)T * RS + n) + 2 * 4 * sizeof(uint64_t) + 16;
+  const size_t nt = n <= 512 ? (size_t)n : 0;
+  return sizeof(float2) * ((size_t)stages_for(n) * n * T + (size_t)T * RS + n + 3 * nt) + sizeof(float) * nt +
+         2 * 4 * sizeof(uint64_t) + 16;
 }
 
 // Tensor-map storage for one plan: 2 axes x 4 buffers.
@@ -314,14 +386,14 @@ bool kw_tma_supported(int n) {
   return encode_fn() != nullptr && kw_reg_shape(n, &E, &P);
 }
 
-#define KW_TMA_SWITCH(n, CALL)                                        \
-  switch (n) {                                                        \
+#define KW_TMA_SWITCH(n, CALL)                                                \
+  switch (n) {                                                                \
     case 64: return axis_variant() ? CALL(16, 4, 2, 2) : CALL(16, 4, 4, 1);    \
     case 128: return axis_variant() ? CALL(16, 8, 2, 2) : CALL(16, 8, 4, 1);   \
     case 256: return axis_variant() ? CALL(16, 16, 2, 2) : CALL(16, 16, 4, 1); \
-    case 512: return CALL(32, 16, 2, 1);                              \
-    case 1024: return CALL(32, 32, 2, 1);                             \
-    default: return cudaErrorInvalidValue;                            \
+    case 512: return CALL(32, 16, 2, 1);                                      \
+    case 1024: return CALL(32, 32, 2, 1);                                     \
+    default: return cudaErrorInvalidValue;                                    \
   }
 
 cudaError_t kw_tma_attr(int n) {
@@ -360,7 +432,8 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
   const int per_sm = (n <= 256 && axis_variant()) ? 2 : 1;
   const int grid = W.nunits < nsm * per_sm ? W.nunits : nsm * per_sm;
   const size_t smem = tma_smem(n, E, P);
-#define KW_T(E_, P_, S_, B_) (k_axis_tma<E_, P_, S_, B_><<<grid, 288, smem, st>>>(A, tp->maps[axis], W), cudaGetLastError())
+#define KW_T(E_, P_, S_, B_) \
+  (k_axis_tma<E_, P_, S_, B_><<<grid, 288, smem, st>>>(A, tp->maps[axis], W), cudaGetLastError())
   KW_TMA_SWITCH(n, KW_T)
 #undef KW_T
 }
