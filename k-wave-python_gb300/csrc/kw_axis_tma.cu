@@ -28,7 +28,7 @@ namespace {
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 struct TmaMaps {
-  CUtensorMap m[4];  // one per spectral buffer S0, S1, S2, P for the pass's axis
+  CUtensorMap m[KW_NBUF];  // one per spectral buffer (KwBuf) for the pass's axis
 };
 
 struct TmaWork {
@@ -36,7 +36,7 @@ struct TmaWork {
   int nouter;  // outer blocks (x planes for the 3-D y pass)
   int nunits;
   int nitems;  // items per unit
-  int inp[4];  // operator mode: distinct input buffers in job order
+  int inp[KW_MAX_JOBS];  // operator mode: distinct input buffers in job order
 };
 
 __device__ __forceinline__ bool consumers_any(bool pred) {

@@ -230,6 +230,16 @@ __device__ void apply_source(const RowsParams& P, const KwSrcDev& S, float* rbuf
   }
 }
 
+// Scatter a source's values at step t into a zeroed rbuf (the field whose
+// k-space corrected version is added, kspace_solver.py:93-101).
+__device__ void scatter_source(const RowsParams& P, const KwSrcDev& S, float* rbuf, int r0, int nr) {
+  const int e0 = S.row_ptr[r0], e1 = S.row_ptr[r0 + nr];
+  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int4 en = S.ent[e];
+    rbuf[(en.x - r0) * P.L + en.y] = S.sig[(long long)P.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+  }
+}
+
 __device__ void record_samples(const RowsParams& P, const float* rbuf, float* rec, int r0, int nr) {
   if (rec == nullptr || P.rec_row < 0 || P.sens_row_ptr == nullptr) return;
   const int e0 = P.sens_row_ptr[r0], e1 = P.sens_row_ptr[r0 + nr];
@@ -305,7 +315,15 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
         rb[0][i] = nu;
       }
       __syncthreads();
-      if (!P.init) apply_source(P, P.src[3 + a], rb[0], r0, nr);
+      if (!P.init) {
+        if (P.srcu_on[a]) {
+          // u_i += Re F^-1[source_kappa F[s_i]] (kspace_solver.py:91-98)
+          rf.c2r(P, P.S[B_SRCU0 + a], rb[1], r0, nr);
+          for (int i = threadIdx.x; i < tot; i += blockDim.x) rb[0][i] = __fadd_rn(rb[0][i], rb[1][i]);
+        } else {
+          apply_source(P, P.src[3 + a], rb[0], r0, nr);
+        }
+      }
       __syncthreads();
       for (int i = threadIdx.x; i < tot; i += blockDim.x) {
         const int row = i / L, z = i - row * L;
@@ -313,7 +331,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
         u[(long long)(r0 + row) * L + z] = rb[0][i];
       }
       record_samples(P, rb[0], P.rec[1 + a], r0, nr);
-      if (!P.init) rf.r2c(P, rb[0], P.S[a], r0, nr);
+      if (!P.init || P.init_r2c) rf.r2c(P, rb[0], P.S[a], r0, nr);
       __syncthreads();
     }
     return;
@@ -345,7 +363,14 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
       rb[3][i] = div;
     }
     __syncthreads();
-    for (int a = 0; a < D; ++a) apply_source(P, P.src[a], rb[a], r0, nr);
+    if (P.srcp_on) {
+      // rho_i += Re F^-1[source_kappa F[s]] / d_i (kspace_solver.py:91-98, scale :619-624)
+      rf.c2r(P, P.S[B_SRCP], rb[4], r0, nr);
+      for (int i = threadIdx.x; i < tot; i += blockDim.x)
+        for (int a = 0; a < D; ++a) rb[a][i] = __fadd_rn(rb[a][i], __fmul_rn(rb[4][i], P.inv_d[a]));
+    } else {
+      for (int a = 0; a < D; ++a) apply_source(P, P.src[a], rb[a], r0, nr);
+    }
     __syncthreads();
     const bool powerlaw = P.absorb == 1;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
@@ -387,6 +412,45 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
     } else {
       record_samples(P, rb[0], P.rec[0], r0, nr);
       rf.r2c(P, rb[0], P.S[3], r0, nr);
+    }
+    if (P.rec_us) {
+      // velocity on the pressure grid, Re F^-1[e^{-i k d/2} F[u_i]] (kspace_solver.py:740-743)
+      for (int a = 0; a < D; ++a) {
+        if (!(P.rec_us & (1 << a))) continue;
+        rf.c2r(P, P.S[B_US0 + a], rb[4], r0, nr);
+        record_samples(P, rb[4], P.rec[4 + a], r0, nr);
+        __syncthreads();
+      }
+    }
+    return;
+  }
+
+  if (P.stage == ST_SRC) {
+    // scattered source fields of this step, transformed for the source-kappa pass
+    if (P.srcp_on) {
+      for (int i = threadIdx.x; i < tot; i += blockDim.x) rb[0][i] = 0.f;
+      __syncthreads();
+      scatter_source(P, P.src[0], rb[0], r0, nr);
+      __syncthreads();
+      rf.r2c(P, rb[0], P.S[B_SRCP], r0, nr);
+    }
+    for (int a = 0; a < D; ++a) {
+      if (!P.srcu_on[a]) continue;
+      for (int i = threadIdx.x; i < tot; i += blockDim.x) rb[0][i] = 0.f;
+      __syncthreads();
+      scatter_source(P, P.src[3 + a], rb[0], r0, nr);
+      __syncthreads();
+      rf.r2c(P, rb[0], P.S[B_SRCU0 + a], r0, nr);
+    }
+    return;
+  }
+
+  if (P.stage == ST_UREC) {
+    for (int a = 0; a < D; ++a) {
+      if (!(P.rec_us & (1 << a))) continue;
+      rf.c2r(P, P.S[B_US0 + a], rb[0], r0, nr);
+      record_samples(P, rb[0], P.rec[4 + a], r0, nr);
+      __syncthreads();
     }
     return;
   }

@@ -20,11 +20,14 @@
 #pragma once
 #include "kw_fft.cuh"
 
-#define KW_NBUF 8
+#define KW_NBUF 12
+// spectral buffers: S0..S2 work spectra, P = spectrum of p, SRCP / SRCU0..2 =
+// k-space corrected source fields, US0..2 = velocity shifted to the pressure grid
+enum KwBuf { B_S0 = 0, B_P = 3, B_SRCP = 4, B_SRCU0 = 5, B_US0 = 8 };
 #define KW_MAX_JOBS 8
-#define KW_NREAL 4
+#define KW_NREAL 5
 
-enum KwStage { ST_INIT = 0, ST_U = 1, ST_RHO = 2, ST_EOS = 3 };
+enum KwStage { ST_INIT = 0, ST_U = 1, ST_RHO = 2, ST_EOS = 3, ST_SRC = 4, ST_UREC = 5 };
 enum KwOp { OP_GRAD = 0, OP_DIV = 1, OP_NAB1 = 2, OP_NAB2 = 3, OP_SKAPPA = 4, OP_UNSTAG = 5 };
 enum KwSrcMode { SRC_DIRICHLET = 0, SRC_ADDITIVE = 1, SRC_ADDITIVE_NC = 2 };
 
@@ -44,7 +47,12 @@ struct RowsParams {
   int nrows, R;
   int t, rec_row, write_p;
   int ex_stride;         // register-FFT rows: exchange region per row (complex values)
-  float2* S[4];          // spectral work buffers S0..S2 and P (index 3)
+  int srcp_on;           // k-space corrected pressure source active at this step
+  int srcu_on[3];        // k-space corrected velocity source active at this step
+  int rec_us;            // bit a: record u_a shifted to the pressure grid at this step
+  int init_r2c;          // ST_U with init: also transform u (for recording at t = 0)
+  float inv_d[3];        // 1 / d_i (pressure source correction per density component)
+  float2* S[KW_NBUF];    // spectral buffers (KwBuf)
   float* u[3];
   float* rho[3];
   float* p;

@@ -75,7 +75,7 @@ struct kw_plan {
   float* d_rho[3] = {nullptr, nullptr, nullptr};
   float* d_p = nullptr;
   float* d_rhosum = nullptr;
-  float2* d_S[4] = {nullptr, nullptr, nullptr, nullptr};
+  float2* d_S[KW_NBUF] = {nullptr};
   float* d_field[9] = {nullptr};
   float* d_tab[6][3] = {{nullptr}};
   float2* d_tw_axis[3] = {nullptr, nullptr, nullptr};
@@ -103,6 +103,8 @@ struct kw_plan {
   bool tma_axis[3] = {false, false, false};
   int nsm = 0;
   int rows_regP = 0, rows_regE = 0, rows_R = 0, rows_RS = 0;
+  // per-step flags passed to the row stages
+  int srcp_on = 0, srcu_on[3] = {0, 0, 0}, rec_us = 0, init_r2c = 0;
   // launch accounting / timing
   long long launches = 0;
   bool timing = false;
@@ -343,7 +345,7 @@ static int zero_state(kw_plan* p) {
     CK(cudaMemset(p->d_rho[a], 0, p->ntot * sizeof(float)));
   }
   CK(cudaMemset(p->d_p, 0, p->ntot * sizeof(float)));
-  for (int b = 0; b < 4; ++b)
+  for (int b = 0; b < KW_NBUF; ++b)
     if (p->d_S[b]) CK(cudaMemset(p->d_S[b], 0, p->spec_elems * sizeof(float2)));
   for (int s = 0; s < 7; ++s)
     if (p->d_rec[s]) CK(cudaMemset(p->d_rec[s], 0, (size_t)p->nrec * p->nslots * sizeof(float)));
@@ -361,11 +363,11 @@ int32_t kw_plan_finalize(kw_plan* p) {
       if (p->htab[tb][a].empty()) return fail(KW_ERR_INVALID, "table %d for axis %d not set", tb, a);
   }
   if (p->g.absorb_mode == 1 && !p->g.use_kspace && false) return KW_ERR_INVALID;
-  for (int sl = 0; sl < 6; ++sl)
-    if (p->hsrc[sl].set && p->hsrc[sl].mode == KW_SRC_ADDITIVE)
-      return fail(KW_ERR_UNSUPPORTED, "k-space corrected additive sources are not implemented yet");
-  if (p->record_mask & (0x70))
-    return fail(KW_ERR_UNSUPPORTED, "non-staggered velocity recording is not implemented yet");
+  // a k-space corrected pressure source is given once (slot P0, scaled without
+  // 1/d_i); the per-component factor 1/d_i is applied on the device
+  for (int sl = 1; sl < 3; ++sl)
+    if (p->hsrc[sl].set && p->hsrc[KW_S_P0].set && p->hsrc[KW_S_P0].mode == KW_SRC_ADDITIVE)
+      return fail(KW_ERR_INVALID, "a k-space corrected pressure source is set once, in slot KW_S_P0");
 
   // state and work buffers
   for (int a = 0; a < D; ++a) {
@@ -375,10 +377,15 @@ int32_t kw_plan_finalize(kw_plan* p) {
   if ((rc = dalloc(p, &p->d_p, p->ntot))) return rc;
   if (p->g.absorb_mode == 1)
     if ((rc = dalloc(p, &p->d_rhosum, p->ntot))) return rc;
-  for (int b = 0; b < 4; ++b) {
-    if (b < D || b == 3 || (b < 2 && p->g.absorb_mode == 1)) {
-      if ((rc = dalloc(p, &p->d_S[b], p->spec_elems))) return rc;
+  for (int b = 0; b < KW_NBUF; ++b) {
+    bool need = b < D || b == B_P || (b < 2 && p->g.absorb_mode == 1);
+    if (b == B_SRCP) need = p->hsrc[KW_S_P0].set && p->hsrc[KW_S_P0].mode == KW_SRC_ADDITIVE;
+    if (b >= B_SRCU0 && b < B_SRCU0 + 3) {
+      const HostSrc& h = p->hsrc[KW_S_U0 + (b - B_SRCU0)];
+      need = (b - B_SRCU0) < D && h.set && h.mode == KW_SRC_ADDITIVE;
     }
+    if (b >= B_US0 && b < B_US0 + 3) need = (b - B_US0) < D && (p->record_mask & (1 << (KW_R_UX + b - B_US0)));
+    if (need && (rc = dalloc(p, &p->d_S[b], p->spec_elems))) return rc;
   }
   // medium fields
   for (int f = 0; f < 9; ++f)
@@ -475,7 +482,7 @@ int32_t kw_plan_finalize(kw_plan* p) {
       int E, Pt;
       kw_reg_shape(p->N[a], &E, &Pt);
       bool ok = true;
-      for (int b = 0; b < 4; ++b) {
+      for (int b = 0; b < KW_NBUF; ++b) {
         if (!p->d_S[b]) continue;
         if (D == 3 && a == 0)
           ok &= kw_tma_encode(p->tma, 0, b, p->d_S[b], p->N[1] * p->Hp, p->N[0], (long long)p->N[1] * p->Hp, 1, 0, Pt);
@@ -526,8 +533,9 @@ static void fill_rows(const kw_plan* p, RowsParams& P) {
   P.even = p->even;
   P.nrows = p->nrows;
   P.R = p->R;
-  for (int b = 0; b < 4; ++b) P.S[b] = p->d_S[b];
+  for (int b = 0; b < KW_NBUF; ++b) P.S[b] = p->d_S[b];
   for (int a = 0; a < 3; ++a) {
+    P.inv_d[a] = a < p->D ? (float)(1.0 / p->g.spacing[a]) : 0.f;
     P.u[a] = p->d_u[a];
     P.rho[a] = p->d_rho[a];
     P.pml[a] = p->d_tab[KW_T_PML][a];
@@ -562,7 +570,41 @@ static void fill_rows(const kw_plan* p, RowsParams& P) {
   for (int s = 0; s < 7; ++s) P.rec[s] = p->d_rec[s];
 }
 
+// Host-side checks that every buffer a launch will touch exists: an internal
+// inconsistency becomes an error return instead of a device fault.
+static int need_buf(const kw_plan* p, int b, const char* what) {
+  if (b < 0 || b >= KW_NBUF || !p->d_S[b]) return fail(KW_ERR_STATE, "internal: spectrum %d (%s) not allocated", b, what);
+  return KW_OK;
+}
+
+static int check_rows(const kw_plan* p, int stage, int init) {
+  int rc;
+  const int D = p->D;
+  if (stage == ST_INIT && (rc = need_buf(p, B_P, "p"))) return rc;
+  if (stage == ST_U || stage == ST_RHO)
+    for (int a = 0; a < D; ++a)
+      if ((rc = need_buf(p, a, "work"))) return rc;
+  if (stage == ST_U && !init)
+    for (int a = 0; a < D; ++a)
+      if (p->srcu_on[a] && (rc = need_buf(p, B_SRCU0 + a, "velocity source"))) return rc;
+  if ((stage == ST_RHO || stage == ST_SRC) && p->srcp_on && (rc = need_buf(p, B_SRCP, "pressure source"))) return rc;
+  if (stage == ST_SRC)
+    for (int a = 0; a < D; ++a)
+      if (p->srcu_on[a] && (rc = need_buf(p, B_SRCU0 + a, "velocity source"))) return rc;
+  if (stage == ST_RHO || stage == ST_UREC)
+    for (int a = 0; a < D; ++a)
+      if (((p->rec_us >> a) & 1) && (rc = need_buf(p, B_US0 + a, "unstaggered velocity"))) return rc;
+  if (stage == ST_RHO || stage == ST_EOS) {
+    if ((rc = need_buf(p, B_P, "p"))) return rc;
+    if (p->g.absorb_mode == 1 && !p->d_rhosum) return fail(KW_ERR_STATE, "internal: density sum not allocated");
+  }
+  if ((p->rec_us || stage == ST_UREC) && p->nslots == 0) return fail(KW_ERR_STATE, "internal: no sensor slots");
+  return KW_OK;
+}
+
 static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cudaStream_t st) {
+  int crc = check_rows(p, stage, init);
+  if (crc) return crc;
   RowsParams P;
   fill_rows(p, P);
   P.stage = stage;
@@ -570,6 +612,10 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   P.t = t;
   P.rec_row = (t >= p->g.record_start) ? t - p->g.record_start : -1;
   P.write_p = write_p;
+  P.srcp_on = p->srcp_on;
+  for (int a = 0; a < 3; ++a) P.srcu_on[a] = p->srcu_on[a];
+  P.rec_us = p->rec_us;
+  P.init_r2c = p->init_r2c;
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
@@ -589,7 +635,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
 
 static void fill_axis_geom(const kw_plan* p, int axis, AxisParams& A) {
   memset(&A, 0, sizeof(A));
-  for (int b = 0; b < 4; ++b) A.bufs[b] = p->d_S[b];
+  for (int b = 0; b < KW_NBUF; ++b) A.bufs[b] = p->d_S[b];
   A.n = p->N[axis];
   A.flen = p->flen_axis[axis];
   A.tw = p->d_tw_axis[axis];
@@ -615,6 +661,10 @@ static void fill_axis_geom(const kw_plan* p, int axis, AxisParams& A) {
 }
 
 static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int nb, cudaStream_t st) {
+  for (int i = 0; i < nb; ++i) {
+    int rc = need_buf(p, bufs[i], "plain pass");
+    if (rc) return rc;
+  }
   AxisParams A;
   fill_axis_geom(p, axis, A);
   A.mode = inv ? 1 : 0;
@@ -638,6 +688,16 @@ static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int
 }
 
 static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t st) {
+  if (nj < 1 || nj > KW_MAX_JOBS) return fail(KW_ERR_STATE, "internal: %d operator jobs", nj);
+  for (int i = 0; i < nj; ++i) {
+    int rc = need_buf(p, jobs[i].in, "operator input");
+    if (!rc) rc = need_buf(p, jobs[i].out, "operator output");
+    if (rc) return rc;
+    if (jobs[i].axis < 0 || jobs[i].axis >= p->D) return fail(KW_ERR_STATE, "internal: job axis %d", jobs[i].axis);
+    const int tb = jobs[i].op == OP_GRAD ? KW_T_OPGRAD : jobs[i].op == OP_DIV ? KW_T_OPDIV
+                 : jobs[i].op == OP_UNSTAG ? KW_T_UNSTAG : -1;
+    if (tb >= 0 && !p->d_tab[tb][jobs[i].axis]) return fail(KW_ERR_STATE, "internal: operator table %d missing", tb);
+  }
   AxisParams A;
   fill_axis_geom(p, 0, A);
   A.mode = 2;
@@ -671,33 +731,94 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
   return ev_end(p, st, KW_K_AXIS_OPS, slot);
 }
 
+// Source-kappa pass over the scattered source fields of step t
+// (kspace_solver.py:91-98): rows -> [y] -> x with source_kappa -> [y^-1].
+static int enqueue_sources(kw_plan* p, int t, cudaStream_t st) {
+  const bool three = p->D == 3;
+  int bufs[4], nb = 0;
+  if (p->srcp_on) bufs[nb++] = B_SRCP;
+  for (int a = 0; a < p->D; ++a)
+    if (p->srcu_on[a]) bufs[nb++] = B_SRCU0 + a;
+  if (!nb) return KW_OK;
+  int rc;
+  if ((rc = launch_rows(p, ST_SRC, 0, t, 0, st))) return rc;
+  if (three && (rc = launch_axis_plain(p, 1, 0, bufs, nb, st))) return rc;
+  AxisJob jobs[KW_MAX_JOBS];
+  for (int i = 0; i < nb; ++i) jobs[i] = AxisJob{bufs[i], bufs[i], OP_SKAPPA, 0};
+  if ((rc = launch_axis_ops(p, jobs, nb, st))) return rc;
+  if (three && (rc = launch_axis_plain(p, 1, 1, bufs, nb, st))) return rc;
+  return KW_OK;
+}
+
+static void set_step_flags(kw_plan* p, int t) {
+  const HostSrc& hp = p->hsrc[KW_S_P0];
+  p->srcp_on = hp.set && hp.mode == KW_SRC_ADDITIVE && t < hp.len;
+  for (int a = 0; a < 3; ++a) {
+    const HostSrc& h = p->hsrc[KW_S_U0 + a];
+    p->srcu_on[a] = a < p->D && h.set && h.mode == KW_SRC_ADDITIVE && t < h.len;
+  }
+  // bit a: u_a on the pressure grid is recorded (its spectrum buffer exists)
+  p->rec_us = (t >= p->g.record_start) ? (p->record_mask >> KW_R_UX) & 0x7 : 0;
+  p->init_r2c = 0;
+}
+
 static int enqueue_step(kw_plan* p, int t, bool last, cudaStream_t st) {
   const int D = p->D;
   const bool three = D == 3;
   int rc;
   const int SB[3] = {0, 1, 2};
-  const int PB[1] = {3};
+  const int PB[1] = {B_P};
+  // work spectra plus the recorded unstaggered-velocity spectra
+  int SUB[6], nus = 0;
+  for (int a = 0; a < D; ++a) SUB[a] = a;
+  for (int a = 0; a < D; ++a)
+    if ((p->record_mask >> (KW_R_UX + a)) & 1) SUB[D + nus++] = B_US0 + a;
   AxisJob jobs[KW_MAX_JOBS];
   const bool has_p0 = !p->hfield[KW_F_P0].empty();
+  set_step_flags(p, t);
   if (t == 0 && has_p0) {
-    // initial condition override (kspace_solver.py:725-733)
+    // initial condition override (kspace_solver.py:725-733); sources of step 0 are overwritten
+    const int rec_us = p->rec_us;
+    p->srcp_on = 0;
+    p->srcu_on[0] = p->srcu_on[1] = p->srcu_on[2] = 0;
+    p->rec_us = 0;
     if ((rc = launch_rows(p, ST_INIT, 0, t, 1, st))) return rc;
     if (three && (rc = launch_axis_plain(p, 1, 0, PB, 1, st))) return rc;
-    for (int a = 0; a < D; ++a) jobs[a] = AxisJob{3, a, OP_GRAD, a};
+    for (int a = 0; a < D; ++a) jobs[a] = AxisJob{B_P, a, OP_GRAD, a};
     if ((rc = launch_axis_ops(p, jobs, D, st))) return rc;
     if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) return rc;
-    return launch_rows(p, ST_U, 1, t, 0, st);
+    p->init_r2c = rec_us;
+    if ((rc = launch_rows(p, ST_U, 1, t, 0, st))) return rc;
+    p->init_r2c = 0;
+    if (rec_us) {
+      // velocity on the pressure grid at t = 0 (kspace_solver.py:740-743)
+      if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) return rc;
+      int nj = 0;
+      for (int a = 0; a < D; ++a)
+        if ((rec_us >> a) & 1) jobs[nj++] = AxisJob{a, B_US0 + a, OP_UNSTAG, a};
+      if ((rc = launch_axis_ops(p, jobs, nj, st))) return rc;
+      if (three && (rc = launch_axis_plain(p, 1, 1, SUB + D, nus, st))) return rc;
+      p->rec_us = rec_us;
+      if ((rc = launch_rows(p, ST_UREC, 0, t, 0, st))) return rc;
+      p->rec_us = 0;
+    }
+    return KW_OK;
   }
+  if ((rc = enqueue_sources(p, t, st))) return rc;
   // momentum
-  for (int a = 0; a < D; ++a) jobs[a] = AxisJob{3, a, OP_GRAD, a};
+  for (int a = 0; a < D; ++a) jobs[a] = AxisJob{B_P, a, OP_GRAD, a};
   if ((rc = launch_axis_ops(p, jobs, D, st))) return rc;
   if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) return rc;
   if ((rc = launch_rows(p, ST_U, 0, t, 0, st))) return rc;
-  // mass conservation
+  // mass conservation (+ velocity on the pressure grid when recorded)
   if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) return rc;
-  for (int a = 0; a < D; ++a) jobs[a] = AxisJob{a, a, OP_DIV, a};
-  if ((rc = launch_axis_ops(p, jobs, D, st))) return rc;
-  if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) return rc;
+  int nj = 0;
+  for (int a = 0; a < D; ++a) {
+    jobs[nj++] = AxisJob{a, a, OP_DIV, a};
+    if ((p->rec_us >> a) & 1) jobs[nj++] = AxisJob{a, B_US0 + a, OP_UNSTAG, a};
+  }
+  if ((rc = launch_axis_ops(p, jobs, nj, st))) return rc;
+  if (three && (rc = launch_axis_plain(p, 1, 1, SUB, p->rec_us ? D + nus : D, st))) return rc;
   const bool powerlaw = p->g.absorb_mode == 1;
   if ((rc = launch_rows(p, ST_RHO, 0, t, (!powerlaw && last) ? 1 : 0, st))) return rc;
   if (powerlaw) {

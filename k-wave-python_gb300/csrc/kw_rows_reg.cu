@@ -106,6 +106,30 @@ struct RowCtx {
     }
   }
 
+  // values of a source at step t on this row, zero elsewhere (the field whose
+  // k-space corrected version is added)
+  __device__ __forceinline__ void scatter(const KwSrcDev& S, float2 (&v)[E]) const {
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = make_float2(0.f, 0.f);
+    if (!ok) return;
+    const int e0 = S.row_ptr[grow], e1 = S.row_ptr[grow + 1];
+    for (int e = e0; e < e1; ++e) {
+      const int4 en = S.ent[e];
+      const int n = en.y >> 1;
+      if ((n % P) != t) continue;
+      const int jj = n / P;
+      const float val = S.sig[(long long)Q.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+#pragma unroll
+      for (int j = 0; j < E; ++j)
+        if (j == jj) {
+          if (en.y & 1)
+            v[j].y = val;
+          else
+            v[j].x = val;
+        }
+    }
+  }
+
   __device__ __forceinline__ void record(const float2 (&v)[E], float* rec) const {
     if (rec == nullptr || Q.rec_row < 0 || Q.sens_row_ptr == nullptr || !ok) return;
     const int e0 = Q.sens_row_ptr[grow], e1 = Q.sens_row_ptr[grow + 1];
@@ -123,6 +147,17 @@ struct RowCtx {
     }
   }
 };
+
+// velocity on the pressure grid, Re F^-1[e^{-i k d/2} F[u_i]] (kspace_solver.py:740-743)
+template <int E, int P>
+__device__ __forceinline__ void record_unstaggered(const RowCtx<E, P>& c, const RowsParams& Q, float2 (&v)[E]) {
+  if (!Q.rec_us) return;
+  for (int a = 0; a < Q.ndim; ++a) {
+    if (!(Q.rec_us & (1 << a))) continue;
+    c.c2r(Q.S[B_US0 + a], v);
+    c.record(v, Q.rec[4 + a]);
+  }
+}
 
 }  // namespace
 
@@ -185,13 +220,23 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
                              __fmul_rn(sg.y, __fsub_rn(__fmul_rn(sg.y, u.y), __fmul_rn(dtr.y, g.y))));
         }
       }
-      if (!Q.init) c.source(Q.src[3 + a], v);
+      if (!Q.init) {
+        if (Q.srcu_on[a]) {
+          // u_i += Re F^-1[source_kappa F[s_i]] (kspace_solver.py:91-98)
+          float2 w[E];
+          c.c2r(Q.S[B_SRCU0 + a], w);
+#pragma unroll
+          for (int j = 0; j < E; ++j) v[j] = make_float2(__fadd_rn(v[j].x, w[j].x), __fadd_rn(v[j].y, w[j].y));
+        } else {
+          c.source(Q.src[3 + a], v);
+        }
+      }
       if (c.ok) {
 #pragma unroll
         for (int j = 0; j < E; ++j) st2(Q.u[a], c.rbase + t + P * j, v[j]);
       }
       c.record(v, Q.rec[1 + a]);
-      if (!Q.init) c.r2c(v, Q.S[a]);
+      if (!Q.init || Q.init_r2c) c.r2c(v, Q.S[a]);
     }
     return;
   }
@@ -216,6 +261,8 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
                             __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v.y), r0v.y));
       }
     }
+    float2 cp[E];
+    if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
     for (int a = 0; a < D; ++a) {
       c.c2r(Q.S[a], v);
 #pragma unroll
@@ -233,7 +280,15 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
         v[j] = make_float2(__fmul_rn(pm.x, __fsub_rn(__fmul_rn(pm.x, ro.x), tx)),
                            __fmul_rn(pm.y, __fsub_rn(__fmul_rn(pm.y, ro.y), ty)));
       }
-      c.source(Q.src[a], v);
+      if (Q.srcp_on) {
+        // rho_i += Re F^-1[source_kappa F[s]] / d_i (kspace_solver.py:91-98, scale :619-624)
+        const float id = Q.inv_d[a];
+#pragma unroll
+        for (int j = 0; j < E; ++j)
+          v[j] = make_float2(__fadd_rn(v[j].x, __fmul_rn(cp[j].x, id)), __fadd_rn(v[j].y, __fmul_rn(cp[j].y, id)));
+      } else {
+        c.source(Q.src[a], v);
+      }
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         if (c.ok) st2(Q.rho[a], c.rbase + t + P * j, v[j]);
@@ -255,6 +310,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
       }
       c.r2c(v, Q.S[0]);
       if (Q.disp) c.r2c(rs, Q.S[1]);
+      record_unstaggered(c, Q, v);
       return;
     }
     // equation of state without fractional Laplacians (kspace_solver.py:719-723)
@@ -283,6 +339,26 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     }
     c.record(v, Q.rec[0]);
     c.r2c(v, Q.S[3]);
+    record_unstaggered(c, Q, v);
+    return;
+  }
+
+  if constexpr (STAGE == ST_SRC) {
+    // scattered source fields of this step, transformed for the source-kappa pass
+    if (Q.srcp_on) {
+      c.scatter(Q.src[0], v);
+      c.r2c(v, Q.S[B_SRCP]);
+    }
+    for (int a = 0; a < D; ++a)
+      if (Q.srcu_on[a]) {
+        c.scatter(Q.src[3 + a], v);
+        c.r2c(v, Q.S[B_SRCU0 + a]);
+      }
+    return;
+  }
+
+  if constexpr (STAGE == ST_UREC) {
+    record_unstaggered(c, Q, v);
     return;
   }
 
@@ -328,7 +404,9 @@ static cudaError_t rows_v2_launch(int stage, dim3 grid, size_t smem, cudaStream_
     case ST_INIT: k_rows_v2<E, P, ST_INIT><<<grid, 128, smem, st>>>(Q); break;
     case ST_U: k_rows_v2<E, P, ST_U><<<grid, 128, smem, st>>>(Q); break;
     case ST_RHO: k_rows_v2<E, P, ST_RHO><<<grid, 128, smem, st>>>(Q); break;
-    default: k_rows_v2<E, P, ST_EOS><<<grid, 128, smem, st>>>(Q); break;
+    case ST_EOS: k_rows_v2<E, P, ST_EOS><<<grid, 128, smem, st>>>(Q); break;
+    case ST_SRC: k_rows_v2<E, P, ST_SRC><<<grid, 128, smem, st>>>(Q); break;
+    default: k_rows_v2<E, P, ST_UREC><<<grid, 128, smem, st>>>(Q); break;
   }
   return cudaGetLastError();
 }
@@ -341,6 +419,8 @@ static cudaError_t rows_v2_attr() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_U>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_RHO>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_EOS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_UREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   return e;
 }
 

@@ -452,9 +452,13 @@ def _build_sources(prob, shape, spacing, dt, c0, ndim):
         idx = _mask_index(pm, shape)
         sig = _signal_rows(ps)
         c = c_at(idx)
-        for i in range(n):
-            scale = 1.0 / (n * c ** 2) if pmode == "dirichlet" else 2 * dt / (n * c * spacing[i])
-            out.append(SourceSpec(i, pmode, idx, _scaled(sig, scale, idx.size)))
+        if pmode == "additive":
+            # one field 2 dt / (n c0) s; the device adds F^-1[source_kappa F[.]] / d_i to rho_i
+            out.append(SourceSpec(0, pmode, idx, _scaled(sig, 2 * dt / (n * c), idx.size)))
+        else:
+            for i in range(n):
+                scale = 1.0 / (n * c ** 2) if pmode == "dirichlet" else 2 * dt / (n * c * spacing[i])
+                out.append(SourceSpec(i, pmode, idx, _scaled(sig, scale, idx.size)))
     um = prob.get("u_mask", 0)
     umode = prob.get("u_mode", None) or "additive"
     for i, v in enumerate(("ux", "uy", "uz")[:n]):

@@ -196,9 +196,6 @@ class Simulation:
     # -- setup / stepping ---------------------------------------------------
     def setup(self):
         self.S = build_setup(self.prob)
-        unsupported = [k for k in self.S.record if k.startswith("I") or k in ("ux", "uy", "uz")]
-        if unsupported:
-            raise NotImplementedError(f"recording {sorted(unsupported)} is not available on the GB300 backend yet")
         self._plan = DevicePlan(self.S, stream=self.stream)
         self.t = 0
         return self
@@ -249,6 +246,11 @@ class Simulation:
             for suf, kind in (("_max", K.KW_AGG_MAX), ("_min", K.KW_AGG_MIN), ("_rms", K.KW_AGG_RMS)):
                 if key + suf in S.requested:
                     out[key + suf] = plan.read_aggregate(sid, kind)
+        if any(k.startswith("I") for k in S.requested):
+            series = {"p": plan.read_series(K.KW_R_P)}
+            for i, a in enumerate(AXES[: S.ndim]):
+                series[f"u{a}"] = plan.read_series(K.KW_R_UX + i)
+            out.update(acoustic_intensity(series))
         interior = tuple(slice(s, N - s if s else None) for s, N in zip(S.pml_sizes, S.shape))
         if "p_final" in S.requested:
             out["p_final"] = plan.read_field(K.KW_FLD_P)[interior].copy()
@@ -261,6 +263,27 @@ class Simulation:
         if self._plan is not None:
             self._plan.close()
             self._plan = None
+
+
+def acoustic_intensity(result):
+    """Intensity from the recorded p and non-staggered u series: u is shifted
+    forward half a time step by a temporal Fourier interpolant, then I = p u
+    and its time average (kwave/solvers/kspace_solver.py:840-862).  This is
+    post-processing of the returned series, done on the host as in the
+    reference."""
+    p = result["p"]
+    n = p.shape[-1]
+    freq = 2 * np.pi * np.arange(-(n // 2), n - n // 2) / n
+    shift = np.fft.ifftshift(np.exp(1j * freq * 0.5))
+    out = {}
+    for a in "xyz":
+        u = result.get(f"u{a}")
+        if u is None:
+            continue
+        us = np.real(np.fft.ifft(shift * np.fft.fft(u, axis=-1), axis=-1))
+        out[f"I{a}"] = p * us
+        out[f"I{a}_avg"] = np.mean(out[f"I{a}"], axis=-1)
+    return out
 
 
 def run_problem(prob, stream=None):

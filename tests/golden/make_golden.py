@@ -239,6 +239,64 @@ def case_nosensor2d():
     return base(sh, (1e-4, 1e-4), 2e-8, 10, p0=gaussian_blobs(sh, 2, rng), pml_size=(4, 4))
 
 
+def case_intensity2d():
+    """p0 with velocity and intensity recording (non-staggered u from t = 0)."""
+    rng = np.random.default_rng(31)
+    sh = (48, 40)
+    mask = np.zeros(sh, bool)
+    mask[30:34, 10:30:3] = True
+    return base(sh, (1e-4, 1e-4), 2e-8, 50, p0=gaussian_blobs(sh, 3, rng), sensor_mask=mask,
+                record=("p", "u", "I", "I_avg", "ux_rms"), sound_speed=smooth_random_field(sh, rng, rel=0.04),
+                pml_size=(8, 8))
+
+
+def case_src3d():
+    """3-D k-space corrected pressure and velocity sources, non-staggered u, record_start_index."""
+    rng = np.random.default_rng(32)
+    sh = (24, 20, 16)
+    pmask = np.zeros(sh, bool)
+    pmask[8, 6:14:2, 8] = True
+    umask = np.zeros(sh, bool)
+    umask[14, 10, 4:12] = True
+    smask = np.zeros(sh, bool)
+    smask[4:20:3, 10, 8] = True
+    return base(sh, (1e-4,) * 3, 2e-8, 40, sound_speed=smooth_random_field(sh, rng, rel=0.04),
+                density=smooth_random_field(sh, rng, rel=0.03, base=1000.0),
+                p_mask=pmask, p=tone_burst_rows(int(pmask.sum()), 25, 2e-8, 3e6, 2, rng), p_mode="additive",
+                u_mask=umask, ux=tone_burst_rows(1, 20, 2e-8, 3e6, 2, rng, max_delay=1) * 1e-3, u_mode="additive",
+                sensor_mask=smask, record=("p", "ux", "uz_staggered", "p_final"), record_start_index=5,
+                pml_size=(4, 4, 4))
+
+
+def case_pow2_2d_src():
+    """Power-of-two grid (register/TMA kernels): additive corrected p source, dirichlet u source."""
+    rng = np.random.default_rng(33)
+    sh = (64, 128)
+    pmask = np.zeros(sh, bool)
+    pmask[20, 40:80:4] = True
+    umask = np.zeros(sh, bool)
+    umask[40:42, 60:64] = True
+    smask = np.zeros(sh, bool)
+    smask[30, :] = True
+    return base(sh, (1e-4, 1e-4), 2e-8, 60, sound_speed=smooth_random_field(sh, rng, rel=0.04),
+                alpha_coeff=0.5, alpha_power=1.1,
+                p_mask=pmask, p=tone_burst_rows(int(pmask.sum()), 30, 2e-8, 3e6, 2, rng), p_mode="additive",
+                u_mask=umask, uy=tone_burst_rows(1, 20, 2e-8, 3e6, 2, rng, max_delay=1) * 1e-3, u_mode="dirichlet",
+                sensor_mask=smask, record=("p", "u", "p_max", "p_final"), pml_size=(8, 8))
+
+
+def case_pow2_3d():
+    """Power-of-two 3-D grid with the headline physics plus Cartesian sensors and u."""
+    rng = np.random.default_rng(34)
+    sh = (64, 64, 64)
+    c = smooth_random_field(sh, rng, rel=0.05)
+    rho = smooth_random_field(sh, rng, rel=0.04, base=1000.0)
+    cart = rng.uniform(-2.5e-3, 2.5e-3, size=(3, 12))
+    return base(sh, (1e-4,) * 3, 2e-8, 30, sound_speed=c, density=rho, alpha_coeff=0.75, alpha_power=1.5, BonA=6.0,
+                p0=gaussian_blobs(sh, 5, rng, sigma=(2.0, 4.0)), smooth_p0=True, sensor_mask=cart,
+                record=("p", "u", "p_rms", "p_final"), pml_size=(10, 10, 10))
+
+
 def case_cfg2_mini():
     """Config-2 physics (heterogeneous, power law y=1.5, BonA 6, 10-pt PML, z-plane sensor) at 48^3."""
     from bench import config2_problem
@@ -259,6 +317,10 @@ CASES = {
     "nodisp2d": case_nodisp2d,
     "nosensor2d": case_nosensor2d,
     "cfg2_mini": case_cfg2_mini,
+    "intensity2d": case_intensity2d,
+    "src3d_additive": case_src3d,
+    "pow2_2d_src": case_pow2_2d_src,
+    "pow2_3d": case_pow2_3d,
 }
 
 

@@ -21,10 +21,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5  # relative L2 against the float32 reference
 
 # features the device path does not provide yet
-PENDING = {
-    "src2d_additive": "k-space corrected additive pressure source",
-    "src2d_velocity": "k-space corrected additive velocity source / non-staggered u",
-}
+PENDING = {}
 
 
 def rel_l2(a, b):
