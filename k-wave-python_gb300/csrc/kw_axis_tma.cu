@@ -39,15 +39,16 @@ struct TmaWork {
   int inp[KW_MAX_JOBS];  // operator mode: distinct input buffers in job order
 };
 
-__device__ __forceinline__ bool consumers_any(bool pred) {
+// OR-reduction of pred over the n consumer threads (named barrier 1)
+__device__ __forceinline__ bool consumers_any(bool pred, int n) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\t"
       "setp.ne.u32 q, %1, 0;\n\t"
-      "bar.red.or.pred p, 1, 256, q;\n\t"
+      "bar.red.or.pred p, 1, %2, q;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(r)
-      : "r"((uint32_t)pred)
+      : "r"((uint32_t)pred), "r"(n)
       : "memory");
   return r != 0;
 }
@@ -116,10 +117,11 @@ __device__ __forceinline__ float2 col_factor(const AxisParams& A, const AxisJob&
 
 }  // namespace
 
-template <int E, int P, int NST, int MINB>
-__global__ void __launch_bounds__(288, MINB)
+// T columns per tile, CT = T * P consumer threads plus one producer warp.
+template <int E, int P, int NST, int MINB, int T>
+__global__ void __launch_bounds__(T * P + 32, MINB)
     k_axis_tma(const __grid_constant__ AxisParams A, const __grid_constant__ TmaMaps maps, const TmaWork W) {
-  constexpr int N = E * P, T = 256 / P, RS = N + E + 1;
+  constexpr int N = E * P, RS = N + E + 1, CT = T * P;
   constexpr uint32_t kStageBytes = N * T * sizeof(float2);
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* stages = reinterpret_cast<float2*>(smem_raw);  // NST * N * T
@@ -138,7 +140,7 @@ __global__ void __launch_bounds__(288, MINB)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       kwtma::mbar_init(&full[s], 1);
-      kwtma::mbar_init(&empty[s], 8);
+      kwtma::mbar_init(&empty[s], CT / 32);
     }
     counters[0] = counters[1] = 0;
     kwtma::fence_barrier_init();
@@ -157,7 +159,7 @@ __global__ void __launch_bounds__(288, MINB)
   const TabX f0s{kTablesInSmem ? f0t : A.fg[0], kTablesInSmem ? f0t + N : A.fd[0], kTablesInSmem ? f0t + 2 * N : A.us[0]};
 
   const bool plain = A.mode < 2;
-  if (warp == 8) {
+  if (warp == CT / 32) {
     // ---------------- producer ----------------
     if (lane == 0) {
       uint32_t it = 0;
@@ -187,7 +189,7 @@ __global__ void __launch_bounds__(288, MINB)
   } else {
     // ---------------- consumers ----------------
     const int cc = tid % T, t = tid / T;
-    auto sync = [] __device__() { kwtma::named_sync(256); };
+    auto sync = [] __device__() { kwtma::named_sync(CT); };
     uint32_t it = 0;
     bool aborted = false;
     for (int u = blockIdx.x; u < W.nunits && !aborted; u += gridDim.x) {
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(288, MINB)
       for (int q = 0; q < W.nitems; ++q, ++it) {
         const uint32_t s = it % NST, k = it / NST;
         const bool got = kwtma::mbar_wait(&full[s], k & 1, kWaitLimitNs);
-        if (consumers_any(!got)) {
+        if (consumers_any(!got, CT)) {
           if (tid == 0) atomicExch(&g_kw_device_error, 2);
           aborted = true;
           break;
@@ -348,8 +350,13 @@ static int axis_variant() {
 }
 static int stages_for(int n) { return (n <= 256 && !axis_variant()) ? 4 : 2; }
 
-static size_t tma_smem(int n, int E, int P) {
-  const int T = 256 / P, RS = n + E + 1;
+// Tile width: plain passes along y of a 3-D grid (axis 1) use narrow 8-column
+// tiles at three CTAs per SM for length 256; everything else 256 / P columns.
+static bool narrow(int n, int axis) { return n == 256 && axis == 1 && axis_variant(); }
+static int tile_cols(int n, int P, int axis) { return narrow(n, axis) ? 8 : 256 / P; }
+
+static size_t tma_smem(int n, int E, int P, int axis) {
+  const int T = tile_cols(n, P, axis), RS = n + E + 1;
   const size_t nt = n <= 512 ? (size_t)n : 0;
   return sizeof(float2) * ((size_t)stages_for(n) * n * T + (size_t)T * RS + n + 3 * nt) + sizeof(float) * nt +
          2 * 4 * sizeof(uint64_t) + 16;
@@ -370,7 +377,7 @@ bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long 
   KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
   EncodeTiledFn fn = encode_fn();
   if (!fn || !base) return false;
-  const int T = 256 / P;
+  const int T = tile_cols(n, P, axis);
   cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)n, (cuuint64_t)nouter};
   cuuint64_t strides[2] = {(cuuint64_t)xs * 8, (cuuint64_t)(nouter > 1 ? os : xs * n) * 8};
   cuuint32_t box[3] = {(cuuint32_t)T, (cuuint32_t)(n < 256 ? n : 256), 1};
@@ -386,22 +393,24 @@ bool kw_tma_supported(int n) {
   return encode_fn() != nullptr && kw_reg_shape(n, &E, &P);
 }
 
-#define KW_TMA_SWITCH(n, CALL)                                                \
-  switch (n) {                                                                \
-    case 64: return axis_variant() ? CALL(16, 4, 2, 2) : CALL(16, 4, 4, 1);    \
-    case 128: return axis_variant() ? CALL(16, 8, 2, 2) : CALL(16, 8, 4, 1);   \
-    case 256: return axis_variant() ? CALL(16, 16, 2, 2) : CALL(16, 16, 4, 1); \
-    case 512: return CALL(32, 16, 2, 1);                                      \
-    case 1024: return CALL(32, 32, 2, 1);                                     \
-    default: return cudaErrorInvalidValue;                                    \
+#define KW_TMA_SWITCH(n, CALL)                                                           \
+  switch (n) {                                                                           \
+    case 64: return axis_variant() ? CALL(16, 4, 2, 2, 64) : CALL(16, 4, 4, 1, 64);       \
+    case 128: return axis_variant() ? CALL(16, 8, 2, 2, 32) : CALL(16, 8, 4, 1, 32);      \
+    case 256:                                                                            \
+      if (narrow(n, axis)) return CALL(16, 16, 2, 3, 8);                                 \
+      return axis_variant() ? CALL(16, 16, 2, 2, 16) : CALL(16, 16, 4, 1, 16);            \
+    case 512: return CALL(32, 16, 2, 1, 16);                                             \
+    case 1024: return CALL(32, 32, 2, 1, 8);                                             \
+    default: return cudaErrorInvalidValue;                                               \
   }
 
-cudaError_t kw_tma_attr(int n) {
+cudaError_t kw_tma_attr(int n, int axis) {
   int E, P;
   if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
-  const int smem = (int)tma_smem(n, E, P);
-#define KW_T(E_, P_, S_, B_) \
-  cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+  const int smem = (int)tma_smem(n, E, P, axis);
+#define KW_T(E_, P_, S_, B_, T_) \
+  cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
   KW_TMA_SWITCH(n, KW_T)
 #undef KW_T
 }
@@ -412,7 +421,7 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
   KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
   int E, P;
   if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
-  const int T = 256 / P;
+  const int T = tile_cols(n, P, axis);
   TmaWork W;
   W.ntile = (A.ncols + T - 1) / T;
   W.nouter = nouter;
@@ -429,11 +438,11 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
     W.nitems = ni;
     W.nunits = W.ntile * nouter;
   }
-  const int per_sm = (n <= 256 && axis_variant()) ? 2 : 1;
+  const int per_sm = narrow(n, axis) ? 3 : ((n <= 256 && axis_variant()) ? 2 : 1);
   const int grid = W.nunits < nsm * per_sm ? W.nunits : nsm * per_sm;
-  const size_t smem = tma_smem(n, E, P);
-#define KW_T(E_, P_, S_, B_) \
-  (k_axis_tma<E_, P_, S_, B_><<<grid, 288, smem, st>>>(A, tp->maps[axis], W), cudaGetLastError())
+  const size_t smem = tma_smem(n, E, P, axis);
+#define KW_T(E_, P_, S_, B_, T_) \
+  (k_axis_tma<E_, P_, S_, B_, T_><<<grid, T_ * P_ + 32, smem, st>>>(A, tp->maps[axis], W), cudaGetLastError())
   KW_TMA_SWITCH(n, KW_T)
 #undef KW_T
 }

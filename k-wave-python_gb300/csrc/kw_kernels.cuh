@@ -155,7 +155,7 @@ void* kw_tma_plan_create();
 void kw_tma_plan_destroy(void* h);
 bool kw_tma_supported(int n);
 bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long long xs, int nouter, long long os, int P);
-cudaError_t kw_tma_attr(int n);
+cudaError_t kw_tma_attr(int n, int axis);
 cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A);
 // Returns and clears the device error word (nonzero: a bounded device wait timed out).
 int kw_device_error_take();

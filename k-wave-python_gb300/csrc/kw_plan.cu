@@ -492,7 +492,7 @@ int32_t kw_plan_finalize(kw_plan* p) {
           ok &= kw_tma_encode(p->tma, 0, b, p->d_S[b], p->Hp, p->N[0], p->Hp, 1, 0, Pt);
       }
       if (ok) {
-        CK(kw_tma_attr(p->N[a]));
+        CK(kw_tma_attr(p->N[a], D == 3 ? a : 0));
         p->tma_axis[a] = true;
       }
     }

@@ -161,7 +161,10 @@ __device__ __forceinline__ void record_unstaggered(const RowCtx<E, P>& c, const 
 
 }  // namespace
 
-template <int E, int P, int STAGE>
+// EXTRA: this launch has k-space corrected sources or records the velocity on
+// the pressure grid; without it those paths are compiled out, which keeps the
+// common launch at its smaller register budget.
+template <int E, int P, int STAGE, bool EXTRA>
 __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsParams Q) {
   constexpr int M = E * P;
   extern __shared__ float4 smem_f4[];
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
         }
       }
       if (!Q.init) {
-        if (Q.srcu_on[a]) {
+        if (EXTRA && Q.srcu_on[a]) {
           // u_i += Re F^-1[source_kappa F[s_i]] (kspace_solver.py:91-98)
           float2 w[E];
           c.c2r(Q.S[B_SRCU0 + a], w);
@@ -261,8 +264,10 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
                             __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v.y), r0v.y));
       }
     }
-    float2 cp[E];
-    if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
+    float2 cp[EXTRA ? E : 1];
+    if constexpr (EXTRA) {
+      if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
+    }
     for (int a = 0; a < D; ++a) {
       c.c2r(Q.S[a], v);
 #pragma unroll
@@ -280,15 +285,18 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
         v[j] = make_float2(__fmul_rn(pm.x, __fsub_rn(__fmul_rn(pm.x, ro.x), tx)),
                            __fmul_rn(pm.y, __fsub_rn(__fmul_rn(pm.y, ro.y), ty)));
       }
-      if (Q.srcp_on) {
-        // rho_i += Re F^-1[source_kappa F[s]] / d_i (kspace_solver.py:91-98, scale :619-624)
-        const float id = Q.inv_d[a];
+      bool corrected = false;
+      if constexpr (EXTRA) {
+        if (Q.srcp_on) {
+          // rho_i += Re F^-1[source_kappa F[s]] / d_i (kspace_solver.py:91-98, scale :619-624)
+          const float id = Q.inv_d[a];
 #pragma unroll
-        for (int j = 0; j < E; ++j)
-          v[j] = make_float2(__fadd_rn(v[j].x, __fmul_rn(cp[j].x, id)), __fadd_rn(v[j].y, __fmul_rn(cp[j].y, id)));
-      } else {
-        c.source(Q.src[a], v);
+          for (int j = 0; j < E; ++j)
+            v[j] = make_float2(__fadd_rn(v[j].x, __fmul_rn(cp[j].x, id)), __fadd_rn(v[j].y, __fmul_rn(cp[j].y, id)));
+          corrected = true;
+        }
       }
+      if (!corrected) c.source(Q.src[a], v);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         if (c.ok) st2(Q.rho[a], c.rbase + t + P * j, v[j]);
@@ -310,7 +318,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
       }
       c.r2c(v, Q.S[0]);
       if (Q.disp) c.r2c(rs, Q.S[1]);
-      record_unstaggered(c, Q, v);
+      if constexpr (EXTRA) record_unstaggered(c, Q, v);
       return;
     }
     // equation of state without fractional Laplacians (kspace_solver.py:719-723)
@@ -339,7 +347,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     }
     c.record(v, Q.rec[0]);
     c.r2c(v, Q.S[3]);
-    record_unstaggered(c, Q, v);
+    if constexpr (EXTRA) record_unstaggered(c, Q, v);
     return;
   }
 
@@ -398,30 +406,43 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
   }
 }
 
-template <int E, int P>
-static cudaError_t rows_v2_launch(int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
+template <int E, int P, bool X>
+static cudaError_t rows_v2_launch_x(int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
   switch (stage) {
-    case ST_INIT: k_rows_v2<E, P, ST_INIT><<<grid, 128, smem, st>>>(Q); break;
-    case ST_U: k_rows_v2<E, P, ST_U><<<grid, 128, smem, st>>>(Q); break;
-    case ST_RHO: k_rows_v2<E, P, ST_RHO><<<grid, 128, smem, st>>>(Q); break;
-    case ST_EOS: k_rows_v2<E, P, ST_EOS><<<grid, 128, smem, st>>>(Q); break;
-    case ST_SRC: k_rows_v2<E, P, ST_SRC><<<grid, 128, smem, st>>>(Q); break;
-    default: k_rows_v2<E, P, ST_UREC><<<grid, 128, smem, st>>>(Q); break;
+    case ST_INIT: k_rows_v2<E, P, ST_INIT, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_U: k_rows_v2<E, P, ST_U, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_RHO: k_rows_v2<E, P, ST_RHO, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_EOS: k_rows_v2<E, P, ST_EOS, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_SRC: k_rows_v2<E, P, ST_SRC, X><<<grid, 128, smem, st>>>(Q); break;
+    default: k_rows_v2<E, P, ST_UREC, X><<<grid, 128, smem, st>>>(Q); break;
   }
   return cudaGetLastError();
 }
 
 template <int E, int P>
-static cudaError_t rows_v2_attr() {
+static cudaError_t rows_v2_launch(int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
+  const bool extra = Q.srcp_on || Q.srcu_on[0] || Q.srcu_on[1] || Q.srcu_on[2] || Q.rec_us;
+  return extra ? rows_v2_launch_x<E, P, true>(stage, grid, smem, st, Q)
+               : rows_v2_launch_x<E, P, false>(stage, grid, smem, st, Q);
+}
+
+template <int E, int P, bool X>
+static cudaError_t rows_v2_attr_x() {
   cudaError_t e = cudaSuccess;
   const int lim = 100 * 1024;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_U>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_RHO>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_EOS>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_UREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_INIT, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_U, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_RHO, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_EOS, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_SRC, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_UREC, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   return e;
+}
+
+template <int E, int P>
+static cudaError_t rows_v2_attr() {
+  cudaError_t e = rows_v2_attr_x<E, P, false>();
+  return e == cudaSuccess ? rows_v2_attr_x<E, P, true>() : e;
 }
 
 #define KW_V2_SWITCH(m, CALL)              \
