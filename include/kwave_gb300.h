@@ -67,7 +67,8 @@ enum {
   KW_T_PMLSG = 2,    /* PML, staggered */
   KW_T_OPGRAD = 3,   /* i k e^{+i k d/2} (Hermitian part), without kappa (complex) */
   KW_T_OPDIV = 4,    /* i k e^{-i k d/2} (Hermitian part), without kappa (complex) */
-  KW_T_UNSTAG = 5    /* e^{-i k d/2} (Hermitian part) (kspace_solver.py:677) (complex) */
+  KW_T_UNSTAG = 5,   /* e^{-i k d/2} (Hermitian part) (kspace_solver.py:677) (complex) */
+  KW_T_WCOORD = 6    /* p0 smoothing: squared window coordinate along the axis, FFT order */
 };
 
 /* Source slots: KW_S_P0..2 = pressure source injected into rho_x/y/z, already
@@ -115,6 +116,12 @@ int32_t kw_plan_set_sensor(kw_plan* plan, const int64_t* slot_index, int32_t n_s
  * sum_c weight[s*n_corners+c] * sample[slot[s*n_corners+c]]. */
 int32_t kw_plan_set_sensor_interp(kw_plan* plan, int32_t n_points, int32_t n_corners, const int32_t* slot,
                                   const double* weight);
+/* Smooth p0 on the device before the first step (kwave/utils/filters.py:549-615,
+ * restore_max=True): p0 <- (max|p0| / max|p0_s|) p0_s with
+ * p0_s = Re F^-1[W F[p0]], W(k) = window(min(sqrt(sum_i c_i^2), radius)) where c_i are
+ * the KW_T_WCOORD tables and window is linearly interpolated from n samples on
+ * [-radius, radius] (the rotated Blackman window of kwave/utils/signals.py:222-283). */
+int32_t kw_plan_set_p0_smoothing(kw_plan* plan, const float* window, int32_t n, double radius);
 /* Allocates device memory, uploads all inputs and resets the state to t = 0. */
 int32_t kw_plan_finalize(kw_plan* plan);
 /* Advances min(nsteps, Nt - t) steps of Simulation.step (kspace_solver.py:691-747)

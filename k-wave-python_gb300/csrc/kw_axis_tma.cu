@@ -72,35 +72,63 @@ struct TabX {
   const float2* unstag;
 };
 
-// Operator of job J at x-frequency index x of column g.  fcol is the job's
-// 1-D factor when it acts along y or z (constant over the column).  With
-// full == false only the 1-D factor of a gradient/divergence is returned
-// (kappa and 1/N already folded into the spectrum).
+// Operator OP of job J at x-frequency index x of column g (OP known at compile
+// time, so each job's element loop carries only its own arithmetic).  fcol is
+// the job's 1-D factor when it acts along y or z.  With full == false only the
+// 1-D factor of a gradient/divergence is returned (kappa and 1/N already folded
+// into the spectrum).
+template <int OP>
 __device__ __forceinline__ float2 op_value(const AxisParams& A, const AxisJob& J, int x, const ColK& g,
                                            const float* k0s, const TabX& f0s, float2 fcol, bool full) {
   float2 op;
-  switch (J.op) {
-    case OP_GRAD:
-    case OP_DIV: {
-      const float2 f = (J.axis == 0) ? (J.op == OP_GRAD ? f0s.grad[x] : f0s.div[x]) : fcol;
-      if (!full) return f;
-      const float kp = kappa_of(A, kmag_of(k0s, A.ndim, x, g)) * A.scale;
-      return make_float2(f.x * kp, f.y * kp);
-    }
-    case OP_NAB1:
-    case OP_NAB2: {
-      const float km = kmag_of(k0s, A.ndim, x, g);
-      op = make_float2(km == 0.f ? 0.f : powf(km, J.op == OP_NAB1 ? A.pow1 : A.pow2), 0.f);
-      break;
-    }
-    case OP_SKAPPA:
-      op = make_float2(A.use_kspace ? cosf(A.kcoef * kmag_of(k0s, A.ndim, x, g)) : 1.f, 0.f);
-      break;
-    default:
-      op = (J.axis == 0) ? f0s.unstag[x] : fcol;
-      break;
+  if constexpr (OP == OP_GRAD || OP == OP_DIV) {
+    const float2 f = (J.axis == 0) ? (OP == OP_GRAD ? f0s.grad[x] : f0s.div[x]) : fcol;
+    if (!full) return f;
+    const float kp = kappa_of(A, kmag_of(k0s, A.ndim, x, g)) * A.scale;
+    return make_float2(f.x * kp, f.y * kp);
+  } else if constexpr (OP == OP_NAB1 || OP == OP_NAB2) {
+    const float km = kmag_of(k0s, A.ndim, x, g);
+    op = make_float2(km == 0.f ? 0.f : powf(km, OP == OP_NAB1 ? A.pow1 : A.pow2), 0.f);
+  } else if constexpr (OP == OP_SKAPPA) {
+    op = make_float2(A.use_kspace ? cosf(A.kcoef * kmag_of(k0s, A.ndim, x, g)) : 1.f, 0.f);
+  } else if constexpr (OP == OP_WIN) {
+    float r2 = A.wc[0][x] + A.wc[1][g.a1];
+    if (A.ndim == 3) r2 += A.wc[2][g.a2];
+    op = make_float2(window_at(A.wtab, A.wlen, A.wrad, r2), 0.f);
+  } else {
+    op = (J.axis == 0) ? f0s.unstag[x] : fcol;
   }
   return make_float2(op.x * A.scale, op.y * A.scale);
+}
+
+// y[r] = conj(op * v[r]) over the thread's frequencies, for operator OP.
+template <int OP, int E, int P>
+__device__ __forceinline__ void apply_op(const AxisParams& A, const AxisJob& J, int t, const ColK& g, const float* k0s,
+                                         const TabX& f0s, float2 fcol, bool full, bool on, const float2 (&v)[E],
+                                         float2 (&y)[E]) {
+#pragma unroll
+  for (int m = 0; m < E / P; ++m)
+#pragma unroll
+    for (int k2 = 0; k2 < P; ++k2) {
+      const int r = m * P + k2;
+      const float2 op = op_value<OP>(A, J, t + P * m + E * k2, g, k0s, f0s, fcol, full);
+      y[r] = on ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
+    }
+}
+
+template <int E, int P>
+__device__ __forceinline__ void apply_job(const AxisParams& A, const AxisJob& J, int t, const ColK& g, const float* k0s,
+                                          const TabX& f0s, float2 fcol, bool full, bool on, const float2 (&v)[E],
+                                          float2 (&y)[E]) {
+  switch (J.op) {
+    case OP_GRAD: apply_op<OP_GRAD, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+    case OP_DIV: apply_op<OP_DIV, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+    case OP_NAB1: apply_op<OP_NAB1, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+    case OP_NAB2: apply_op<OP_NAB2, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+    case OP_SKAPPA: apply_op<OP_SKAPPA, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+    case OP_WIN: apply_op<OP_WIN, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+    default: apply_op<OP_UNSTAG, E, P>(A, J, t, g, k0s, f0s, fcol, full, on, v, y); break;
+  }
 }
 
 // The column-constant 1-D factor of job J (axis 1 or 2).
@@ -118,7 +146,9 @@ __device__ __forceinline__ float2 col_factor(const AxisParams& A, const AxisJob&
 }  // namespace
 
 // T columns per tile, CT = T * P consumer threads plus one producer warp.
-template <int E, int P, int NST, int MINB, int T>
+// OPS selects the operator pass (A.mode == 2) or the plain transforms, so that
+// each instantiation carries only one of the two code paths.
+template <int E, int P, int NST, int MINB, int T, bool OPS>
 __global__ void __launch_bounds__(T * P + 32, MINB)
     k_axis_tma(const __grid_constant__ AxisParams A, const __grid_constant__ TmaMaps maps, const TmaWork W) {
   constexpr int N = E * P, RS = N + E + 1, CT = T * P;
@@ -158,7 +188,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
   const float* k0s = kTablesInSmem ? k0t : A.k[0];
   const TabX f0s{kTablesInSmem ? f0t : A.fg[0], kTablesInSmem ? f0t + N : A.fd[0], kTablesInSmem ? f0t + 2 * N : A.us[0]};
 
-  const bool plain = A.mode < 2;
+  constexpr bool plain = !OPS;
   if (warp == CT / 32) {
     // ---------------- producer ----------------
     if (lane == 0) {
@@ -170,7 +200,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
         const int outer = rest % W.nouter;
         const int b = rest / W.nouter;
         for (int q = 0; q < W.nitems; ++q, ++it) {
-          const int buf = plain ? A.plain[b] : W.inp[q];
+          const int buf = OPS ? W.inp[q] : A.plain[b];
           const uint32_t s = it % NST, k = it / NST;
           if (k > 0 && !kwtma::mbar_wait(&empty[s], (k - 1) & 1, kWaitLimitNs)) {
             atomicExch(&g_kw_device_error, 1);
@@ -202,7 +232,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
       const long long base = (long long)outer * A.os + c0 + cc;
       const long long xs = A.xs;
       ColK g;
-      if (!plain) g = col_geometry(A, act ? c0 + cc : c0);
+      if constexpr (OPS) g = col_geometry(A, act ? c0 + cc : c0);
       for (int q = 0; q < W.nitems; ++q, ++it) {
         const uint32_t s = it % NST, k = it / NST;
         const bool got = kwtma::mbar_wait(&full[s], k & 1, kWaitLimitNs);
@@ -213,7 +243,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
         }
         const float2* st = stages + (size_t)s * N * T;
         float2 v[E];
-        if (plain && A.mode == 1) {
+        if (!OPS && A.mode == 1) {
 #pragma unroll
           for (int m = 0; m < E / P; ++m)
 #pragma unroll
@@ -225,7 +255,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
         __syncwarp();
         if (lane == 0) kwtma::mbar_arrive(&empty[s]);
 
-        if (plain) {
+        if constexpr (!OPS) {
           float2* buf = A.bufs[A.plain[b]];
           if (A.mode == 0) {
             kwreg::Reg<E, P>::fwd(v, t, ex + cc * RS, 1, tw, sync);
@@ -242,8 +272,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
               for (int j = 0; j < E; ++j) buf[base + (t + P * j) * xs] = cconj(v[j]);
             }
           }
-          continue;
-        }
+        } else {
         // operator mode: forward FFT of this input, then every job reading it
         kwreg::Reg<E, P>::fwd(v, t, ex + cc * RS, 1, tw, sync);
         const int in = W.inp[q];
@@ -259,14 +288,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
           // one job: multiply in place
           const AxisJob J = A.jobs[jlast];
           const float2 fcol = col_factor(A, J, g);
-#pragma unroll
-          for (int m = 0; m < E / P; ++m)
-#pragma unroll
-            for (int k2 = 0; k2 < P; ++k2) {
-              const int r = m * P + k2;
-              const float2 op = op_value(A, J, t + P * m + E * k2, g, k0s, f0s, fcol, true);
-              v[r] = (act && g.valid) ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
-            }
+          apply_job<E, P>(A, J, t, g, k0s, f0s, fcol, true, act && g.valid, v, v);
           kwreg::Reg<E, P>::rev(v, t, ex + cc * RS, 1, tw, sync);
           if (act) {
             float2* out = A.bufs[J.out];
@@ -290,20 +312,14 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
           if (J.in != in) continue;
           const float2 fcol = col_factor(A, J, g);
           float2 y[E];
-#pragma unroll
-          for (int m = 0; m < E / P; ++m)
-#pragma unroll
-            for (int k2 = 0; k2 < P; ++k2) {
-              const int r = m * P + k2;
-              const float2 op = op_value(A, J, t + P * m + E * k2, g, k0s, f0s, fcol, !all_kappa);
-              y[r] = (act && g.valid) ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
-            }
+          apply_job<E, P>(A, J, t, g, k0s, f0s, fcol, !all_kappa, act && g.valid, v, y);
           kwreg::Reg<E, P>::rev(y, t, ex + cc * RS, 1, tw, sync);
           if (act) {
             float2* out = A.bufs[J.out];
 #pragma unroll
             for (int j = 0; j < E; ++j) out[base + (t + P * j) * xs] = cconj(y[j]);
           }
+        }
         }
       }
     }
@@ -409,8 +425,11 @@ cudaError_t kw_tma_attr(int n, int axis) {
   int E, P;
   if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
   const int smem = (int)tma_smem(n, E, P, axis);
-#define KW_T(E_, P_, S_, B_, T_) \
-  cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+#define KW_T(E_, P_, S_, B_, T_)                                                                                 \
+  (cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != \
+           cudaSuccess                                                                                           \
+       ? cudaGetLastError()                                                                                      \
+       : cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
   KW_TMA_SWITCH(n, KW_T)
 #undef KW_T
 }
@@ -441,8 +460,10 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
   const int per_sm = narrow(n, axis) ? 3 : ((n <= 256 && axis_variant()) ? 2 : 1);
   const int grid = W.nunits < nsm * per_sm ? W.nunits : nsm * per_sm;
   const size_t smem = tma_smem(n, E, P, axis);
-#define KW_T(E_, P_, S_, B_, T_) \
-  (k_axis_tma<E_, P_, S_, B_, T_><<<grid, T_ * P_ + 32, smem, st>>>(A, tp->maps[axis], W), cudaGetLastError())
+#define KW_T(E_, P_, S_, B_, T_)                                                                          \
+  ((A.mode == 2 ? k_axis_tma<E_, P_, S_, B_, T_, true><<<grid, T_ * P_ + 32, smem, st>>>(A, tp->maps[axis], W) \
+                : k_axis_tma<E_, P_, S_, B_, T_, false><<<grid, T_ * P_ + 32, smem, st>>>(A, tp->maps[axis], W)), \
+   cudaGetLastError())
   KW_TMA_SWITCH(n, KW_T)
 #undef KW_T
 }

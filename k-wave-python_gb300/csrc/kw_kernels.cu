@@ -52,6 +52,12 @@ __device__ __forceinline__ float2 axis_op(const AxisParams& P, const AxisJob& J,
     case OP_SKAPPA:
       v = make_float2(P.use_kspace ? cosf(P.kcoef * kmag) : 1.f, 0.f);
       break;
+    case OP_WIN: {
+      float r2 = P.wc[0][x] + P.wc[1][a1];
+      if (P.ndim == 3) r2 += P.wc[2][a2];
+      v = make_float2(window_at(P.wtab, P.wlen, P.wrad, r2), 0.f);
+      break;
+    }
     default:
       v = P.us[J.axis][ai];
       break;
@@ -280,7 +286,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
       const int row = i / L, z = i - row * L;
       if (row >= nr) continue;
       const long long g = (long long)(r0 + row) * L + z;
-      const float pv = P.p0[g];
+      const float pv = P.p0_scale ? __fmul_rn(P.p0[g], *P.p0_scale) : P.p0[g];
       const float c = fld(P.c0, P.c0_s, g);
       const float c2 = __fmul_rn(c, c);
       const float r = __fdiv_rn(pv, __fmul_rn(c2, (float)D));
@@ -445,6 +451,26 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
     return;
   }
 
+  if (P.stage == ST_P0FFT) {
+    // spectrum of p0 for the smoothing window
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = i / L, z = i - row * L;
+      rb[0][i] = (row < nr) ? P.p0w[(long long)(r0 + row) * L + z] : 0.f;
+    }
+    __syncthreads();
+    rf.r2c(P, rb[0], P.S[B_P], r0, nr);
+    return;
+  }
+
+  if (P.stage == ST_P0BACK) {
+    rf.c2r(P, P.S[B_P], rb[0], r0, nr);
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = i / L, z = i - row * L;
+      if (row < nr) P.p0w[(long long)(r0 + row) * L + z] = rb[0][i];
+    }
+    return;
+  }
+
   if (P.stage == ST_UREC) {
     for (int a = 0; a < D; ++a) {
       if (!(P.rec_us & (1 << a))) continue;
@@ -531,6 +557,12 @@ __device__ __forceinline__ float2 col_op(const AxisParams& A, const AxisJob& J, 
     case OP_SKAPPA:
       v = make_float2(A.use_kspace ? cosf(A.kcoef * kmag) : 1.f, 0.f);
       break;
+    case OP_WIN: {
+      float r2 = A.wc[0][x] + A.wc[1][g.a1];
+      if (A.ndim == 3) r2 += A.wc[2][g.a2];
+      v = make_float2(window_at(A.wtab, A.wlen, A.wrad, r2), 0.f);
+      break;
+    }
     default:
       v = A.us[J.axis][ai];
       break;
@@ -646,6 +678,24 @@ cudaError_t kw_axis_reg_launch(int n, dim3 grid, size_t smem, cudaStream_t st, c
 #undef KW_A
 }
 
+
+// ---------------------------------------------------------------------------
+// p0 smoothing helpers (kwave/utils/filters.py:613-614, restore_max)
+// ---------------------------------------------------------------------------
+__global__ void k_absmax(const float* __restrict__ x, long long n, unsigned int* out) {
+  float m = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const float den = __uint_as_float(*b);
+    *out = den > 0.f ? __uint_as_float(*a) / den : 1.f;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // recorder post-processing (kspace_solver.py:335-359, :824-837)

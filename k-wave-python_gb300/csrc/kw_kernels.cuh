@@ -27,8 +27,8 @@ enum KwBuf { B_S0 = 0, B_P = 3, B_SRCP = 4, B_SRCU0 = 5, B_US0 = 8 };
 #define KW_MAX_JOBS 8
 #define KW_NREAL 5
 
-enum KwStage { ST_INIT = 0, ST_U = 1, ST_RHO = 2, ST_EOS = 3, ST_SRC = 4, ST_UREC = 5 };
-enum KwOp { OP_GRAD = 0, OP_DIV = 1, OP_NAB1 = 2, OP_NAB2 = 3, OP_SKAPPA = 4, OP_UNSTAG = 5 };
+enum KwStage { ST_INIT = 0, ST_U = 1, ST_RHO = 2, ST_EOS = 3, ST_SRC = 4, ST_UREC = 5, ST_P0FFT = 6, ST_P0BACK = 7 };
+enum KwOp { OP_GRAD = 0, OP_DIV = 1, OP_NAB1 = 2, OP_NAB2 = 3, OP_SKAPPA = 4, OP_UNSTAG = 5, OP_WIN = 6 };
 enum KwSrcMode { SRC_DIRICHLET = 0, SRC_ADDITIVE = 1, SRC_ADDITIVE_NC = 2 };
 
 struct KwSrcDev {
@@ -58,6 +58,8 @@ struct RowsParams {
   float* p;
   float* rho_sum;
   const float* p0;
+  float* p0w;             // ST_P0FFT reads it, ST_P0BACK writes the smoothed p0 into it
+  const float* p0_scale;  // restore-max factor applied to p0 in ST_INIT (nullptr: 1)
   const float* c0;
   float c0_s;
   const float* rho0;
@@ -106,6 +108,10 @@ struct AxisParams {
   const float2* fg[3];
   const float2* fd[3];
   const float2* us[3];
+  const float* wc[3];   // p0 smoothing: squared window coordinates (FFT order)
+  const float* wtab;    // window samples on [-wrad, wrad]
+  int wlen;
+  float wrad;
   float kcoef;    // c_ref * dt / 2
   int use_kspace;
   float pow1, pow2;
@@ -157,6 +163,21 @@ bool kw_tma_supported(int n);
 bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long long xs, int nouter, long long os, int P);
 cudaError_t kw_tma_attr(int n, int axis);
 cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A);
+// Window value of the p0 smoothing at squared radius r2 (linear interpolation).
+__device__ __forceinline__ float window_at(const float* tab, int n, float rad, float r2) {
+  float r = sqrtf(r2);
+  if (r > rad) r = rad;
+  const float pos = (r + rad) / (2.f * rad) * (float)(n - 1);
+  int i0 = (int)pos;
+  if (i0 > n - 2) i0 = n - 2;
+  const float f = pos - (float)i0;
+  return tab[i0] + f * (tab[i0 + 1] - tab[i0]);
+}
+
+// max |x| over n values, as float bits folded into *out with atomicMax (n > 0)
+__global__ void k_absmax(const float* __restrict__ x, long long n, unsigned int* out);
+// out = a / b for two float bit patterns (restore-max factor)
+__global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out);
 // Returns and clears the device error word (nonzero: a bounded device wait timed out).
 int kw_device_error_take();
 __global__ void k_rows(const __grid_constant__ RowsParams P);

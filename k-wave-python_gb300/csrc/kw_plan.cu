@@ -62,7 +62,7 @@ struct kw_plan {
   // staged host inputs
   std::vector<float> hfield[9];
   float hscalar[9] = {0};
-  std::vector<float> htab[6][3];
+  std::vector<float> htab[7][3];
   HostSrc hsrc[6];
   std::vector<long long> sens_idx;
   int record_mask = 0;
@@ -77,7 +77,7 @@ struct kw_plan {
   float* d_rhosum = nullptr;
   float2* d_S[KW_NBUF] = {nullptr};
   float* d_field[9] = {nullptr};
-  float* d_tab[6][3] = {{nullptr}};
+  float* d_tab[7][3] = {{nullptr}};
   float2* d_tw_axis[3] = {nullptr, nullptr, nullptr};
   KwFftLen flen_axis[3];
   float2* d_tw_row = nullptr;
@@ -103,6 +103,14 @@ struct kw_plan {
   bool tma_axis[3] = {false, false, false};
   int nsm = 0;
   int rows_regP = 0, rows_regE = 0, rows_R = 0, rows_RS = 0;
+  // p0 smoothing on the device
+  bool smooth = false, p0s_ready = false;
+  std::vector<float> hwin;
+  double wrad = 0.0;
+  float* d_win = nullptr;
+  float* d_p0s = nullptr;
+  float* d_p0scale = nullptr;
+  unsigned int* d_maxes = nullptr;
   // per-step flags passed to the row stages
   int srcp_on = 0, srcu_on[3] = {0, 0, 0}, rec_us = 0, init_r2c = 0;
   // launch accounting / timing
@@ -264,11 +272,21 @@ int32_t kw_plan_set_field(kw_plan* p, int32_t field, const float* host, int64_t 
 int32_t kw_plan_set_table(kw_plan* p, int32_t table, int32_t axis, const float* host, int64_t n_floats) {
   if (!p || !host) return fail(KW_ERR_INVALID, "null argument");
   if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
-  if (table < 0 || table > KW_T_UNSTAG || axis < 0 || axis >= p->D) return fail(KW_ERR_INVALID, "bad table %d / axis %d", table, axis);
-  const bool cplx = table >= KW_T_OPGRAD;
+  if (table < 0 || table > KW_T_WCOORD || axis < 0 || axis >= p->D) return fail(KW_ERR_INVALID, "bad table %d / axis %d", table, axis);
+  const bool cplx = table >= KW_T_OPGRAD && table <= KW_T_UNSTAG;
   const long long want = (long long)p->N[axis] * (cplx ? 2 : 1);
   if (n_floats != want) return fail(KW_ERR_INVALID, "table %d axis %d: %lld floats, expected %lld", table, axis, (long long)n_floats, want);
   p->htab[table][axis].assign(host, host + n_floats);
+  return KW_OK;
+}
+
+int32_t kw_plan_set_p0_smoothing(kw_plan* p, const float* window, int32_t n, double radius) {
+  if (!p || !window) return fail(KW_ERR_INVALID, "null argument");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (n < 2 || !(radius > 0.0)) return fail(KW_ERR_INVALID, "smoothing window needs n >= 2 and radius > 0");
+  p->hwin.assign(window, window + n);
+  p->wrad = radius;
+  p->smooth = true;
   return KW_OK;
 }
 
@@ -391,8 +409,18 @@ int32_t kw_plan_finalize(kw_plan* p) {
   for (int f = 0; f < 9; ++f)
     if (!p->hfield[f].empty())
       if ((rc = upload(p, &p->d_field[f], p->hfield[f].data(), p->hfield[f].size()))) return rc;
+  // p0 smoothing
+  if (p->smooth) {
+    if (!p->d_field[KW_F_P0]) return fail(KW_ERR_INVALID, "p0 smoothing requested without a p0 grid");
+    for (int a = 0; a < D; ++a)
+      if (p->htab[KW_T_WCOORD][a].empty()) return fail(KW_ERR_INVALID, "smoothing coordinates for axis %d not set", a);
+    if ((rc = upload(p, &p->d_win, p->hwin.data(), p->hwin.size()))) return rc;
+    if ((rc = dalloc(p, &p->d_p0s, p->ntot))) return rc;
+    if ((rc = dalloc(p, &p->d_p0scale, 1))) return rc;
+    if ((rc = dalloc(p, &p->d_maxes, 2))) return rc;
+  }
   // tables
-  for (int tb = 0; tb < 6; ++tb)
+  for (int tb = 0; tb < 7; ++tb)
     for (int a = 0; a < D; ++a)
       if (!p->htab[tb][a].empty())
         if ((rc = upload(p, &p->d_tab[tb][a], p->htab[tb][a].data(), p->htab[tb][a].size()))) return rc;
@@ -545,7 +573,9 @@ static void fill_rows(const kw_plan* p, RowsParams& P) {
   }
   P.p = p->d_p;
   P.rho_sum = p->d_rhosum;
-  P.p0 = p->d_field[KW_F_P0];
+  P.p0 = p->smooth ? p->d_p0s : p->d_field[KW_F_P0];
+  P.p0w = p->d_p0s;
+  P.p0_scale = p->smooth ? p->d_p0scale : nullptr;
   P.c0 = p->d_field[KW_F_C0];
   P.c0_s = p->hscalar[KW_F_C0];
   P.rho0 = p->d_field[KW_F_RHO0];
@@ -580,7 +610,8 @@ static int need_buf(const kw_plan* p, int b, const char* what) {
 static int check_rows(const kw_plan* p, int stage, int init) {
   int rc;
   const int D = p->D;
-  if (stage == ST_INIT && (rc = need_buf(p, B_P, "p"))) return rc;
+  if ((stage == ST_INIT || stage == ST_P0FFT || stage == ST_P0BACK) && (rc = need_buf(p, B_P, "p"))) return rc;
+  if ((stage == ST_P0FFT || stage == ST_P0BACK) && !p->d_p0s) return fail(KW_ERR_STATE, "internal: no smoothing buffer");
   if (stage == ST_U || stage == ST_RHO)
     for (int a = 0; a < D; ++a)
       if ((rc = need_buf(p, a, "work"))) return rc;
@@ -697,6 +728,7 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
     const int tb = jobs[i].op == OP_GRAD ? KW_T_OPGRAD : jobs[i].op == OP_DIV ? KW_T_OPDIV
                  : jobs[i].op == OP_UNSTAG ? KW_T_UNSTAG : -1;
     if (tb >= 0 && !p->d_tab[tb][jobs[i].axis]) return fail(KW_ERR_STATE, "internal: operator table %d missing", tb);
+    if (jobs[i].op == OP_WIN && (!p->d_win || !p->d_tab[KW_T_WCOORD][0])) return fail(KW_ERR_STATE, "internal: no window");
   }
   AxisParams A;
   fill_axis_geom(p, 0, A);
@@ -709,6 +741,10 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
     A.fd[a] = reinterpret_cast<const float2*>(p->d_tab[KW_T_OPDIV][a]);
     A.us[a] = reinterpret_cast<const float2*>(p->d_tab[KW_T_UNSTAG][a]);
   }
+  for (int a = 0; a < p->D; ++a) A.wc[a] = p->d_tab[KW_T_WCOORD][a];
+  A.wtab = p->d_win;
+  A.wlen = (int)p->hwin.size();
+  A.wrad = (float)p->wrad;
   A.kcoef = (float)(p->g.c_ref * p->g.dt / 2.0);
   A.use_kspace = p->g.use_kspace;
   A.pow1 = (float)(p->g.alpha_power - 2.0);
@@ -782,6 +818,26 @@ static int enqueue_step(kw_plan* p, int t, bool last, cudaStream_t st) {
     p->srcp_on = 0;
     p->srcu_on[0] = p->srcu_on[1] = p->srcu_on[2] = 0;
     p->rec_us = 0;
+    if (p->smooth && !p->p0s_ready) {
+      // p0 smoothing with restore_max (kwave/utils/filters.py:549-615), once per plan
+      const long long n = p->ntot;
+      const int grid = (int)std::min<long long>((n + 255) / 256, 4 * (long long)p->nsm);
+      CK(cudaMemsetAsync(p->d_maxes, 0, 2 * sizeof(unsigned int), st));
+      k_absmax<<<grid, 256, 0, st>>>(p->d_field[KW_F_P0], n, p->d_maxes);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(p->d_p0s, p->d_field[KW_F_P0], n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+      if ((rc = launch_rows(p, ST_P0FFT, 0, t, 0, st))) return rc;
+      if (three && (rc = launch_axis_plain(p, 1, 0, PB, 1, st))) return rc;
+      jobs[0] = AxisJob{B_P, B_P, OP_WIN, 0};
+      if ((rc = launch_axis_ops(p, jobs, 1, st))) return rc;
+      if (three && (rc = launch_axis_plain(p, 1, 1, PB, 1, st))) return rc;
+      if ((rc = launch_rows(p, ST_P0BACK, 0, t, 0, st))) return rc;
+      k_absmax<<<grid, 256, 0, st>>>(p->d_p0s, n, p->d_maxes + 1);
+      CK(cudaGetLastError());
+      k_ratio<<<1, 32, 0, st>>>(p->d_maxes, p->d_maxes + 1, p->d_p0scale);
+      CK(cudaGetLastError());
+      p->p0s_ready = true;
+    }
     if ((rc = launch_rows(p, ST_INIT, 0, t, 1, st))) return rc;
     if (three && (rc = launch_axis_plain(p, 1, 0, PB, 1, st))) return rc;
     for (int a = 0; a < D; ++a) jobs[a] = AxisJob{B_P, a, OP_GRAD, a};

@@ -190,6 +190,10 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
       float2 pv = make_float2(0.f, 0.f);
       if (c.ok) {
         pv = ld2(Q.p0, i);
+        if (Q.p0_scale) {
+          const float sc = *Q.p0_scale;
+          pv = make_float2(__fmul_rn(pv.x, sc), __fmul_rn(pv.y, sc));
+        }
         const float2 cc = fld2(Q.c0, Q.c0_s, i);
         const float2 r = make_float2(__fdiv_rn(pv.x, __fmul_rn(__fmul_rn(cc.x, cc.x), (float)D)),
                                      __fdiv_rn(pv.y, __fmul_rn(__fmul_rn(cc.y, cc.y), (float)D)));
@@ -365,6 +369,23 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     return;
   }
 
+  if constexpr (STAGE == ST_P0FFT) {
+    // spectrum of p0 for the smoothing window
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = c.ok ? ld2(Q.p0w, c.rbase + t + P * j) : make_float2(0.f, 0.f);
+    c.r2c(v, Q.S[B_P]);
+    return;
+  }
+
+  if constexpr (STAGE == ST_P0BACK) {
+    c.c2r(Q.S[B_P], v);
+    if (c.ok) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) st2(Q.p0w, c.rbase + t + P * j, v[j]);
+    }
+    return;
+  }
+
   if constexpr (STAGE == ST_UREC) {
     record_unstaggered(c, Q, v);
     return;
@@ -414,6 +435,8 @@ static cudaError_t rows_v2_launch_x(int stage, dim3 grid, size_t smem, cudaStrea
     case ST_RHO: k_rows_v2<E, P, ST_RHO, X><<<grid, 128, smem, st>>>(Q); break;
     case ST_EOS: k_rows_v2<E, P, ST_EOS, X><<<grid, 128, smem, st>>>(Q); break;
     case ST_SRC: k_rows_v2<E, P, ST_SRC, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_P0FFT: k_rows_v2<E, P, ST_P0FFT, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_P0BACK: k_rows_v2<E, P, ST_P0BACK, X><<<grid, 128, smem, st>>>(Q); break;
     default: k_rows_v2<E, P, ST_UREC, X><<<grid, 128, smem, st>>>(Q); break;
   }
   return cudaGetLastError();
@@ -436,6 +459,8 @@ static cudaError_t rows_v2_attr_x() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_EOS, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_SRC, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_UREC, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_P0FFT, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_P0BACK, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
   return e;
 }
 

@@ -20,7 +20,7 @@ KW_OK, KW_ERR_INVALID, KW_ERR_CUDA, KW_ERR_OOM, KW_ERR_UNSUPPORTED, KW_ERR_STATE
 # field ids
 KW_F_C0, KW_F_RHO0, KW_F_DTRSG0, KW_F_DTRSG1, KW_F_DTRSG2, KW_F_BONA, KW_F_TAU, KW_F_ETA, KW_F_P0 = range(9)
 # tables
-KW_T_K, KW_T_PML, KW_T_PMLSG, KW_T_OPGRAD, KW_T_OPDIV, KW_T_UNSTAG = range(6)
+KW_T_K, KW_T_PML, KW_T_PMLSG, KW_T_OPGRAD, KW_T_OPDIV, KW_T_UNSTAG, KW_T_WCOORD = range(7)
 # source modes
 KW_SRC_DIRICHLET, KW_SRC_ADDITIVE, KW_SRC_ADDITIVE_NC = range(3)
 SRC_MODES = {"dirichlet": KW_SRC_DIRICHLET, "additive": KW_SRC_ADDITIVE, "additive-no-correction": KW_SRC_ADDITIVE_NC}
@@ -72,6 +72,7 @@ _PROTOS = {
     "kw_plan_set_source": (C.c_int32, [_P, C.c_int32, C.c_int32, _P, C.c_int32, _P, C.c_int32, C.c_int32]),
     "kw_plan_set_sensor": (C.c_int32, [_P, _P, C.c_int32, C.c_int32]),
     "kw_plan_set_sensor_interp": (C.c_int32, [_P, C.c_int32, C.c_int32, _P, _P]),
+    "kw_plan_set_p0_smoothing": (C.c_int32, [_P, _P, C.c_int32, C.c_double]),
     "kw_plan_finalize": (C.c_int32, [_P]),
     "kw_plan_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_plan_sync": (C.c_int32, [_P, _P]),

@@ -159,11 +159,26 @@ def blackman_rotated(shape):
     return np.abs(win[tuple(slice(0, int(m)) for m in N)])
 
 
-def smooth_restore_max(a):
-    """kwave/utils/filters.py:549-615 with restore_max=True (FP64 host FFT)."""
-    win = blackman_rotated(a.shape)
-    a_sm = np.real(np.fft.ifftn(np.fft.fftn(a) * np.fft.ifftshift(win)))
-    return (np.abs(a).max() / np.abs(a_sm).max()) * a_sm
+def smoothing_tables(shape):
+    """1-D description of the rotated Blackman window of kwave/utils/signals.py
+    :222-283 as used by kwave/utils/filters.py:586-601 (even sizes enlarged by
+    one, then trimmed; applied after ifftshift): the window samples on
+    [-radius, radius] and, per axis, the squared coordinate of every FFT index.
+    The device evaluates window(min(sqrt(sum c^2), radius)) per cell."""
+    N = np.array(shape, dtype=int)
+    sym = (N % 2).astype(bool)
+    Ne = N + (1 - sym.astype(int))
+    L = int(Ne.max())
+    n = np.arange(L)
+    a = 0.16
+    win_lin = (1 - a) / 2 - 0.5 * np.cos(2 * np.pi * n / (L - 1)) + (a / 2) * np.cos(4 * np.pi * n / (L - 1))
+    radius = (L - 1) / 2
+    coords = []
+    for m, ne in zip(N, Ne):
+        xx = np.linspace(-radius, radius, int(ne))[: int(m)]
+        idx = (np.arange(m) + m // 2) % m  # ifftshift
+        coords.append((xx[idx] ** 2).astype(np.float32))
+    return np.abs(win_lin).astype(np.float32), float(radius), coords
 
 
 def stagger(arr, axis):
@@ -216,6 +231,7 @@ class Setup:
     record_start: int = 0
     pml_sizes: tuple = ()
     has_p0: bool = False
+    smooth: tuple = None                              # (window, radius, coords) when p0 is smoothed
 
 
 def parse_record(record, ndim):
@@ -407,8 +423,8 @@ def build_setup(prob) -> Setup:
         if isinstance(p0, float):
             p0 = np.full(shape, p0)
         if prob.get("smooth_p0", True) and ndim >= 2:
-            # the reference casts p0 to the solver dtype before smoothing
-            p0 = smooth_restore_max(np.asarray(p0, dtype=np.float32).astype(np.float64))
+            # smoothed on the device before the first step (kwave/utils/filters.py:549-615)
+            S.smooth = smoothing_tables(shape)
         S.fields["p0"] = np.ascontiguousarray(p0, dtype=np.float32)
         S.has_p0 = True
     return S

@@ -107,6 +107,15 @@ class DevicePlan:
             w = np.ascontiguousarray(S.interp_w, dtype=np.float64)
             nbytes += sl.nbytes + w.nbytes
             K.check(lib.kw_plan_set_sensor_interp(h, sl.shape[0], sl.shape[1], K.ptr(sl), K.ptr(w)))
+        if S.smooth is not None:
+            win, radius, coords = S.smooth
+            for axis, cw in enumerate(coords):
+                a = np.ascontiguousarray(cw, dtype=np.float32)
+                nbytes += a.nbytes
+                K.check(lib.kw_plan_set_table(h, K.KW_T_WCOORD, axis, K.ptr(a), a.size))
+            w = np.ascontiguousarray(win, dtype=np.float32)
+            nbytes += w.nbytes
+            K.check(lib.kw_plan_set_p0_smoothing(h, K.ptr(w), w.size, C.c_double(radius)))
         self.h2d_bytes = nbytes
         STATS["h2d_bytes"] = nbytes
 

@@ -32,8 +32,27 @@ def test_setup_matches_oracle(name):
         np.testing.assert_allclose(np.broadcast_to(S.fields["tau"], o.tau.shape), o.tau, rtol=1e-6)
     if o.eta is not None:
         np.testing.assert_allclose(np.broadcast_to(S.fields["eta"], o.eta.shape), o.eta, rtol=1e-6)
-    if o._p0_initial is not None:
+    if o._p0_initial is not None and S.smooth is None:
         np.testing.assert_allclose(S.fields["p0"], o._p0_initial, rtol=0, atol=2e-6 * np.abs(o._p0_initial).max())
+
+
+@pytest.mark.parametrize("shape", [(128, 128), (48, 40), (45, 27), (32, 24, 20), (15, 16, 17)])
+def test_smoothing_tables_reproduce_reference_window(shape):
+    """The device window (linear interpolation of the 1-D samples at the
+    per-axis squared coordinates) equals ifftshift(rotated Blackman window)."""
+    from kwave_gb300.precompute import smoothing_tables
+    from oracle.kspace_oracle import blackman_window_rotated
+
+    win, radius, coords = smoothing_tables(shape)
+    r2 = sum(np.asarray(c, np.float64).reshape([-1 if i == a else 1 for i in range(len(shape))])
+             for a, c in enumerate(coords))
+    r = np.minimum(np.sqrt(r2), radius)
+    pos = (r + radius) / (2 * radius) * (len(win) - 1)
+    i0 = np.minimum(pos.astype(int), len(win) - 2)
+    f = pos - i0
+    w = win[i0] + f * (win[i0 + 1] - win[i0])
+    ref = np.fft.ifftshift(np.abs(blackman_window_rotated(shape)))
+    np.testing.assert_allclose(w, ref, rtol=0, atol=2e-6)
 
 
 @pytest.mark.parametrize("name", ["src2d_dirichlet", "src2d_velocity", "vel2d_dirichlet", "src2d_additive"])
