@@ -6,9 +6,16 @@ Entry points:
   * ``backend.run_gb300_backend`` — the bridge itself (the counterpart of
     ``kwave.solvers.native.run_python_backend``);
   * ``solver.Simulation`` — the counterpart of
-    ``kwave.solvers.kspace_solver.Simulation``.
+    ``kwave.solvers.kspace_solver.Simulation``;
+  * ``unified.kspaceFirstOrder`` — the unified entry point
+    (``kwave.kspaceFirstOrder.kspaceFirstOrder``) for ``backend="gb300"``;
+  * ``backend.kspaceFirstOrder2D`` / ``3D`` — the legacy signatures;
+  * ``reconstruction.TimeReversal`` — time-reversal reconstruction.
 """
 __version__ = "0.1.0"
 
-from .backend import BACKEND, execution_options, install, run_gb300_backend, uninstall  # noqa: F401
+from .backend import (BACKEND, execution_options, install, kspaceFirstOrder2D, kspaceFirstOrder3D,  # noqa: F401
+                      run_gb300_backend, uninstall)
+from .reconstruction import TimeReversal  # noqa: F401
 from .solver import Simulation, run_problem  # noqa: F401
+from .unified import get_optimal_pml_size, kspaceFirstOrder, reshape_to_grid  # noqa: F401

@@ -66,6 +66,27 @@ def run_gb300_backend(kgrid, medium, source, sensor, simulation_options, executi
         sim.close()
 
 
+def _legacy(ndim_expected, name):
+    def run(kgrid, source, sensor, medium, simulation_options, execution_options=None):
+        dim = len(grid_of(kgrid)[0])
+        if dim != ndim_expected:
+            raise ValueError(f"{name} needs a {ndim_expected}-D grid, got {dim}-D")
+        return run_gb300_backend(kgrid, medium, source, sensor, simulation_options, execution_options)
+
+    run.__name__ = run.__qualname__ = name
+    run.__doc__ = (f"{name}(kgrid, source, sensor, medium, simulation_options, execution_options) on the GB300 "
+                   "time loop: the legacy signature (kwave/kspaceFirstOrder2D.py:140-148, "
+                   "kwave/kspaceFirstOrder3D.py) taking the python-backend branch "
+                   "(kwave/kspaceFirstOrder2D.py:215-218) straight to :func:`run_gb300_backend`.  "
+                   "``simulation_options`` is read for pml_size, pml_alpha, use_sg, use_kspace and "
+                   "smooth_p0; ``execution_options`` is accepted and ignored.")
+    return run
+
+
+kspaceFirstOrder2D = _legacy(2, "kspaceFirstOrder2D")
+kspaceFirstOrder3D = _legacy(3, "kspaceFirstOrder3D")
+
+
 _installed = {}
 
 

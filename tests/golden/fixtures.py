@@ -4,7 +4,10 @@ A case file ``<name>.npz`` holds
   * ``in:<key>``       problem inputs (see ``oracle/kspace_oracle.py`` for keys),
   * ``ref32:<key>``    outputs of the unmodified reference solver, dtype=float32,
   * ``ref64:<key>``    outputs of the unmodified reference solver, dtype=float64.
+  * ``meta:<key>``     anything else the case needs (options of the call).
 Strings and tuples are stored as 0-d/1-d numpy arrays; ``None`` is omitted.
+Cases of the solver itself sit in this folder; cases of the entry points
+built on it (unified ``kspaceFirstOrder``, ``TimeReversal``) in ``api/``.
 """
 from pathlib import Path
 
@@ -17,7 +20,11 @@ _STR_KEYS = ("p_mode", "u_mode", "alpha_mode")
 _BOOL_KEYS = ("use_sg", "use_kspace", "smooth_p0")
 
 
-def save_case(name, prob, outs32, outs64, meta=None):
+def _dir(subdir):
+    return GOLDEN_DIR / subdir if subdir else GOLDEN_DIR
+
+
+def save_case(name, prob, outs32, outs64, meta=None, subdir=None):
     arrs = {}
     for k, v in prob.items():
         if v is None:
@@ -29,11 +36,12 @@ def save_case(name, prob, outs32, outs64, meta=None):
         arrs[f"ref64:{k}"] = np.asarray(v)
     for k, v in (meta or {}).items():
         arrs[f"meta:{k}"] = np.asarray(v)
-    np.savez_compressed(GOLDEN_DIR / f"{name}.npz", **arrs)
+    _dir(subdir).mkdir(exist_ok=True)
+    np.savez_compressed(_dir(subdir) / f"{name}.npz", **arrs)
 
 
-def load_case(name):
-    z = np.load(GOLDEN_DIR / f"{name}.npz", allow_pickle=False)
+def load_case(name, subdir=None):
+    z = np.load(_dir(subdir) / f"{name}.npz", allow_pickle=False)
     prob, r32, r64, meta = {}, {}, {}, {}
     for key in z.files:
         kind, k = key.split(":", 1)
@@ -57,5 +65,5 @@ def load_case(name):
     return prob, r32, r64, meta
 
 
-def case_names():
-    return sorted(p.stem for p in GOLDEN_DIR.glob("*.npz"))
+def case_names(subdir=None):
+    return sorted(p.stem for p in _dir(subdir).glob("*.npz"))

@@ -1,0 +1,71 @@
+"""Unified ``kspaceFirstOrder(..., backend="gb300")`` and ``TimeReversal`` on
+the GPU against the reference's results (tests/golden/api).
+
+Same bar as the solver parity: 1e-5 relative L2 against the reference's
+float32 result for every returned key (or, where float32 itself cannot
+resolve a quantity, within 1.5x the reference's own float32-vs-float64 gap
+of the float64 result).
+"""
+from types import SimpleNamespace as NS
+
+import numpy as np
+import pytest
+
+import api_cases
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def check(name, got, r32, r64):
+    assert set(got) == set(r32), (sorted(got), sorted(r32))
+    for k in sorted(r32):
+        assert got[k].shape == r32[k].shape, (k, got[k].shape, r32[k].shape)
+        assert np.all(np.isfinite(got[k])), k
+        e32, e64, gap = rel_l2(got[k], r32[k]), rel_l2(got[k], r64[k]), rel_l2(r32[k], r64[k])
+        print(f"{name}:{k} vs ref32 {e32:.2e} vs ref64 {e64:.2e} (ref32 vs ref64 {gap:.2e})")
+        if gap > 0.5 * TOL:
+            assert e32 <= TOL or e64 <= 1.5 * gap + 1e-6, (k, e32, e64, gap)
+        else:
+            assert e32 <= TOL, (k, e32, e64)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300 import _lib
+
+    _lib.require_device()
+
+
+@pytest.mark.parametrize("name", api_cases.names("unified"))
+def test_unified_entry_point(name):
+    from kwave_gb300 import kspaceFirstOrder
+
+    prob, opts, r32, r64 = api_cases.load(name)
+    kgrid, medium, source, sensor = api_cases.objects(prob)
+    got = kspaceFirstOrder(kgrid, medium, source, sensor, backend="gb300", **opts)
+    check(name, got, r32, r64)
+
+
+def test_time_reversal():
+    from kwave_gb300 import TimeReversal
+
+    prob, opts, r32, r64 = api_cases.load("tr2d")
+    kgrid, medium, _, _ = api_cases.objects(prob)
+    sensor = NS(mask=prob["sensor_mask"], record=["p"], recorded_pressure=prob["recorded_pressure"])
+    tr = TimeReversal(kgrid, medium, sensor, compensation_factor=opts["compensation_factor"])
+    so = NS(pml_size=opts["pml_size"], pml_alpha=opts["pml_alpha"], use_sg=True, use_kspace=True, smooth_p0=True)
+    got = tr(None, so, None)                        # default: the GB300 legacy 2-D entry point
+    check("tr2d", {"p0_recon": got}, r32, r64)
+    # the reconstruction resembles the true p0 on the region the line sees
+    assert np.corrcoef(got.T.ravel(), prob["p0_true"][10:-10, 10:-10].ravel())[0, 1] > 0.5
