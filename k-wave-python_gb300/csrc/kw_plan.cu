@@ -363,6 +363,7 @@ static int zero_state(kw_plan* p) {
     CK(cudaMemset(p->d_rho[a], 0, p->ntot * sizeof(float)));
   }
   CK(cudaMemset(p->d_p, 0, p->ntot * sizeof(float)));
+  if (p->d_rhosum) CK(cudaMemset(p->d_rhosum, 0, p->ntot * sizeof(float)));
   for (int b = 0; b < KW_NBUF; ++b)
     if (p->d_S[b]) CK(cudaMemset(p->d_S[b], 0, p->spec_elems * sizeof(float2)));
   for (int s = 0; s < 7; ++s)

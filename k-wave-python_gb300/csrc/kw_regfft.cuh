@@ -35,6 +35,14 @@ __device__ __forceinline__ float sinc_taylor(float x) {
   return s;
 }
 
+// sin(x)/x from the same series given y = x^2 < 9
+__device__ __forceinline__ float sinc_taylor_sq(float y) {
+  float s = 1.0f;
+#pragma unroll
+  for (int n = 10; n >= 1; --n) s = fmaf(-y * (1.0f / float((2 * n) * (2 * n + 1))), s, 1.0f);
+  return s;
+}
+
 // cos/sin(2 pi j / 32), j = 0..31 (constant twiddles of the small DFTs)
 __device__ __forceinline__ float2 w32(int j) {
   // exp(-2 pi i j / 32)

@@ -1,493 +1,44 @@
-// Row stages of the time step for power-of-two last-axis lengths, with all
-// real-space physics held in registers in the layout of the row FFT.
-//
-// P consecutive threads own one row of L = 2M reals; thread t owns the float2
-// pairs n = t + P j (j < E), i.e. reals 2n and 2n+1.  The inverse row
-// transform (half spectrum -> reals) leaves exactly these pairs in registers
-// and the forward transform starts from them, so the physics between them
-// (velocity update, split-density update, equation of state, sources,
-// sensors) needs no shared-memory staging: fields are read and written as
-// float2 straight from global memory.  Shared memory holds only twiddles and
-// the per-row FFT exchange regions.
-//
-// The arithmetic and its order follow kwave/solvers/kspace_solver.py
-// (Simulation.step, :691-747) as the generic row kernel does.
-#include "kw_kernels.cuh"
-#include "kw_regfft.cuh"
-
-namespace {
-
-__device__ __forceinline__ float2 ld2(const float* p, long long i) { return reinterpret_cast<const float2*>(p)[i]; }
-__device__ __forceinline__ void st2(float* p, long long i, float2 v) { reinterpret_cast<float2*>(p)[i] = v; }
-__device__ __forceinline__ float2 fld2(const float* p, float s, long long i) {
-  return p ? ld2(p, i) : make_float2(s, s);
-}
+// Register row stages, first group: the stages of every time step (initial
+// condition, velocity, density) and the public launch/attribute dispatch.
+// The kernel template is kw_rows_reg.cuh; the other stages are instantiated
+// in kw_rows_reg2.cu.
+#include "kw_rows_reg.cuh"
 
 template <int E, int P>
-struct RowCtx {
-  static constexpr int M = E * P;
-  const RowsParams& Q;
-  const float2* tw;
-  const float2* twp;
-  float2* exr;      // this row's exchange region
-  int row, t, grow;
-  bool ok;          // row < nrows
-  long long rbase;  // float2 index of the row's first pair
-
-  // half-spectrum row -> register pairs (unnormalised: L * x)
-  __device__ __forceinline__ void c2r(const float2* S, float2 (&v)[E]) const {
-    const float2* sr = S + (long long)(ok ? grow : 0) * Q.Hp;
-#pragma unroll
-    for (int m = 0; m < E / P; ++m)
-#pragma unroll
-      for (int k2 = 0; k2 < P; ++k2) {
-        const int k = t + P * m + E * k2;
-        float2 z = make_float2(0.f, 0.f);
-        if (ok) {
-          const float2 xk = sr[k];
-          const float2 xc = cconj(sr[M - k]);
-          const float2 e = cadd(xk, xc);
-          const float2 o = kwreg::cmulf(csub(xk, xc), cconj(twp[k]));
-          z = make_float2(e.x - o.y, e.y + o.x);
-        }
-        v[m * P + k2] = cconj(z);
-      }
-    kwreg::Reg<E, P>::rev(v, t, exr, 1, tw, [] __device__() { __syncwarp(); });
-#pragma unroll
-    for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
-  }
-
-  // register pairs -> half-spectrum row
-  __device__ __forceinline__ void r2c(float2 (&v)[E], float2* S) const {
-    kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, [] __device__() { __syncwarp(); });
-#pragma unroll
-    for (int m = 0; m < E / P; ++m)
-#pragma unroll
-      for (int k2 = 0; k2 < P; ++k2) exr[t + P * m + E * k2] = v[m * P + k2];
-    __syncwarp();
-    if (ok) {
-      float2* so = S + (long long)grow * Q.Hp;
-      for (int k = t; k <= M; k += P) {
-        const float2 zk = exr[k == M ? 0 : k];
-        const float2 zc = cconj(exr[k == 0 ? 0 : M - k]);
-        const float2 e = cscale(cadd(zk, zc), 0.5f);
-        const float2 d = csub(zk, zc);
-        const float2 o = make_float2(0.5f * d.y, -0.5f * d.x);
-        so[k] = cadd(e, kwreg::cmulf(twp[k], o));
-      }
-    }
-    __syncwarp();
-  }
-
-  // PML factors of the two reals of pair n along `axis`
-  __device__ __forceinline__ float2 pml2(const float* tab, int axis, int n) const {
-    if (axis == Q.ndim - 1) return ld2(tab, n);
-    const int idx = (axis == 0) ? (Q.ndim == 3 ? grow / Q.N1 : grow) : grow % Q.N1;
-    const float s = tab[idx];
-    return make_float2(s, s);
-  }
-
-  // sparse source on this row (kspace_solver.py:86-109): owner thread updates its pair
-  __device__ __forceinline__ void source(const KwSrcDev& S, float2 (&v)[E]) const {
-    if (!S.active || Q.t >= S.len || !ok) return;
-    const int e0 = S.row_ptr[grow], e1 = S.row_ptr[grow + 1];
-    for (int e = e0; e < e1; ++e) {
-      const int4 en = S.ent[e];
-      const int n = en.y >> 1;
-      if ((n % P) != t) continue;
-      const int jj = n / P;
-      const float val = S.sig[(long long)Q.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
-#pragma unroll
-      for (int j = 0; j < E; ++j)
-        if (j == jj) {
-          float& f = (en.y & 1) ? v[j].y : v[j].x;
-          f = (S.mode == SRC_DIRICHLET) ? val : __fadd_rn(f, val);
-        }
-    }
-  }
-
-  // values of a source at step t on this row, zero elsewhere (the field whose
-  // k-space corrected version is added)
-  __device__ __forceinline__ void scatter(const KwSrcDev& S, float2 (&v)[E]) const {
-#pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = make_float2(0.f, 0.f);
-    if (!ok) return;
-    const int e0 = S.row_ptr[grow], e1 = S.row_ptr[grow + 1];
-    for (int e = e0; e < e1; ++e) {
-      const int4 en = S.ent[e];
-      const int n = en.y >> 1;
-      if ((n % P) != t) continue;
-      const int jj = n / P;
-      const float val = S.sig[(long long)Q.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
-#pragma unroll
-      for (int j = 0; j < E; ++j)
-        if (j == jj) {
-          if (en.y & 1)
-            v[j].y = val;
-          else
-            v[j].x = val;
-        }
-    }
-  }
-
-  __device__ __forceinline__ void record(const float2 (&v)[E], float* rec) const {
-    if (rec == nullptr || Q.rec_row < 0 || Q.sens_row_ptr == nullptr || !ok) return;
-    const int e0 = Q.sens_row_ptr[grow], e1 = Q.sens_row_ptr[grow + 1];
-    float* out = rec + (long long)Q.rec_row * Q.nslots;
-    for (int e = e0; e < e1; ++e) {
-      const int4 en = Q.sens_ent[e];
-      const int n = en.y >> 1;
-      if ((n % P) != t) continue;
-      const int jj = n / P;
-      float val = 0.f;
-#pragma unroll
-      for (int j = 0; j < E; ++j)
-        if (j == jj) val = (en.y & 1) ? v[j].y : v[j].x;
-      out[en.z] = val;
-    }
-  }
-};
-
-// velocity on the pressure grid, Re F^-1[e^{-i k d/2} F[u_i]] (kspace_solver.py:740-743)
-template <int E, int P>
-__device__ __forceinline__ void record_unstaggered(const RowCtx<E, P>& c, const RowsParams& Q, float2 (&v)[E]) {
-  if (!Q.rec_us) return;
-  for (int a = 0; a < Q.ndim; ++a) {
-    if (!(Q.rec_us & (1 << a))) continue;
-    c.c2r(Q.S[B_US0 + a], v);
-    c.record(v, Q.rec[4 + a]);
-  }
-}
-
-}  // namespace
-
-// EXTRA: this launch has k-space corrected sources or records the velocity on
-// the pressure grid; without it those paths are compiled out, which keeps the
-// common launch at its smaller register budget.
-template <int E, int P, int STAGE, bool EXTRA>
-__global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsParams Q) {
-  constexpr int M = E * P;
-  extern __shared__ float4 smem_f4[];
-  float2* tw = reinterpret_cast<float2*>(smem_f4);
-  float2* twp = tw + M;
-  float2* ex = twp + (M + 1);
-  for (int i = threadIdx.x; i < M; i += blockDim.x) tw[i] = Q.tw[i];
-  for (int i = threadIdx.x; i <= M; i += blockDim.x) twp[i] = Q.twpost[i];
-  __syncthreads();
-
-  const int row = threadIdx.x / P, t = threadIdx.x % P;
-  const int R = blockDim.x / P;
-  const int grow = blockIdx.x * R + row;
-  RowCtx<E, P> c{Q, tw, twp, ex + row * Q.ex_stride, row, t, grow, grow < Q.nrows, (long long)grow * M};
-  const int D = Q.ndim;
-  float2 v[E];
-
-  if constexpr (STAGE == ST_INIT) {
-    // t = 0 with p0: p = p0, rho_i = p0 / (c0^2 D) (kspace_solver.py:729-733)
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
-      float2 pv = make_float2(0.f, 0.f);
-      if (c.ok) {
-        pv = ld2(Q.p0, i);
-        if (Q.p0_scale) {
-          const float sc = *Q.p0_scale;
-          pv = make_float2(__fmul_rn(pv.x, sc), __fmul_rn(pv.y, sc));
-        }
-        const float2 cc = fld2(Q.c0, Q.c0_s, i);
-        const float2 r = make_float2(__fdiv_rn(pv.x, __fmul_rn(__fmul_rn(cc.x, cc.x), (float)D)),
-                                     __fdiv_rn(pv.y, __fmul_rn(__fmul_rn(cc.y, cc.y), (float)D)));
-        for (int a = 0; a < D; ++a) st2(Q.rho[a], i, r);
-        if (Q.write_p) st2(Q.p, i, pv);
-      }
-      v[j] = pv;
-    }
-    c.record(v, Q.rec[0]);
-    c.r2c(v, Q.S[3]);
-    return;
-  }
-
-  if constexpr (STAGE == ST_U) {
-    // u_i = pml_sg (pml_sg u_i - dt/rho_sg g_i) (kspace_solver.py:703-707)
-    for (int a = 0; a < D; ++a) {
-      c.c2r(Q.S[a], v);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        const int n = t + P * j;
-        const long long i = c.rbase + n;
-        if (!c.ok) continue;
-        const float2 g = v[j];
-        const float2 dtr = fld2(Q.dtrsg[a], Q.dtrsg_s[a], i);
-        if (Q.init) {
-          v[j] = make_float2(__fmul_rn(__fmul_rn(dtr.x, 0.5f), g.x), __fmul_rn(__fmul_rn(dtr.y, 0.5f), g.y));
-        } else {
-          const float2 sg = c.pml2(Q.pmlsg[a], a, n);
-          const float2 u = ld2(Q.u[a], i);
-          v[j] = make_float2(__fmul_rn(sg.x, __fsub_rn(__fmul_rn(sg.x, u.x), __fmul_rn(dtr.x, g.x))),
-                             __fmul_rn(sg.y, __fsub_rn(__fmul_rn(sg.y, u.y), __fmul_rn(dtr.y, g.y))));
-        }
-      }
-      if (!Q.init) {
-        if (EXTRA && Q.srcu_on[a]) {
-          // u_i += Re F^-1[source_kappa F[s_i]] (kspace_solver.py:91-98)
-          float2 w[E];
-          c.c2r(Q.S[B_SRCU0 + a], w);
-#pragma unroll
-          for (int j = 0; j < E; ++j) v[j] = make_float2(__fadd_rn(v[j].x, w[j].x), __fadd_rn(v[j].y, w[j].y));
-        } else {
-          c.source(Q.src[3 + a], v);
-        }
-      }
-      if (c.ok) {
-#pragma unroll
-        for (int j = 0; j < E; ++j) st2(Q.u[a], c.rbase + t + P * j, v[j]);
-      }
-      c.record(v, Q.rec[1 + a]);
-      if (!Q.init || Q.init_r2c) c.r2c(v, Q.S[a]);
-    }
-    return;
-  }
-
-  if constexpr (STAGE == ST_RHO) {
-    // mass conservation with split density (kspace_solver.py:709-717)
-    float2 nl[E], div[E], rs[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      nl[j] = make_float2(1.f, 1.f);
-      div[j] = make_float2(0.f, 0.f);
-      rs[j] = make_float2(0.f, 0.f);
-      if (Q.nonlin && c.ok) {
-        const long long i = c.rbase + t + P * j;
-        const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-        float2 sr = ld2(Q.rho[0], i);
-        for (int a = 1; a < D; ++a) {
-          const float2 ra = ld2(Q.rho[a], i);
-          sr = make_float2(__fadd_rn(sr.x, ra.x), __fadd_rn(sr.y, ra.y));
-        }
-        nl[j] = make_float2(__fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.x), r0v.x), r0v.x),
-                            __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v.y), r0v.y));
-      }
-    }
-    float2 cp[EXTRA ? E : 1];
-    if constexpr (EXTRA) {
-      if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
-    }
-    for (int a = 0; a < D; ++a) {
-      c.c2r(Q.S[a], v);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        const int n = t + P * j;
-        const long long i = c.rbase + n;
-        const float2 du = v[j];
-        div[j] = make_float2(__fadd_rn(div[j].x, du.x), __fadd_rn(div[j].y, du.y));
-        if (!c.ok) continue;
-        const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-        const float2 pm = c.pml2(Q.pml[a], a, n);
-        const float2 ro = ld2(Q.rho[a], i);
-        const float tx = __fmul_rn(__fmul_rn(__fmul_rn(Q.dt, r0v.x), du.x), nl[j].x);
-        const float ty = __fmul_rn(__fmul_rn(__fmul_rn(Q.dt, r0v.y), du.y), nl[j].y);
-        v[j] = make_float2(__fmul_rn(pm.x, __fsub_rn(__fmul_rn(pm.x, ro.x), tx)),
-                           __fmul_rn(pm.y, __fsub_rn(__fmul_rn(pm.y, ro.y), ty)));
-      }
-      bool corrected = false;
-      if constexpr (EXTRA) {
-        if (Q.srcp_on) {
-          // rho_i += Re F^-1[source_kappa F[s]] / d_i (kspace_solver.py:91-98, scale :619-624)
-          const float id = Q.inv_d[a];
-#pragma unroll
-          for (int j = 0; j < E; ++j)
-            v[j] = make_float2(__fadd_rn(v[j].x, __fmul_rn(cp[j].x, id)), __fadd_rn(v[j].y, __fmul_rn(cp[j].y, id)));
-          corrected = true;
-        }
-      }
-      if (!corrected) c.source(Q.src[a], v);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        if (c.ok) st2(Q.rho[a], c.rbase + t + P * j, v[j]);
-        rs[j] = (a == 0) ? v[j] : make_float2(__fadd_rn(rs[j].x, v[j].x), __fadd_rn(rs[j].y, v[j].y));
-      }
-    }
-    if (Q.absorb == 1) {
-      // power law: transform rho0 * div and the density sum (kspace_solver.py:498, :524)
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        const long long i = c.rbase + t + P * j;
-        if (c.ok) {
-          st2(Q.rho_sum, i, rs[j]);
-          const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-          v[j] = make_float2(__fmul_rn(r0v.x, div[j].x), __fmul_rn(r0v.y, div[j].y));
-        } else {
-          v[j] = make_float2(0.f, 0.f);
-        }
-      }
-      c.r2c(v, Q.S[0]);
-      if (Q.disp) c.r2c(rs, Q.S[1]);
-      if constexpr (EXTRA) record_unstaggered(c, Q, v);
-      return;
-    }
-    // equation of state without fractional Laplacians (kspace_solver.py:719-723)
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
-      float2 pv = make_float2(0.f, 0.f);
-      if (c.ok) {
-        const float2 cc = fld2(Q.c0, Q.c0_s, i);
-        const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-        float ax = rs[j].x, ay = rs[j].y;
-        if (Q.absorb == 2) {
-          const float2 tau = fld2(Q.tau, Q.tau_s, i);
-          ax = __fadd_rn(ax, __fmul_rn(__fmul_rn(tau.x, r0v.x), div[j].x));
-          ay = __fadd_rn(ay, __fmul_rn(__fmul_rn(tau.y, r0v.y), div[j].y));
-        }
-        if (Q.nonlin) {
-          const float2 b = fld2(Q.bona, Q.bona_s, i);
-          ax = __fadd_rn(ax, __fdiv_rn(__fmul_rn(b.x, __fmul_rn(rs[j].x, rs[j].x)), __fmul_rn(2.f, r0v.x)));
-          ay = __fadd_rn(ay, __fdiv_rn(__fmul_rn(b.y, __fmul_rn(rs[j].y, rs[j].y)), __fmul_rn(2.f, r0v.y)));
-        }
-        pv = make_float2(__fmul_rn(__fmul_rn(cc.x, cc.x), ax), __fmul_rn(__fmul_rn(cc.y, cc.y), ay));
-        if (Q.write_p) st2(Q.p, i, pv);
-      }
-      v[j] = pv;
-    }
-    c.record(v, Q.rec[0]);
-    c.r2c(v, Q.S[3]);
-    if constexpr (EXTRA) record_unstaggered(c, Q, v);
-    return;
-  }
-
-  if constexpr (STAGE == ST_SRC) {
-    // scattered source fields of this step, transformed for the source-kappa pass
-    if (Q.srcp_on) {
-      c.scatter(Q.src[0], v);
-      c.r2c(v, Q.S[B_SRCP]);
-    }
-    for (int a = 0; a < D; ++a)
-      if (Q.srcu_on[a]) {
-        c.scatter(Q.src[3 + a], v);
-        c.r2c(v, Q.S[B_SRCU0 + a]);
-      }
-    return;
-  }
-
-  if constexpr (STAGE == ST_P0FFT) {
-    // spectrum of p0 for the smoothing window
-#pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = c.ok ? ld2(Q.p0w, c.rbase + t + P * j) : make_float2(0.f, 0.f);
-    c.r2c(v, Q.S[B_P]);
-    return;
-  }
-
-  if constexpr (STAGE == ST_P0BACK) {
-    c.c2r(Q.S[B_P], v);
-    if (c.ok) {
-#pragma unroll
-      for (int j = 0; j < E; ++j) st2(Q.p0w, c.rbase + t + P * j, v[j]);
-    }
-    return;
-  }
-
-  if constexpr (STAGE == ST_UREC) {
-    record_unstaggered(c, Q, v);
-    return;
-  }
-
-  if constexpr (STAGE == ST_EOS) {
-  // p = c0^2 (rho + tau F^-1[nabla1 F[rho0 div]] - eta F^-1[nabla2 F[rho]] + B/A rho^2 / (2 rho0))
-  float2 w[E];
-  c.c2r(Q.S[0], v);
-  if (Q.disp) c.c2r(Q.S[1], w);
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    const long long i = c.rbase + t + P * j;
-    float2 pv = make_float2(0.f, 0.f);
-    if (c.ok) {
-      const float2 rsum = ld2(Q.rho_sum, i);
-      const float2 cc = fld2(Q.c0, Q.c0_s, i);
-      const float2 tau = fld2(Q.tau, Q.tau_s, i);
-      float ax = __fadd_rn(rsum.x, __fmul_rn(tau.x, v[j].x));
-      float ay = __fadd_rn(rsum.y, __fmul_rn(tau.y, v[j].y));
-      if (Q.disp) {
-        const float2 eta = fld2(Q.eta, Q.eta_s, i);
-        ax = __fsub_rn(ax, __fmul_rn(eta.x, w[j].x));
-        ay = __fsub_rn(ay, __fmul_rn(eta.y, w[j].y));
-      }
-      if (Q.nonlin) {
-        const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-        const float2 b = fld2(Q.bona, Q.bona_s, i);
-        ax = __fadd_rn(ax, __fdiv_rn(__fmul_rn(b.x, __fmul_rn(rsum.x, rsum.x)), __fmul_rn(2.f, r0v.x)));
-        ay = __fadd_rn(ay, __fdiv_rn(__fmul_rn(b.y, __fmul_rn(rsum.y, rsum.y)), __fmul_rn(2.f, r0v.y)));
-      }
-      pv = make_float2(__fmul_rn(__fmul_rn(cc.x, cc.x), ax), __fmul_rn(__fmul_rn(cc.y, cc.y), ay));
-      if (Q.write_p) st2(Q.p, i, pv);
-    }
-    v[j] = pv;
-  }
-  c.record(v, Q.rec[0]);
-  c.r2c(v, Q.S[3]);
-  }
-}
-
-template <int E, int P, bool X>
-static cudaError_t rows_v2_launch_x(int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
+static cudaError_t rows_a_launch(int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
   switch (stage) {
-    case ST_INIT: k_rows_v2<E, P, ST_INIT, X><<<grid, 128, smem, st>>>(Q); break;
-    case ST_U: k_rows_v2<E, P, ST_U, X><<<grid, 128, smem, st>>>(Q); break;
-    case ST_RHO: k_rows_v2<E, P, ST_RHO, X><<<grid, 128, smem, st>>>(Q); break;
-    case ST_EOS: k_rows_v2<E, P, ST_EOS, X><<<grid, 128, smem, st>>>(Q); break;
-    case ST_SRC: k_rows_v2<E, P, ST_SRC, X><<<grid, 128, smem, st>>>(Q); break;
-    case ST_P0FFT: k_rows_v2<E, P, ST_P0FFT, X><<<grid, 128, smem, st>>>(Q); break;
-    case ST_P0BACK: k_rows_v2<E, P, ST_P0BACK, X><<<grid, 128, smem, st>>>(Q); break;
-    default: k_rows_v2<E, P, ST_UREC, X><<<grid, 128, smem, st>>>(Q); break;
+    case ST_INIT: return rows_v2_launch_stage<E, P, ST_INIT>(grid, smem, st, Q);
+    case ST_U: return rows_v2_launch_stage<E, P, ST_U>(grid, smem, st, Q);
+    case ST_RHO:
+      if (Q.absorb == 1 && Q.rho_sum) return rows_v2_launch_stage<E, P, ST_RHO_PL>(grid, smem, st, Q);
+      return rows_v2_launch_stage<E, P, ST_RHO>(grid, smem, st, Q);
+    default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 template <int E, int P>
-static cudaError_t rows_v2_launch(int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
-  const bool extra = Q.srcp_on || Q.srcu_on[0] || Q.srcu_on[1] || Q.srcu_on[2] || Q.rec_us;
-  return extra ? rows_v2_launch_x<E, P, true>(stage, grid, smem, st, Q)
-               : rows_v2_launch_x<E, P, false>(stage, grid, smem, st, Q);
-}
-
-template <int E, int P, bool X>
-static cudaError_t rows_v2_attr_x() {
-  cudaError_t e = cudaSuccess;
-  const int lim = 100 * 1024;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_INIT, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_U, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_RHO, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_EOS, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_SRC, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_UREC, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_P0FFT, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rows_v2<E, P, ST_P0BACK, X>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+static cudaError_t rows_a_attr() {
+  cudaError_t e = rows_v2_attr_stage<E, P, ST_INIT>();
+  if (e == cudaSuccess) e = rows_v2_attr_stage<E, P, ST_U>();
+  if (e == cudaSuccess) e = rows_v2_attr_stage<E, P, ST_RHO>();
+  if (e == cudaSuccess) e = rows_v2_attr_stage<E, P, ST_RHO_PL>();
   return e;
 }
 
-template <int E, int P>
-static cudaError_t rows_v2_attr() {
-  cudaError_t e = rows_v2_attr_x<E, P, false>();
-  return e == cudaSuccess ? rows_v2_attr_x<E, P, true>() : e;
-}
-
-#define KW_V2_SWITCH(m, CALL)              \
-  switch (m) {                             \
-    case 64: return CALL(16, 4);           \
-    case 128: return CALL(16, 8);          \
-    case 256: return CALL(16, 16);         \
-    case 512: return CALL(32, 16);         \
-    case 1024: return CALL(32, 32);        \
-    default: return cudaErrorInvalidValue; \
-  }
-
-cudaError_t kw_rows_v2_attr(int m) {
-#define KW_R(E, P) rows_v2_attr<E, P>()
+static cudaError_t kw_rows_v2_attr_a(int m) {
+#define KW_R(E, P) rows_a_attr<E, P>()
   KW_V2_SWITCH(m, KW_R)
 #undef KW_R
 }
 
+cudaError_t kw_rows_v2_attr(int m) {
+  cudaError_t e = kw_rows_v2_attr_a(m);
+  return e == cudaSuccess ? kw_rows_v2_attr_b(m) : e;
+}
+
 cudaError_t kw_rows_v2_launch(int m, int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
-#define KW_R(E, P) rows_v2_launch<E, P>(stage, grid, smem, st, Q)
+  if (stage != ST_INIT && stage != ST_U && stage != ST_RHO) return kw_rows_v2_launch_b(m, stage, grid, smem, st, Q);
+#define KW_R(E, P) rows_a_launch<E, P>(stage, grid, smem, st, Q)
   KW_V2_SWITCH(m, KW_R)
 #undef KW_R
 }

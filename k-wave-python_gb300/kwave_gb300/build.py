@@ -17,7 +17,8 @@ CSRC = PKG_DIR.parent / "csrc"
 INCLUDE = PKG_DIR.parent.parent / "include"
 BUILD_DIR = PKG_DIR.parent / "_build"
 LIB = PKG_DIR / "libkwave_gb300.so"
-SOURCES = ["kw_kernels.cu", "kw_axis_tma.cu", "kw_rows_reg.cu", "kw_plan.cu", "kw_noalloc.cu"]
+SOURCES = ["kw_kernels.cu", "kw_axis_tma.cu", "kw_axis_tma_plain.cu", "kw_axis_tma_ops.cu", "kw_axis_tma_ops2.cu",
+           "kw_rows_reg.cu", "kw_rows_reg2.cu", "kw_plan.cu", "kw_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "--extended-lambda"]
 
@@ -58,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             print(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=4) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(_sources()), max(2, os.cpu_count() or 2))) as ex:
         objs = list(ex.map(compile_one, _sources()))
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
