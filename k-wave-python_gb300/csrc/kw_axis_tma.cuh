@@ -438,12 +438,12 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
 // launch geometry (shared by the host side of every translation unit)
 // ---------------------------------------------------------------------------
 
-// Tile width: plain passes along y of a 3-D grid (axis 1) use narrow 8-column
-// tiles at three CTAs per SM for length 256; everything else 256 / P columns
-// at two CTAs per SM (lengths <= 256) or one (512, 1024).
-inline bool kw_tma_narrow(int n, int axis, int kind) { return n == 256 && axis == 1 && kind == KK_PLAIN; }
-inline int kw_tma_tile_cols(int n, int P, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 8 : 256 / P; }
-inline int kw_tma_per_sm(int n, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 3 : (n <= 256 ? 2 : 1); }
+// Tile width: lengths up to 256 use tiles of 128 / P columns (128 consumer
+// threads plus the producer warp) at three CTAs per SM, which leaves each
+// thread 128 registers; 512 and 1024 use 256 / P columns at one CTA per SM.
+inline bool kw_tma_narrow(int n, int axis, int kind) { return n <= 256; }
+inline int kw_tma_tile_cols(int n, int P, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 128 / P : 256 / P; }
+inline int kw_tma_per_sm(int n, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 3 : 1; }
 
 inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
   const int T = kw_tma_tile_cols(n, P, axis, kind), RS = n + E + 1;
@@ -452,20 +452,15 @@ inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
          2 * 2 * sizeof(uint64_t) + 16;
 }
 
-// Instantiation table: (E, P, stages, CTAs per SM, tile columns) per length
-// (used inside templates on KIND; the narrow tiles exist for plain passes only).
-#define KW_TMA_SWITCH(n, narrow_, CALL)              \
-  switch (n) {                                       \
-    case 64: return CALL(16, 4, 2, 2, 64);           \
-    case 128: return CALL(16, 8, 2, 2, 32);          \
-    case 256:                                        \
-      if constexpr (KIND == KK_PLAIN) {              \
-        if (narrow_) return CALL(16, 16, 2, 3, 8);   \
-      }                                              \
-      return CALL(16, 16, 2, 2, 16);                 \
-    case 512: return CALL(32, 16, 2, 1, 16);         \
-    case 1024: return CALL(32, 32, 2, 1, 8);         \
-    default: return cudaErrorInvalidValue;           \
+// Instantiation table: (E, P, stages, CTAs per SM, tile columns) per length.
+#define KW_TMA_SWITCH(n, narrow_, CALL)      \
+  switch (n) {                               \
+    case 64: return CALL(16, 4, 2, 3, 32);   \
+    case 128: return CALL(16, 8, 2, 3, 16);  \
+    case 256: return CALL(16, 16, 2, 3, 8);  \
+    case 512: return CALL(32, 16, 2, 1, 16); \
+    case 1024: return CALL(32, 32, 2, 1, 8); \
+    default: return cudaErrorInvalidValue;   \
   }
 
 // Attribute set-up and launch of one KIND (instantiated in the translation
@@ -475,20 +470,18 @@ cudaError_t kw_tma_attr_kind(int n, int axis) {
   int E, P;
   if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
   const int smem = (int)kw_tma_smem(n, E, P, axis, KIND);
-  const bool nar = kw_tma_narrow(n, axis, KIND);
 #define KW_T(E_, P_, S_, B_, T_) \
   cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-  KW_TMA_SWITCH(n, nar, KW_T)
+  KW_TMA_SWITCH(n, 0, KW_T)
 #undef KW_T
 }
 
 template <int KIND>
 cudaError_t kw_tma_launch_kind(int n, int axis, int grid, size_t smem, cudaStream_t st, const AxisParams& A,
                                const TmaMaps& maps, const TmaWork& W) {
-  const bool nar = kw_tma_narrow(n, axis, KIND);
 #define KW_T(E_, P_, S_, B_, T_) \
   (k_axis_tma<E_, P_, S_, B_, T_, KIND><<<grid, T_ * P_ + 32, smem, st>>>(A, maps, W), cudaGetLastError())
-  KW_TMA_SWITCH(n, nar, KW_T)
+  KW_TMA_SWITCH(n, 0, KW_T)
 #undef KW_T
 }
 

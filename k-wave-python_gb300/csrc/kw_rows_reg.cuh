@@ -367,8 +367,11 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     // mass conservation with split density and power-law absorption
     // (kspace_solver.py:709-717, :498, :524).  The nonlinear factor
     // (2 sum_a rho_a + rho0) / rho0 uses the sum stored by the previous step,
-    // which is the same float sum of the same values.
-    float2 div[E], rs[E];
+    // which is the same float sum of the same values.  Only the divergence
+    // stays in registers across the components; the new density sum is
+    // formed afterwards from the just-written rho_a (cache hits), which keeps
+    // this stage at two register arrays.
+    float2 div[E];
     float2 cp[EXTRA ? E : 1];
     if constexpr (EXTRA) {
       if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
@@ -407,28 +410,41 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
         }
       }
       if (!corrected) c.source(Q.src[a], v);
+      if (c.ok) {
 #pragma unroll
-      for (int j = 0; j < E; ++j) {
-        if (c.ok) st2(Q.rho[a], c.rbase + t + P * j, v[j]);
-        rs[j] = (a == 0) ? v[j] : make_float2(__fadd_rn(rs[j].x, v[j].x), __fadd_rn(rs[j].y, v[j].y));
+        for (int j = 0; j < E; ++j) st2(Q.rho[a], c.rbase + t + P * j, v[j]);
       }
     }
-    // transform rho0 * div and the density sum; the sum is kept for the
-    // equation of state and the next step's nonlinear factor
+    // rho0 * div -> spectrum 0
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       const long long i = c.rbase + t + P * j;
       if (c.ok) {
-        st2(Q.rho_sum, i, rs[j]);
         const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-        v[j] = make_float2(__fmul_rn(r0v.x, div[j].x), __fmul_rn(r0v.y, div[j].y));
+        div[j] = make_float2(__fmul_rn(r0v.x, div[j].x), __fmul_rn(r0v.y, div[j].y));
       } else {
-        v[j] = make_float2(0.f, 0.f);
+        div[j] = make_float2(0.f, 0.f);
       }
     }
-    c.r2c(v, Q.S[0]);
-    if (Q.disp) c.r2c(rs, Q.S[1]);
-    if constexpr (EXTRA) record_unstaggered(c, Q, v);
+    c.r2c(div, Q.S[0]);
+    if constexpr (EXTRA) record_unstaggered(c, Q, div);
+    // the new density sum (components added in order), kept for the equation
+    // of state and the next step's nonlinear factor, and its spectrum
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const long long i = c.rbase + t + P * j;
+      float2 rs = make_float2(0.f, 0.f);
+      if (c.ok) {
+        rs = ld2(Q.rho[0], i);
+        for (int a = 1; a < D; ++a) {
+          const float2 ra = ld2(Q.rho[a], i);
+          rs = make_float2(__fadd_rn(rs.x, ra.x), __fadd_rn(rs.y, ra.y));
+        }
+        st2(Q.rho_sum, i, rs);
+      }
+      v[j] = rs;
+    }
+    if (Q.disp) c.r2c(v, Q.S[1]);
     return;
   }
 
