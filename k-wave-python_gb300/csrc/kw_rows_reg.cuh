@@ -160,6 +160,50 @@ __device__ __forceinline__ void record_unstaggered(const RowCtx<E, P>& c, const 
   }
 }
 
+// Bulk prefetch into L2 of one contiguous byte range (16-byte aligned start
+// and size; no completion to wait for).
+__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Lane `lane` of warp 0 prefetches into L2 the lane-th array this block's
+// rows [r0, r0 + R) of stage STAGE will read: the rows of a block are
+// contiguous in every row-major array, so one bulk prefetch per array covers
+// them, and every later load of the stage hits L2 instead of waiting on HBM.
+template <int STAGE>
+__device__ __forceinline__ void prefetch_block(const RowsParams& Q, int r0, int lane) {
+  const int nr = min(Q.R, Q.nrows - r0);
+  if (nr <= 0) return;
+  const uint32_t sb = (uint32_t)nr * Q.Hp * 8u, fb = (uint32_t)nr * Q.L * 4u;
+  const long long so = (long long)r0 * Q.Hp, fo = (long long)r0 * Q.L;
+  const void* p = nullptr;
+  uint32_t bytes = 0;
+  const int D = Q.ndim;
+  auto spec = [&](int b) { p = Q.S[b] + so; bytes = sb; };
+  auto fld = [&](const float* f) { if (f) { p = f + fo; bytes = fb; } };
+  if constexpr (STAGE == ST_U) {
+    if (lane < D) spec(lane);
+    else if (lane < 2 * D) fld(Q.u[lane - D]);
+    else if (lane < 3 * D) fld(Q.dtrsg[lane - 2 * D]);
+  } else if constexpr (STAGE == ST_RHO_PL || STAGE == ST_RHO) {
+    if (lane < D) spec(lane);
+    else if (lane < 2 * D) fld(Q.rho[lane - D]);
+    else if (lane == 2 * D) fld(Q.rho0);
+    else if (lane == 2 * D + 1 && STAGE == ST_RHO_PL && Q.nonlin) fld(Q.rho_sum);
+    else if (lane == 2 * D + 2 && STAGE == ST_RHO) fld(Q.c0);
+  } else if constexpr (STAGE == ST_EOS) {
+    if (lane == 0) spec(0);
+    else if (lane == 1 && Q.disp) spec(1);
+    else if (lane == 2) fld(Q.rho_sum);
+    else if (lane == 3) fld(Q.c0);
+    else if (lane == 4) fld(Q.tau);
+    else if (lane == 5 && Q.disp) fld(Q.eta);
+    else if (lane == 6 && Q.nonlin) fld(Q.rho0);
+    else if (lane == 7 && Q.nonlin) fld(Q.bona);
+  }
+  if (p && bytes) l2_prefetch(p, bytes);
+}
+
 }  // namespace kwrows
 
 // EXTRA: this launch has k-space corrected sources or records the velocity on
@@ -172,6 +216,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
   float2* tw = reinterpret_cast<float2*>(smem_f4);
   float2* twp = tw + M;
   float2* ex = twp + (M + 1);
+  if (threadIdx.x < 32) kwrows::prefetch_block<STAGE>(Q, blockIdx.x * (blockDim.x / P), threadIdx.x);
   for (int i = threadIdx.x; i < M; i += blockDim.x) tw[i] = Q.tw[i];
   for (int i = threadIdx.x; i <= M; i += blockDim.x) twp[i] = Q.twpost[i];
   __syncthreads();
