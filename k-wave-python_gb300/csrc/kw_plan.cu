@@ -654,7 +654,11 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   if (p->rows_reg) {
     P.R = p->rows_R;
     P.ex_stride = p->rows_RS;
-    const size_t smem = sizeof(float2) * (2 * (size_t)p->Mfft + 1 + (size_t)p->rows_R * p->rows_RS);
+    // the power-law density stage keeps the divergence in shared memory (one
+    // float2 per thread and register pair)
+    const bool dsm = stage == ST_RHO && p->g.absorb_mode == 1 && p->d_rhosum;
+    const size_t smem = sizeof(float2) * (2 * (size_t)p->Mfft + 1 + (size_t)p->rows_R * p->rows_RS +
+                                          (dsm ? (size_t)128 * p->rows_regE : 0));
     const int grid = (p->nrows + p->rows_R - 1) / p->rows_R;
     CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
   } else {

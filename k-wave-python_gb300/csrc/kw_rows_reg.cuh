@@ -166,32 +166,30 @@ __device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// Lane `lane` of warp 0 prefetches into L2 the lane-th array this block's
-// rows [r0, r0 + R) of stage STAGE will read: the rows of a block are
-// contiguous in every row-major array, so one bulk prefetch per array covers
-// them, and every later load of the stage hits L2 instead of waiting on HBM.
+// Lane `lane` of warp 0 prefetches into L2 one of the arrays that component
+// `comp` of the density stage (or the equation of state) reads for this block's rows [r0, r0 + R): the rows of
+// a block are contiguous in every row-major array, so one bulk prefetch per
+// array covers them.  Component 0 also brings the arrays shared by all
+// components; each later component is prefetched while the previous one is
+// computed, so that only about one component's data per block is in flight.
 template <int STAGE>
-__device__ __forceinline__ void prefetch_block(const RowsParams& Q, int r0, int lane) {
+__device__ __forceinline__ void prefetch_block(const RowsParams& Q, int r0, int lane, int comp) {
   const int nr = min(Q.R, Q.nrows - r0);
-  if (nr <= 0) return;
+  if (nr <= 0 || comp >= Q.ndim) return;
   const uint32_t sb = (uint32_t)nr * Q.Hp * 8u, fb = (uint32_t)nr * Q.L * 4u;
   const long long so = (long long)r0 * Q.Hp, fo = (long long)r0 * Q.L;
   const void* p = nullptr;
   uint32_t bytes = 0;
-  const int D = Q.ndim;
   auto spec = [&](int b) { p = Q.S[b] + so; bytes = sb; };
   auto fld = [&](const float* f) { if (f) { p = f + fo; bytes = fb; } };
-  if constexpr (STAGE == ST_U) {
-    if (lane < D) spec(lane);
-    else if (lane < 2 * D) fld(Q.u[lane - D]);
-    else if (lane < 3 * D) fld(Q.dtrsg[lane - 2 * D]);
-  } else if constexpr (STAGE == ST_RHO_PL || STAGE == ST_RHO) {
-    if (lane < D) spec(lane);
-    else if (lane < 2 * D) fld(Q.rho[lane - D]);
-    else if (lane == 2 * D) fld(Q.rho0);
-    else if (lane == 2 * D + 1 && STAGE == ST_RHO_PL && Q.nonlin) fld(Q.rho_sum);
-    else if (lane == 2 * D + 2 && STAGE == ST_RHO) fld(Q.c0);
+  if constexpr (STAGE == ST_RHO_PL || STAGE == ST_RHO) {
+    if (lane == 0) spec(comp);
+    else if (lane == 1) fld(Q.rho[comp]);
+    else if (comp == 0 && lane == 2) fld(Q.rho0);
+    else if (comp == 0 && lane == 3 && STAGE == ST_RHO_PL && Q.nonlin) fld(Q.rho_sum);
+    else if (comp == 0 && lane == 3 && STAGE == ST_RHO) fld(Q.c0);
   } else if constexpr (STAGE == ST_EOS) {
+    if (comp != 0) return;
     if (lane == 0) spec(0);
     else if (lane == 1 && Q.disp) spec(1);
     else if (lane == 2) fld(Q.rho_sum);
@@ -216,7 +214,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
   float2* tw = reinterpret_cast<float2*>(smem_f4);
   float2* twp = tw + M;
   float2* ex = twp + (M + 1);
-  if (threadIdx.x < 32) kwrows::prefetch_block<STAGE>(Q, blockIdx.x * (blockDim.x / P), threadIdx.x);
+  if (threadIdx.x < 32) kwrows::prefetch_block<STAGE>(Q, blockIdx.x * (blockDim.x / P), threadIdx.x, 0);
   for (int i = threadIdx.x; i < M; i += blockDim.x) tw[i] = Q.tw[i];
   for (int i = threadIdx.x; i <= M; i += blockDim.x) twp[i] = Q.twpost[i];
   __syncthreads();
@@ -263,6 +261,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
   if constexpr (STAGE == ST_U) {
     // u_i = pml_sg (pml_sg u_i - dt/rho_sg g_i) (kspace_solver.py:703-707)
     for (int a = 0; a < D; ++a) {
+      if (threadIdx.x < 32) prefetch_block<STAGE>(Q, blockIdx.x * (blockDim.x / P), threadIdx.x, a + 1);
       c.c2r(Q.S[a], v);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
@@ -326,6 +325,7 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
       if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
     }
     for (int a = 0; a < D; ++a) {
+      if (threadIdx.x < 32) prefetch_block<STAGE>(Q, blockIdx.x * (blockDim.x / P), threadIdx.x, a + 1);
       c.c2r(Q.S[a], v);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
@@ -414,22 +414,27 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     // (2 sum_a rho_a + rho0) / rho0 uses the sum stored by the previous step,
     // which is the same float sum of the same values.  Only the divergence
     // stays in registers across the components; the new density sum is
-    // formed afterwards from the just-written rho_a (cache hits), which keeps
-    // this stage at two register arrays.
-    float2 div[E];
+    // formed afterwards from the just-written rho_a (cache hits), and the
+    // divergence accumulates in this thread's slots of shared memory
+    // (dsm[j * blockDim + thread], after the exchange regions), which keeps
+    // this stage at one register array.
+    float2* dsm = ex + Q.R * Q.ex_stride;
+    const int nthr = blockDim.x;
     float2 cp[EXTRA ? E : 1];
     if constexpr (EXTRA) {
       if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
     }
     for (int a = 0; a < D; ++a) {
+      if (threadIdx.x < 32) prefetch_block<STAGE>(Q, blockIdx.x * (blockDim.x / P), threadIdx.x, a + 1);
       c.c2r(Q.S[a], v);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         const int n = t + P * j;
         const long long i = c.rbase + n;
         const float2 du = v[j];
-        const float2 d0 = (a == 0) ? make_float2(0.f, 0.f) : div[j];
-        div[j] = make_float2(__fadd_rn(d0.x, du.x), __fadd_rn(d0.y, du.y));
+        float2* dp = dsm + j * nthr + threadIdx.x;
+        const float2 d0 = (a == 0) ? make_float2(0.f, 0.f) : *dp;
+        *dp = make_float2(__fadd_rn(d0.x, du.x), __fadd_rn(d0.y, du.y));
         if (!c.ok) continue;
         const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
         const float2 pm = c.pml2(Q.pml[a], a, n);
@@ -464,15 +469,16 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       const long long i = c.rbase + t + P * j;
+      const float2 dv = dsm[j * nthr + threadIdx.x];
       if (c.ok) {
         const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
-        div[j] = make_float2(__fmul_rn(r0v.x, div[j].x), __fmul_rn(r0v.y, div[j].y));
+        v[j] = make_float2(__fmul_rn(r0v.x, dv.x), __fmul_rn(r0v.y, dv.y));
       } else {
-        div[j] = make_float2(0.f, 0.f);
+        v[j] = make_float2(0.f, 0.f);
       }
     }
-    c.r2c(div, Q.S[0]);
-    if constexpr (EXTRA) record_unstaggered(c, Q, div);
+    c.r2c(v, Q.S[0]);
+    if constexpr (EXTRA) record_unstaggered(c, Q, v);
     // the new density sum (components added in order), kept for the equation
     // of state and the next step's nonlinear factor, and its spectrum
 #pragma unroll
