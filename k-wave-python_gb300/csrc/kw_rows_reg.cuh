@@ -207,8 +207,15 @@ __device__ __forceinline__ void prefetch_block(const RowsParams& Q, int r0, int 
 // EXTRA: this launch has k-space corrected sources or records the velocity on
 // the pressure grid; without it those paths are compiled out, which keeps the
 // common launch at its smaller register budget.
+// Resident blocks per SM each stage is compiled for (register budget
+// 65536 / (128 * blocks)): velocity 72, power-law density 128, equation of
+// state 96, generic density 168, the rest 128.
+constexpr int kw_rows_min_blocks(int stage) {
+  return stage == ST_U ? 7 : stage == ST_RHO_PL ? 4 : stage == ST_EOS ? 5 : stage == ST_RHO ? 3 : 4;
+}
+
 template <int E, int P, int STAGE, bool EXTRA>
-__global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsParams Q) {
+__global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(const __grid_constant__ RowsParams Q) {
   constexpr int M = E * P;
   extern __shared__ float4 smem_f4[];
   float2* tw = reinterpret_cast<float2*>(smem_f4);
@@ -412,7 +419,9 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     // mass conservation with split density and power-law absorption
     // (kspace_solver.py:709-717, :498, :524).  The nonlinear factor
     // (2 sum_a rho_a + rho0) / rho0 uses the sum stored by the previous step,
-    // which is the same float sum of the same values.  Only the divergence
+    // which is the same float sum of the same values; it is folded with
+    // dt rho0 into one factor per pair (the reference multiplies the three in
+    // the order dt rho0 du nl, so results can differ in the last bit).  Only the divergence
     // stays in registers across the components; the new density sum is
     // formed afterwards from the just-written rho_a (cache hits), and the
     // divergence accumulates in this thread's slots of shared memory
@@ -420,6 +429,23 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
     // this stage at one register array.
     float2* dsm = ex + Q.R * Q.ex_stride;
     const int nthr = blockDim.x;
+    // w = dt rho0 (2 sum_a rho_a + rho0) / rho0 per pair, loaded and formed
+    // once for the three components (all loads issued together)
+    float2 w[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const long long i = c.rbase + t + P * j;
+      w[j] = make_float2(0.f, 0.f);
+      if (c.ok) {
+        const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
+        w[j] = make_float2(__fmul_rn(Q.dt, r0v.x), __fmul_rn(Q.dt, r0v.y));
+        if (Q.nonlin) {
+          const float2 sr = ld2(Q.rho_sum, i);
+          w[j] = make_float2(__fmul_rn(w[j].x, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.x), r0v.x), r0v.x)),
+                             __fmul_rn(w[j].y, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v.y), r0v.y)));
+        }
+      }
+    }
     float2 cp[EXTRA ? E : 1];
     if constexpr (EXTRA) {
       if (Q.srcp_on) c.c2r(Q.S[B_SRCP], cp);
@@ -436,16 +462,10 @@ __global__ void __launch_bounds__(128) k_rows_v2(const __grid_constant__ RowsPar
         const float2 d0 = (a == 0) ? make_float2(0.f, 0.f) : *dp;
         *dp = make_float2(__fadd_rn(d0.x, du.x), __fadd_rn(d0.y, du.y));
         if (!c.ok) continue;
-        const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
         const float2 pm = c.pml2(Q.pml[a], a, n);
         const float2 ro = ld2(Q.rho[a], i);
-        float tx = __fmul_rn(__fmul_rn(Q.dt, r0v.x), du.x);
-        float ty = __fmul_rn(__fmul_rn(Q.dt, r0v.y), du.y);
-        if (Q.nonlin) {
-          const float2 sr = ld2(Q.rho_sum, i);
-          tx = __fmul_rn(tx, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.x), r0v.x), r0v.x));
-          ty = __fmul_rn(ty, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v.y), r0v.y));
-        }
+        const float tx = __fmul_rn(w[j].x, du.x);
+        const float ty = __fmul_rn(w[j].y, du.y);
         v[j] = make_float2(__fmul_rn(pm.x, __fsub_rn(__fmul_rn(pm.x, ro.x), tx)),
                            __fmul_rn(pm.y, __fsub_rn(__fmul_rn(pm.y, ro.y), ty)));
       }
