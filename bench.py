@@ -180,6 +180,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes (read + write) per launch of each kernel class, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on the 256^3 headline
+# workload; profiles/timeloop_256cubed_kernels.md has the capture and command.
+NCU_TRAFFIC_256 = {"rows_rho": 914.7e6, "rows_u": 957.6e6, "rows_eos": 566.2e6, "axis_ops": 267.7e6,
+                   "axis_plain": 263.4e6}
+
+
 def launch_bytes(S):
     """Algorithmic bytes per launch of each kernel class for a set-up problem:
     every array a launch must read or write, counted once (fp32 reals, complex64
@@ -370,7 +377,10 @@ def run_gb300(args):
                    "l2": "inputs larger than L2 (state + medium ~1.1 GB per step)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
+                     "frac": achieved / peak,
+                     "traffic": NCU_TRAFFIC_256.get(names[dom]) if n == 256 else None,
+                     "traffic_source": "ncu dram bytes per launch, profiles/timeloop_256cubed_kernels.md",
+                     "peak_source": peak_kind},
         "step_roofline": {"model_bytes_per_cell_step": A_MODEL_BYTES_PER_CELL_STEP, "achieved": step_gbs,
                           "peak": peak, "frac": step_gbs / peak, "unit": "GB/s"},
         "kernels": kernels,
