@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
   float2* ex = stages + (size_t)NST * N * T;             // T * RS
   float2* tw = ex + (size_t)T * RS;                      // N
   // x-axis tables (k, op_grad, op_div, unstag) in shared memory when they fit
-  constexpr bool kTablesInSmem = N <= 512;
+  constexpr bool kTablesInSmem = N <= 512 && KIND != KK_PLAIN;
   constexpr int NT = kTablesInSmem ? N : 0;
   float* k0t = reinterpret_cast<float*>(tw + N);
   float2* f0t = reinterpret_cast<float2*>(k0t + NT);
@@ -445,19 +445,23 @@ inline bool kw_tma_narrow(int n, int axis, int kind) { return n <= 256; }
 inline int kw_tma_tile_cols(int n, int P, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 128 / P : 256 / P; }
 inline int kw_tma_per_sm(int n, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 3 : 1; }
 
+// Stages of the TMA ring (a third stage measured no faster for the plain passes).
+inline int kw_tma_stages(int n, int kind) { return 2; }
+#define KW_NST_S 2
+
 inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
-  const int T = kw_tma_tile_cols(n, P, axis, kind), RS = n + E + 1;
-  const size_t nt = n <= 512 ? (size_t)n : 0;
-  return sizeof(float2) * ((size_t)2 * n * T + (size_t)T * RS + n + 3 * nt) + sizeof(float) * nt +
-         2 * 2 * sizeof(uint64_t) + 16;
+  const int T = kw_tma_tile_cols(n, P, axis, kind), RS = n + E + 1, NST = kw_tma_stages(n, kind);
+  const size_t nt = (n <= 512 && kind != KK_PLAIN) ? (size_t)n : 0;
+  return sizeof(float2) * ((size_t)NST * n * T + (size_t)T * RS + n + 3 * nt) + sizeof(float) * nt +
+         2 * NST * sizeof(uint64_t) + 16;
 }
 
 // Instantiation table: (E, P, stages, CTAs per SM, tile columns) per length.
 #define KW_TMA_SWITCH(n, narrow_, CALL)      \
   switch (n) {                               \
-    case 64: return CALL(16, 4, 2, 3, 32);   \
-    case 128: return CALL(16, 8, 2, 3, 16);  \
-    case 256: return CALL(16, 16, 2, 3, 8);  \
+    case 64: return CALL(16, 4, KW_NST_S, 3, 32);   \
+    case 128: return CALL(16, 8, KW_NST_S, 3, 16);  \
+    case 256: return CALL(16, 16, KW_NST_S, 3, 8);  \
     case 512: return CALL(32, 16, 2, 1, 16); \
     case 1024: return CALL(32, 32, 2, 1, 8); \
     default: return cudaErrorInvalidValue;   \

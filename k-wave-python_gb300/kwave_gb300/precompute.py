@@ -24,6 +24,7 @@ as the reference computes it (:705, :796).
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -98,13 +99,16 @@ def expand_to_grid(val, shape, name):
     """kspace_solver.py:48-57; returns a Python float for scalars."""
     if val is None:
         raise ValueError(f"Missing required parameter: {name}")
-    arr = np.asarray(val, dtype=np.float64).ravel()
+    raw = np.asarray(val)
     n = int(np.prod(shape))
-    if arr.size == 1:
-        return float(arr[0])
-    if arr.size == n:
-        return arr.reshape(shape)
-    raise ValueError(f"{name} size {arr.size} incompatible with grid size {n}")
+    if raw.size == 1:
+        return float(np.asarray(raw, dtype=np.float64).ravel()[0])
+    if raw.size == n:
+        if raw.dtype == np.float64:
+            return raw.reshape(shape)
+        src = raw.reshape(shape)
+        return _par_fill(tuple(shape), lambda i, j: src[i:j], dtype=np.float64)
+    raise ValueError(f"{name} size {raw.size} incompatible with grid size {n}")
 
 
 def pml_profile(N, dx, dt, c, size, alpha, staggered):
@@ -179,6 +183,57 @@ def smoothing_tables(shape):
         idx = (np.arange(m) + m // 2) % m  # ifftshift
         coords.append((xx[idx] ** 2).astype(np.float32))
     return np.abs(win_lin).astype(np.float32), float(radius), coords
+
+
+# ---------------------------------------------------------------------------
+# slab-parallel evaluation of the per-cell set-up arrays
+# ---------------------------------------------------------------------------
+
+_POOL = None
+
+
+def _pool():
+    """Thread pool for the per-cell set-up arrays (NumPy releases the GIL on
+    large array operations, so slabs along axis 0 run in parallel)."""
+    global _POOL
+    if _POOL is None:
+        from concurrent.futures import ThreadPoolExecutor
+
+        _POOL = ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+    return _POOL
+
+
+def _par_fill(shape, fn, dtype=np.float32):
+    """Array of ``shape`` and ``dtype`` (float32 by default) whose slabs [a, b)
+    along axis 0 are ``fn(a, b)`` (each evaluated in FP64 and cast), computed
+    in parallel."""
+    out = np.empty(shape, dtype=dtype)
+    n0 = shape[0]
+    nslab = min(n0, 4 * (_pool()._max_workers))
+    bounds = [(i * n0 // nslab, (i + 1) * n0 // nslab) for i in range(nslab)]
+
+    def run(ab):
+        a, b = ab
+        if b > a:
+            out[a:b] = fn(a, b)
+
+    list(_pool().map(run, bounds))
+    return out
+
+
+def _stagger_slab(arr, axis, a, b):
+    """``stagger(arr, axis)[a:b]`` computed from the slab (and, along axis 0,
+    the next plane)."""
+    if axis != 0:
+        return stagger(arr[a:b], axis)
+    n0 = arr.shape[0]
+    hi_end = min(b + 1, n0)
+    lo = arr[a:min(b, n0 - 1)]
+    hi = arr[a + 1:hi_end]
+    avg = 0.5 * (lo + hi)
+    if b == n0:
+        return np.concatenate([avg, arr[n0 - 1:n0]], axis=0)
+    return avg
 
 
 def stagger(arr, axis):
@@ -306,12 +361,18 @@ def build_setup(prob) -> Setup:
     c0 = expand_to_grid(prob.get("sound_speed"), shape, "sound_speed")
     dens = prob.get("density")
     rho0 = expand_to_grid(dens if dens is not None else 1000.0, shape, "density")
+    def f32(a):
+        if isinstance(a, float):
+            return a
+        arr = np.asarray(a)
+        return _par_fill(arr.shape, lambda i, j: arr[i:j])
+
+    c0_32 = f32(c0)
     # c_ref = max(c0) of the FP32-cast medium (kspace_solver.py:228-231)
-    c_ref = float(np.max(np.asarray(c0, dtype=np.float32)))
+    c_ref = float(np.float32(c0_32)) if isinstance(c0_32, float) else float(np.max(c0_32))
     S = Setup(shape=shape, spacing=spacing, dt=dt, Nt=Nt, ndim=ndim, c_ref=c_ref,
               use_sg=bool(prob.get("use_sg", True)), use_kspace=bool(prob.get("use_kspace", True)))
-    f32 = lambda a: a if isinstance(a, float) else np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
-    S.fields["c0"] = f32(c0)
+    S.fields["c0"] = c0_32
     S.fields["rho0"] = f32(rho0)
 
     # --- sensor (kspace_solver.py:243-361) ---
@@ -393,13 +454,16 @@ def build_setup(prob) -> Setup:
             S.absorb_mode = 0
         elif stokes:
             S.absorb_mode = 2
-            S.fields["tau"] = _fv(-2 * a_np * (c0 if isinstance(c0, float) else np.asarray(c0)))
+            S.fields["tau"] = _cell_field(shape, lambda sl: -2 * _sl(a_np, sl) * _sl(c0, sl), a_np, c0)
         else:
             S.absorb_mode = 1
-            S.fields["tau"] = _fv(-2 * a_np * (np.power(c0, y - 1) if not isinstance(c0, float) else c0 ** (y - 1)))
+            S.fields["tau"] = _cell_field(
+                shape, lambda sl: -2 * _sl(a_np, sl) * _pow(_sl(c0, sl), y - 1), a_np, c0)
             if mode not in ("no_absorption", "no_dispersion"):
                 S.dispersion = 1
-                S.fields["eta"] = _fv(2 * a_np * (np.power(c0, y) if not isinstance(c0, float) else c0 ** y) * math.tan(math.pi * y / 2))
+                tn = math.tan(math.pi * y / 2)
+                S.fields["eta"] = _cell_field(
+                    shape, lambda sl: 2 * _sl(a_np, sl) * _pow(_sl(c0, sl), y) * tn, a_np, c0)
     B = prob.get("BonA", 0)
     if _enabled(B):
         S.nonlinear = 1
@@ -407,11 +471,12 @@ def build_setup(prob) -> Setup:
 
     # --- dt / rho0 on the staggered grids (kspace_solver.py:655-666) ---
     for a in range(ndim):
-        if isinstance(rho0, float) or not S.use_sg:
-            r = rho0
+        if isinstance(rho0, float):
+            S.fields[f"dtrsg{a}"] = dt / rho0
+        elif not S.use_sg:
+            S.fields[f"dtrsg{a}"] = _par_fill(shape, lambda i, j: dt / rho0[i:j])
         else:
-            r = stagger(rho0, a)
-        S.fields[f"dtrsg{a}"] = (dt / r) if isinstance(r, float) else np.ascontiguousarray(dt / r, dtype=np.float32)
+            S.fields[f"dtrsg{a}"] = _par_fill(shape, lambda i, j, a=a: dt / _stagger_slab(rho0, a, i, j))
 
     # --- sources (kspace_solver.py:552-645) ---
     S.sources = _build_sources(prob, shape, spacing, dt, c0, ndim)
@@ -425,9 +490,26 @@ def build_setup(prob) -> Setup:
         if prob.get("smooth_p0", True) and ndim >= 2:
             # smoothed on the device before the first step (kwave/utils/filters.py:549-615)
             S.smooth = smoothing_tables(shape)
-        S.fields["p0"] = np.ascontiguousarray(p0, dtype=np.float32)
+        S.fields["p0"] = _par_fill(tuple(shape), lambda i, j: p0[i:j])
         S.has_p0 = True
     return S
+
+
+def _sl(x, sl):
+    """Slab of a grid array, or the scalar itself."""
+    return x if np.ndim(x) == 0 else x[sl]
+
+
+def _pow(x, e):
+    return x ** e if np.ndim(x) == 0 else np.power(x, e)
+
+
+def _cell_field(shape, fn, *inputs):
+    """Python float when every input is a scalar, else the float32 grid of
+    fn(slab) evaluated slab-parallel along axis 0."""
+    if all(np.ndim(x) == 0 for x in inputs):
+        return float(fn(slice(None)))
+    return _par_fill(tuple(shape), lambda i, j: np.broadcast_to(fn(slice(i, j)), (j - i,) + tuple(shape[1:])))
 
 
 def _fv(x):
