@@ -125,6 +125,9 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
   }
   const int per_sm = kw_tma_per_sm(n, axis, kind);
   const int grid = W.nunits < nsm * per_sm ? W.nunits : nsm * per_sm;
+  W.st_tile = grid % W.ntile;
+  W.st_outer = (grid / W.ntile) % W.nouter;
+  W.st_b = grid / W.ntile / W.nouter;
   const size_t smem = kw_tma_smem(n, E, P, axis, kind);
   const TmaMaps& maps = tp->maps[axis];
   switch (kind) {

@@ -46,6 +46,32 @@ struct TmaWork {
   int nitems;  // items per unit
   int inp[KW_MAX_JOBS];  // operator mode: distinct input buffers in job order
   int* err;    // device error word (set on a wait timeout)
+  // the grid stride gridDim.x as (buffer, outer, tile) digits, for the
+  // division-free walk over units (UnitPos)
+  int st_tile, st_outer, st_b;
+};
+
+// Position (b, outer, tile) of unit u = b * nouter * ntile + outer * ntile +
+// tile, advanced by the grid stride without divisions.
+struct UnitPos {
+  int u, tile, outer, b;
+  __device__ __forceinline__ void init(int u0, const TmaWork& W) {
+    u = u0;
+    tile = u0 % W.ntile;
+    const int rest = u0 / W.ntile;
+    outer = rest % W.nouter;
+    b = rest / W.nouter;
+  }
+  __device__ __forceinline__ void next(const TmaWork& W) {
+    u += gridDim.x;
+    tile += W.st_tile;
+    int c = tile >= W.ntile;
+    if (c) tile -= W.ntile;
+    outer += W.st_outer + c;
+    c = outer >= W.nouter;
+    if (c) outer -= W.nouter;
+    b += W.st_b + c;
+  }
 };
 
 namespace kwtmak {
@@ -179,7 +205,7 @@ __device__ __forceinline__ float2 col_factor(const AxisParams& A, const AxisJob&
 // Inverse transform of y (frequency layout) and store of column cc to `out`.
 template <int E, int P, class Sync>
 __device__ __forceinline__ void rev_store(float2 (&y)[E], int t, float2* exr, const float2* tw, Sync sync, bool act,
-                                          float2* out, long long base, long long xs) {
+                                          float2* out, uint32_t base, uint32_t xs) {
   kwreg::Reg<E, P>::rev(y, t, exr, 1, tw, sync);
   if (act) {
 #pragma unroll
@@ -237,11 +263,9 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
     if (lane == 0) {
       uint32_t it = 0;
       bool ok = true;
-      for (int u = blockIdx.x; u < W.nunits && ok; u += gridDim.x) {
-        const int tile = u % W.ntile;
-        const int rest = u / W.ntile;
-        const int outer = rest % W.nouter;
-        const int b = rest / W.nouter;
+      UnitPos up;
+      for (up.init(blockIdx.x, W); up.u < W.nunits && ok; up.next(W)) {
+        const int tile = up.tile, outer = up.outer, b = up.b;
         for (int q = 0; q < W.nitems; ++q, ++it) {
           const int buf = OPS ? W.inp[q] : A.plain[b];
           const uint32_t s = it % NST, k = it / NST;
@@ -268,15 +292,14 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
     // per-tile operator cache (KK_DIV: kappa / N; KK_NAB: log2 |k|^2, -inf at k = 0)
     constexpr int NC = (KIND == KK_DIV || KIND == KK_NAB) ? E : 1;
     float kc[NC];
-    for (int u = blockIdx.x; u < W.nunits && !aborted; u += gridDim.x) {
-      const int tile = u % W.ntile;
-      const int rest = u / W.ntile;
-      const int outer = rest % W.nouter;
-      const int b = rest / W.nouter;
+    UnitPos up;
+    for (up.init(blockIdx.x, W); up.u < W.nunits && !aborted; up.next(W)) {
+      const int tile = up.tile, outer = up.outer, b = up.b;
       const int c0 = tile * T;
       const bool act = cc < A.ncols - c0;
-      const long long base = (long long)outer * A.os + c0 + cc;
-      const long long xs = A.xs;
+      // 32-bit element offsets (the host uses this pass only for spectra below 2^31 elements)
+      const uint32_t base = (uint32_t)outer * (uint32_t)A.os + (uint32_t)(c0 + cc);
+      const uint32_t xs = (uint32_t)A.xs;
       ColK g;
       if constexpr (OPS) g = col_geometry(A, act ? c0 + cc : c0);
       const bool on = OPS && act && g.valid;

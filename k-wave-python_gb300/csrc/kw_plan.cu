@@ -505,7 +505,9 @@ int32_t kw_plan_finalize(kw_plan* p) {
   if (!p->generic_only) {
     const char* env = getenv("KWAVE_GB300_NO_TMA");
     const bool no_tma = env && env[0] == '1';
-    for (int a = 0; a < D - 1 && !no_tma; ++a) {
+    // the TMA pass indexes a spectrum with 32-bit element offsets
+    const bool fits32 = (long long)p->spec_elems < (1LL << 31);
+    for (int a = 0; a < D - 1 && !no_tma && fits32; ++a) {
       if (!kw_tma_supported(p->N[a])) continue;
       if (!p->tma) p->tma = kw_tma_plan_create();
       int E, Pt;
