@@ -532,7 +532,8 @@ int32_t kw_plan_finalize(kw_plan* p) {
       if (p->axis_reg[a]) CK(kw_axis_reg_attr(p->N[a]));
     }
     if (p->even) {
-      p->rows_reg = kw_reg_shape(p->Mfft, &p->rows_regE, &p->rows_regP);
+      // the register row kernels index pairs with 32 bits
+      p->rows_reg = p->ntot < (1LL << 32) && kw_reg_shape(p->Mfft, &p->rows_regE, &p->rows_regP);
       if (p->rows_reg) {
         p->rows_R = 128 / p->rows_regP;
         const int target = p->rows_regP == 4 ? 4 : (p->rows_regP == 8 ? 8 : 0);

@@ -18,9 +18,10 @@
 
 namespace kwrows {
 
-__device__ __forceinline__ float2 ld2(const float* p, long long i) { return reinterpret_cast<const float2*>(p)[i]; }
-__device__ __forceinline__ void st2(float* p, long long i, float2 v) { reinterpret_cast<float2*>(p)[i] = v; }
-__device__ __forceinline__ float2 fld2(const float* p, float s, long long i) {
+// pair indices are 32-bit: the host uses these kernels only for grids below 2^32 cells
+__device__ __forceinline__ float2 ld2(const float* p, uint32_t i) { return reinterpret_cast<const float2*>(p)[i]; }
+__device__ __forceinline__ void st2(float* p, uint32_t i, float2 v) { reinterpret_cast<float2*>(p)[i] = v; }
+__device__ __forceinline__ float2 fld2(const float* p, float s, uint32_t i) {
   return p ? ld2(p, i) : make_float2(s, s);
 }
 
@@ -33,11 +34,12 @@ struct RowCtx {
   float2* exr;      // this row's exchange region
   int row, t, grow;
   bool ok;          // row < nrows
-  long long rbase;  // float2 index of the row's first pair
+  uint32_t rbase;   // float2 index of the row's first pair
+  int gx, gy;       // the row's x and (3-D) y index
 
   // half-spectrum row -> register pairs (unnormalised: L * x)
   __device__ __forceinline__ void c2r(const float2* S, float2 (&v)[E]) const {
-    const float2* sr = S + (long long)(ok ? grow : 0) * Q.Hp;
+    const float2* sr = S + (uint32_t)(ok ? grow : 0) * (uint32_t)Q.Hp;
 #pragma unroll
     for (int m = 0; m < E / P; ++m)
 #pragma unroll
@@ -67,7 +69,7 @@ struct RowCtx {
       for (int k2 = 0; k2 < P; ++k2) exr[t + P * m + E * k2] = v[m * P + k2];
     __syncwarp();
     if (ok) {
-      float2* so = S + (long long)grow * Q.Hp;
+      float2* so = S + (uint32_t)grow * (uint32_t)Q.Hp;
       for (int k = t; k <= M; k += P) {
         const float2 zk = exr[k == M ? 0 : k];
         const float2 zc = cconj(exr[k == 0 ? 0 : M - k]);
@@ -83,7 +85,7 @@ struct RowCtx {
   // PML factors of the two reals of pair n along `axis`
   __device__ __forceinline__ float2 pml2(const float* tab, int axis, int n) const {
     if (axis == Q.ndim - 1) return ld2(tab, n);
-    const int idx = (axis == 0) ? (Q.ndim == 3 ? grow / Q.N1 : grow) : grow % Q.N1;
+    const int idx = (axis == 0) ? gx : gy;
     const float s = tab[idx];
     return make_float2(s, s);
   }
@@ -230,7 +232,9 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
   const int R = blockDim.x / P;
   const int grow = blockIdx.x * R + row;
   using namespace kwrows;
-  RowCtx<E, P> c{Q, tw, twp, ex + row * Q.ex_stride, row, t, grow, grow < Q.nrows, (long long)grow * M};
+  RowCtx<E, P> c{Q, tw, twp, ex + row * Q.ex_stride, row, t, grow, grow < Q.nrows, (uint32_t)grow * (uint32_t)M};
+  c.gx = Q.ndim == 3 ? grow / Q.N1 : grow;
+  c.gy = Q.ndim == 3 ? grow - c.gx * Q.N1 : 0;
   const int D = Q.ndim;
   float2 v[E];
 
@@ -238,7 +242,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
     // t = 0 with p0: p = p0, rho_i = p0 / (c0^2 D) (kspace_solver.py:729-733)
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
+      const uint32_t i = c.rbase + t + P * j;
       float2 pv = make_float2(0.f, 0.f);
       if (c.ok) {
         pv = ld2(Q.p0, i);
@@ -273,7 +277,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         const int n = t + P * j;
-        const long long i = c.rbase + n;
+        const uint32_t i = c.rbase + n;
         if (!c.ok) continue;
         const float2 g = v[j];
         const float2 dtr = fld2(Q.dtrsg[a], Q.dtrsg_s[a], i);
@@ -316,7 +320,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
       div[j] = make_float2(0.f, 0.f);
       rs[j] = make_float2(0.f, 0.f);
       if (Q.nonlin && c.ok) {
-        const long long i = c.rbase + t + P * j;
+        const uint32_t i = c.rbase + t + P * j;
         const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
         float2 sr = ld2(Q.rho[0], i);
         for (int a = 1; a < D; ++a) {
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         const int n = t + P * j;
-        const long long i = c.rbase + n;
+        const uint32_t i = c.rbase + n;
         const float2 du = v[j];
         div[j] = make_float2(__fadd_rn(div[j].x, du.x), __fadd_rn(div[j].y, du.y));
         if (!c.ok) continue;
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
       // power law: transform rho0 * div and the density sum (kspace_solver.py:498, :524)
 #pragma unroll
       for (int j = 0; j < E; ++j) {
-        const long long i = c.rbase + t + P * j;
+        const uint32_t i = c.rbase + t + P * j;
         if (c.ok) {
           st2(Q.rho_sum, i, rs[j]);
           const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
@@ -388,7 +392,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
     // equation of state without fractional Laplacians (kspace_solver.py:719-723)
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
+      const uint32_t i = c.rbase + t + P * j;
       float2 pv = make_float2(0.f, 0.f);
       if (c.ok) {
         const float2 cc = fld2(Q.c0, Q.c0_s, i);
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
     float2 w[E];
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
+      const uint32_t i = c.rbase + t + P * j;
       w[j] = make_float2(0.f, 0.f);
       if (c.ok) {
         const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
@@ -456,7 +460,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         const int n = t + P * j;
-        const long long i = c.rbase + n;
+        const uint32_t i = c.rbase + n;
         const float2 du = v[j];
         float2* dp = dsm + j * nthr + threadIdx.x;
         const float2 d0 = (a == 0) ? make_float2(0.f, 0.f) : *dp;
@@ -488,7 +492,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
     // rho0 * div -> spectrum 0
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
+      const uint32_t i = c.rbase + t + P * j;
       const float2 dv = dsm[j * nthr + threadIdx.x];
       if (c.ok) {
         const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
     // of state and the next step's nonlinear factor, and its spectrum
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      const long long i = c.rbase + t + P * j;
+      const uint32_t i = c.rbase + t + P * j;
       float2 rs = make_float2(0.f, 0.f);
       if (c.ok) {
         rs = ld2(Q.rho[0], i);
@@ -562,7 +566,7 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
   if (Q.disp) c.c2r(Q.S[1], w);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    const long long i = c.rbase + t + P * j;
+    const uint32_t i = c.rbase + t + P * j;
     float2 pv = make_float2(0.f, 0.f);
     if (c.ok) {
       const float2 rsum = ld2(Q.rho_sum, i);
