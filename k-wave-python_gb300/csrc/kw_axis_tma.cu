@@ -139,6 +139,8 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
   }
 }
 
+int* kw_device_error_ptr() { return device_error_ptr(); }
+
 int kw_device_error_take() {
   int v = 0, z = 0;
   if (cudaMemcpyFromSymbol(&v, g_kw_device_error, sizeof(int)) != cudaSuccess) return -1;

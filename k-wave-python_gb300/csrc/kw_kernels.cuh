@@ -184,6 +184,11 @@ __global__ void k_absmax(const float* __restrict__ x, long long n, unsigned int*
 __global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out);
 // Returns and clears the device error word (nonzero: a bounded device wait timed out).
 int kw_device_error_take();
+// Device address of that word on the current device (nullptr on failure).
+int* kw_device_error_ptr();
+// Velocity stage fed by bulk copies (kw_rows_tma.cu), power-of-two row lengths.
+cudaError_t kw_rows_u_tma_attr(int m, int Hp, int ex_stride);
+cudaError_t kw_rows_u_tma_launch(int m, int nsm, cudaStream_t st, const RowsParams& Q, int* err);
 __global__ void k_rows(const __grid_constant__ RowsParams P);
 __global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
                                 const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out);

@@ -39,7 +39,11 @@ struct RowCtx {
 
   // half-spectrum row -> register pairs (unnormalised: L * x)
   __device__ __forceinline__ void c2r(const float2* S, float2 (&v)[E]) const {
-    const float2* sr = S + (uint32_t)(ok ? grow : 0) * (uint32_t)Q.Hp;
+    c2r_row(S + (uint32_t)(ok ? grow : 0) * (uint32_t)Q.Hp, v);
+  }
+
+  // the same from the row's H values at sr (global or shared memory)
+  __device__ __forceinline__ void c2r_row(const float2* sr, float2 (&v)[E]) const {
 #pragma unroll
     for (int m = 0; m < E / P; ++m)
 #pragma unroll
