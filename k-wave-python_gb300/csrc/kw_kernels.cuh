@@ -186,9 +186,10 @@ __global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out
 int kw_device_error_take();
 // Device address of that word on the current device (nullptr on failure).
 int* kw_device_error_ptr();
-// Velocity stage fed by bulk copies (kw_rows_tma.cu), power-of-two row lengths.
-cudaError_t kw_rows_u_tma_attr(int m, int Hp, int ex_stride);
-cudaError_t kw_rows_u_tma_launch(int m, int nsm, cudaStream_t st, const RowsParams& Q, int* err);
+// Velocity and power-law density stages fed by bulk copies (kw_rows_tma.cu),
+// power-of-two row lengths; stage is ST_U or ST_RHO_PL.
+cudaError_t kw_rows_tma_attr(int m, int Hp, int ex_stride);
+cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err);
 __global__ void k_rows(const __grid_constant__ RowsParams P);
 __global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
                                 const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out);

@@ -101,7 +101,7 @@ struct kw_plan {
   // persistent TMA axis passes
   void* tma = nullptr;
   bool tma_axis[3] = {false, false, false};
-  bool rows_u_tma = false;  // velocity stage through kw_rows_u_tma
+  bool rows_tma = false;  // velocity / power-law density stages through kw_rows_tma
   int nsm = 0;
   int rows_regP = 0, rows_regE = 0, rows_R = 0, rows_RS = 0;
   // p0 smoothing on the device
@@ -544,8 +544,8 @@ int32_t kw_plan_finalize(kw_plan* p) {
         CK(kw_rows_v2_attr(p->Mfft));
         const char* env = getenv("KWAVE_GB300_ROWS_TMA");
         if (!(env && env[0] == '0') && kw_device_error_ptr()) {
-          CK(kw_rows_u_tma_attr(p->Mfft, p->Hp, p->rows_RS));
-          p->rows_u_tma = true;
+          CK(kw_rows_tma_attr(p->Mfft, p->Hp, p->rows_RS));
+          p->rows_tma = true;
         }
       }
     }
@@ -670,8 +670,10 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
                                           (dsm ? (size_t)128 * p->rows_regE : 0));
     const int grid = (p->nrows + p->rows_R - 1) / p->rows_R;
     const bool extra = P.srcp_on || P.srcu_on[0] || P.srcu_on[1] || P.srcu_on[2] || P.rec_us;
-    if (stage == ST_U && !init && !extra && p->rows_u_tma)
-      CK(kw_rows_u_tma_launch(p->Mfft, p->nsm, st, P, kw_device_error_ptr()));
+    if (stage == ST_U && !init && !extra && p->rows_tma)
+      CK(kw_rows_tma_launch(p->Mfft, ST_U, p->nsm, st, P, kw_device_error_ptr()));
+    else if (stage == ST_RHO && dsm && !extra && p->rows_tma)
+      CK(kw_rows_tma_launch(p->Mfft, ST_RHO_PL, p->nsm, st, P, kw_device_error_ptr()));
     else
       CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
   } else {

@@ -1,27 +1,32 @@
-// Velocity stage fed by bulk copies (power-of-two row lengths).
+// Row stages fed by bulk copies (power-of-two row lengths).
 //
 // The register row kernel (kw_rows_reg.cuh) loads its inputs with ordinary
 // global loads; with its register budget a warp keeps only a few of them in
 // flight, so it waits on memory latency.  Here a persistent CTA streams, for
-// each block of R rows and each component a, the three arrays the velocity
-// update reads -- the rows of the gradient spectrum S_a, of u_a and of
-// dt/rho_sg_a -- into a ring of shared-memory slots with 1-D bulk copies
-// (cp.async.bulk, mbarrier completion), issued by one producer lane up to
-// NST copies ahead.  The 128 consumer threads (P per row) run the same
-// arithmetic as ST_U of the register kernel, reading the staged rows:
-//   u_a = pml_sg (pml_sg u_a - dt/rho_sg_a g_a)     (kspace_solver.py:703-707)
-// and write u_a and its spectrum to global memory.
+// each block of R rows, the arrays the stage reads -- spectrum rows and
+// field rows, each a contiguous range -- into a ring of shared-memory slots
+// with 1-D bulk copies (cp.async.bulk, mbarrier completion), issued by one
+// producer lane up to NST copies ahead.  The 128 consumer threads (P per row)
+// run the same arithmetic as the register kernel's stage, reading the staged
+// rows, and write their outputs to global memory.
 //
-// Used for the ordinary velocity update (not the t = 0 half step, not with
-// k-space corrected velocity sources or velocity-on-pressure-grid records:
-// those keep the register kernel).  All waits are bounded (2 s) and report
-// through the device error word, as in the TMA axis pass.
+//   ST_U      per component a: S_a, u_a, dt/rho_sg_a (if a grid)
+//             u_a = pml_sg (pml_sg u_a - dt/rho_sg_a g_a)   (kspace_solver.py:703-707)
+//   ST_RHO_PL rho0 (if a grid), sum rho (if nonlinear), then per component a:
+//             S_a, rho_a; split-density update with power-law absorption
+//             (kspace_solver.py:709-717, :498, :524), as the register
+//             kernel's ST_RHO_PL
+//
+// Launches with k-space corrected sources, velocity-on-pressure-grid records
+// or the t = 0 half step keep the register kernel.  All waits are bounded
+// (2 s) and report through the device error word, as in the TMA axis pass.
 #include "kw_rows_reg.cuh"
 #include "kw_tma.cuh"
 
 namespace {
 
 constexpr uint64_t kRowWaitNs = 2000000000ull;
+constexpr int kRowNst = 4;
 
 __device__ __forceinline__ bool consumers_any_rows(bool pred, int n) {
   uint32_t r;
@@ -36,10 +41,41 @@ __device__ __forceinline__ bool consumers_any_rows(bool pred, int n) {
   return r != 0;
 }
 
+// The idx-th array a block of rows of stage STAGE reads, in stream order:
+// base pointer and whether it is a spectrum (else a real field).  Arrays that
+// are absent (scalar medium values) are skipped by the caller.
+template <int STAGE>
+__device__ __forceinline__ const void* row_load(const RowsParams& Q, int idx, bool& spec) {
+  const int D = Q.ndim;
+  if constexpr (STAGE == ST_U) {
+    const int a = idx / 3, q = idx - 3 * a;
+    spec = q == 0;
+    return q == 0 ? (const void*)Q.S[a] : q == 1 ? (const void*)Q.u[a] : (const void*)Q.dtrsg[a];
+  } else {
+    if (idx == 0) {
+      spec = false;
+      return Q.rho0;
+    }
+    if (idx == 1) {
+      spec = false;
+      return Q.nonlin ? Q.rho_sum : nullptr;
+    }
+    const int a = (idx - 2) >> 1, q = (idx - 2) & 1;
+    spec = q == 0;
+    (void)D;
+    return q == 0 ? (const void*)Q.S[a] : (const void*)Q.rho[a];
+  }
+}
+
+template <int STAGE>
+__device__ __forceinline__ int row_nloads(const RowsParams& Q) {
+  return STAGE == ST_U ? 3 * Q.ndim : 2 + 2 * Q.ndim;
+}
+
 }  // namespace
 
-template <int E, int P, int NST>
-__global__ void __launch_bounds__(160, 2) k_rows_u_tma(const __grid_constant__ RowsParams Q, int* err) {
+template <int E, int P, int NST, int STAGE>
+__global__ void __launch_bounds__(160, 2) k_rows_tma(const __grid_constant__ RowsParams Q, int* err) {
   using namespace kwrows;
   constexpr int M = E * P, R = 128 / P, CT = 128;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -51,7 +87,11 @@ __global__ void __launch_bounds__(160, 2) k_rows_u_tma(const __grid_constant__ R
   float2* tw = reinterpret_cast<float2*>(slots + (size_t)NST * slot_bytes);
   float2* twp = tw + M;
   float2* ex = twp + (M + 1);
-  uint64_t* full = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(ex + R * Q.ex_stride) + 7) & ~uintptr_t(7));
+  // ST_RHO_PL: the new density sum accumulates in this thread's slots
+  // (rsm[j * 128 + thread]) instead of registers
+  float2* rsm = ex + R * Q.ex_stride;
+  constexpr int NRS = STAGE == ST_RHO_PL ? 128 * E : 0;
+  uint64_t* full = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(rsm + NRS) + 7) & ~uintptr_t(7));
   uint64_t* empty = full + NST;
   int* counters = reinterpret_cast<int*>(empty + NST);
 
@@ -69,8 +109,7 @@ __global__ void __launch_bounds__(160, 2) k_rows_u_tma(const __grid_constant__ R
   __syncthreads();
 
   const int nblk = (Q.nrows + R - 1) / R;
-  const bool has_dtr = Q.dtrsg[0] != nullptr;
-  const int per_a = has_dtr ? 3 : 2;
+  const int nload = row_nloads<STAGE>(Q);
 
   if (warp == CT / 32) {
     // ---------------- producer ----------------
@@ -79,26 +118,22 @@ __global__ void __launch_bounds__(160, 2) k_rows_u_tma(const __grid_constant__ R
       bool ok = true;
       for (int rb = blockIdx.x; rb < nblk && ok; rb += gridDim.x) {
         const int r0 = rb * R, nr = min(R, Q.nrows - r0);
-        for (int a = 0; a < D && ok; ++a) {
-          for (int q = 0; q < per_a; ++q, ++it) {
-            const uint32_t s = it % NST, k = it / NST;
-            if (k > 0 && !kwtma::mbar_wait(&empty[s], (k - 1) & 1, kRowWaitNs)) {
-              atomicExch(err, 3);
-              ok = false;
-              break;
-            }
-            const void* src;
-            uint32_t bytes;
-            if (q == 0) {
-              src = Q.S[a] + (size_t)r0 * Hp;
-              bytes = (uint32_t)nr * spec_row;
-            } else {
-              src = reinterpret_cast<const float2*>(q == 1 ? Q.u[a] : Q.dtrsg[a]) + (size_t)r0 * M;
-              bytes = (uint32_t)nr * fld_row;
-            }
-            kwtma::mbar_arrive_expect_tx(&full[s], bytes);
-            kwtma::bulk_load(slots + (size_t)s * slot_bytes, src, bytes, &full[s]);
+        for (int idx = 0; idx < nload; ++idx) {
+          bool spec;
+          const void* base = row_load<STAGE>(Q, idx, spec);
+          if (!base) continue;
+          const uint32_t s = it % NST, k = it / NST;
+          if (k > 0 && !kwtma::mbar_wait(&empty[s], (k - 1) & 1, kRowWaitNs)) {
+            atomicExch(err, 3);
+            ok = false;
+            break;
           }
+          const void* src = spec ? (const void*)(reinterpret_cast<const float2*>(base) + (size_t)r0 * Hp)
+                                 : (const void*)(reinterpret_cast<const float2*>(base) + (size_t)r0 * M);
+          const uint32_t bytes = (uint32_t)nr * (spec ? spec_row : fld_row);
+          kwtma::mbar_arrive_expect_tx(&full[s], bytes);
+          kwtma::bulk_load(slots + (size_t)s * slot_bytes, src, bytes, &full[s]);
+          ++it;
         }
       }
       counters[0] = (int)it;
@@ -108,85 +143,144 @@ __global__ void __launch_bounds__(160, 2) k_rows_u_tma(const __grid_constant__ R
     const int row = tid / P, t = tid % P;
     uint32_t it = 0;
     bool aborted = false;
+    // wait for item `i` (bounded; all consumers agree on a timeout)
+    auto wait_item = [&](uint32_t i) -> const float2* {
+      const uint32_t s = i % NST;
+      const bool got = kwtma::mbar_wait(&full[s], (i / NST) & 1, kRowWaitNs);
+      if (consumers_any_rows(!got, CT)) {
+        if (tid == 0) atomicExch(err, 4);
+        aborted = true;
+        return nullptr;
+      }
+      return reinterpret_cast<const float2*>(slots + (size_t)s * slot_bytes);
+    };
+    auto release = [&](uint32_t i) {
+      __syncwarp();
+      if (lane == 0) kwtma::mbar_arrive(&empty[i % NST]);
+    };
     float2 v[E];
     for (int rb = blockIdx.x; rb < nblk && !aborted; rb += gridDim.x) {
       const int grow = rb * R + row;
       RowCtx<E, P> c{Q, tw, twp, ex + row * Q.ex_stride, row, t, grow, grow < Q.nrows, (uint32_t)grow * (uint32_t)M};
       c.gx = D == 3 ? grow / Q.N1 : grow;
       c.gy = D == 3 ? grow - c.gx * Q.N1 : 0;
-      for (int a = 0; a < D && !aborted; ++a) {
-        // gradient spectrum rows -> register pairs
-        uint32_t s = it % NST;
-        bool got = kwtma::mbar_wait(&full[s], (it / NST) & 1, kRowWaitNs);
-        if (consumers_any_rows(!got, CT)) {
-          if (tid == 0) atomicExch(err, 4);
-          aborted = true;
-          break;
-        }
-        const float2* srow = reinterpret_cast<const float2*>(slots + (size_t)s * slot_bytes) + row * Hp;
-        // read the staged row into registers, then free the slot
-        {
+
+      if constexpr (STAGE == ST_U) {
+        const bool has_dtr = Q.dtrsg[0] != nullptr;
+        for (int a = 0; a < D; ++a) {
+          const float2* ss = wait_item(it);
+          if (!ss) break;
+          c.c2r_row(ss + row * Hp, v);  // reads the slot before its transform's first exchange
+          release(it);
+          ++it;
+          const float2* su = wait_item(it);
+          if (!su) break;
+          const float2* sd = su;
+          if (has_dtr) {
+            sd = wait_item(it + 1);
+            if (!sd) break;
+          }
+          const float2* urow = su + row * M;
+          const float2* drow = sd + row * M;
 #pragma unroll
-          for (int m = 0; m < E / P; ++m)
+          for (int j = 0; j < E; ++j) {
+            const int n = t + P * j;
+            if (!c.ok) continue;
+            const float2 g = v[j];
+            const float2 dtr = has_dtr ? drow[n] : make_float2(Q.dtrsg_s[a], Q.dtrsg_s[a]);
+            const float2 sg = c.pml2(Q.pmlsg[a], a, n);
+            const float2 u = urow[n];
+            v[j] = make_float2(__fmul_rn(sg.x, __fsub_rn(__fmul_rn(sg.x, u.x), __fmul_rn(dtr.x, g.x))),
+                               __fmul_rn(sg.y, __fsub_rn(__fmul_rn(sg.y, u.y), __fmul_rn(dtr.y, g.y))));
+          }
+          release(it);
+          if (has_dtr) release(it + 1);
+          it += has_dtr ? 2 : 1;
+          c.source(Q.src[3 + a], v);
+          if (c.ok) {
 #pragma unroll
-            for (int k2 = 0; k2 < P; ++k2) {
-              const int k = t + P * m + E * k2;
-              float2 z = make_float2(0.f, 0.f);
-              if (c.ok) {
-                const float2 xk = srow[k];
-                const float2 xc = cconj(srow[M - k]);
-                const float2 e = cadd(xk, xc);
-                const float2 o = kwreg::cmulf(csub(xk, xc), cconj(twp[k]));
-                z = make_float2(e.x - o.y, e.y + o.x);
-              }
-              v[m * P + k2] = cconj(z);
-            }
+            for (int j = 0; j < E; ++j) st2(Q.u[a], c.rbase + t + P * j, v[j]);
+          }
+          c.record(v, Q.rec[1 + a]);
+          c.r2c(v, Q.S[a]);
         }
-        __syncwarp();
-        if (lane == 0) kwtma::mbar_arrive(&empty[s]);
-        ++it;
-        kwreg::Reg<E, P>::rev(v, t, c.exr, 1, tw, [] __device__() { __syncwarp(); });
-#pragma unroll
-        for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
-        // u_a and dt/rho_sg_a rows
-        const uint32_t su = it % NST;
-        got = kwtma::mbar_wait(&full[su], (it / NST) & 1, kRowWaitNs);
-        uint32_t sd = su;
-        if (has_dtr) {
-          sd = (it + 1) % NST;
-          got = got && kwtma::mbar_wait(&full[sd], ((it + 1) / NST) & 1, kRowWaitNs);
+      } else {
+        // w = dt rho0 (2 sum rho + rho0) / rho0 per pair (nonlinear factor from
+        // the previous step's density sum), rho0 kept for rho0 * div
+        float2 w[E], r0v[E], div[E];
+        const float2* s0 = nullptr;
+        const float2* s1 = nullptr;
+        const uint32_t i0 = it;
+        if (Q.rho0) {
+          s0 = wait_item(it++);
+          if (!s0) break;
         }
-        if (consumers_any_rows(!got, CT)) {
-          if (tid == 0) atomicExch(err, 4);
-          aborted = true;
-          break;
+        if (Q.nonlin) {
+          s1 = wait_item(it++);
+          if (!s1) break;
         }
-        const float2* urow = reinterpret_cast<const float2*>(slots + (size_t)su * slot_bytes) + row * M;
-        const float2* drow = reinterpret_cast<const float2*>(slots + (size_t)sd * slot_bytes) + row * M;
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int n = t + P * j;
-          if (!c.ok) continue;
-          const float2 g = v[j];
-          const float2 dtr = has_dtr ? drow[n] : make_float2(Q.dtrsg_s[a], Q.dtrsg_s[a]);
-          const float2 sg = c.pml2(Q.pmlsg[a], a, n);
-          const float2 u = urow[n];
-          v[j] = make_float2(__fmul_rn(sg.x, __fsub_rn(__fmul_rn(sg.x, u.x), __fmul_rn(dtr.x, g.x))),
-                             __fmul_rn(sg.y, __fsub_rn(__fmul_rn(sg.y, u.y), __fmul_rn(dtr.y, g.y))));
+          r0v[j] = s0 ? s0[row * M + n] : make_float2(Q.rho0_s, Q.rho0_s);
+          w[j] = make_float2(__fmul_rn(Q.dt, r0v[j].x), __fmul_rn(Q.dt, r0v[j].y));
+          if (Q.nonlin) {
+            const float2 sr = s1[row * M + n];
+            w[j] = make_float2(__fmul_rn(w[j].x, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.x), r0v[j].x), r0v[j].x)),
+                               __fmul_rn(w[j].y, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v[j].y), r0v[j].y)));
+          }
         }
-        __syncwarp();
-        if (lane == 0) {
-          kwtma::mbar_arrive(&empty[su]);
-          if (has_dtr) kwtma::mbar_arrive(&empty[sd]);
-        }
-        it += has_dtr ? 2 : 1;
-        c.source(Q.src[3 + a], v);
-        if (c.ok) {
+        for (uint32_t i = i0; i < it; ++i) release(i);
+        for (int a = 0; a < D; ++a) {
+          const float2* ss = wait_item(it);
+          if (!ss) break;
+          c.c2r_row(ss + row * Hp, v);
+          release(it);
+          ++it;
+          const float2* sr = wait_item(it);
+          if (!sr) break;
+          const float2* rrow = sr + row * M;
 #pragma unroll
-          for (int j = 0; j < E; ++j) st2(Q.u[a], c.rbase + t + P * j, v[j]);
+          for (int j = 0; j < E; ++j) {
+            const int n = t + P * j;
+            const float2 du = v[j];
+            const float2 d0 = (a == 0) ? make_float2(0.f, 0.f) : div[j];
+            div[j] = make_float2(__fadd_rn(d0.x, du.x), __fadd_rn(d0.y, du.y));
+            if (!c.ok) continue;
+            const float2 pm = c.pml2(Q.pml[a], a, n);
+            const float2 ro = rrow[n];
+            const float tx = __fmul_rn(w[j].x, du.x);
+            const float ty = __fmul_rn(w[j].y, du.y);
+            v[j] = make_float2(__fmul_rn(pm.x, __fsub_rn(__fmul_rn(pm.x, ro.x), tx)),
+                               __fmul_rn(pm.y, __fsub_rn(__fmul_rn(pm.y, ro.y), ty)));
+          }
+          release(it);
+          ++it;
+          c.source(Q.src[a], v);
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            if (c.ok) st2(Q.rho[a], c.rbase + t + P * j, v[j]);
+            float2* rp = rsm + j * CT + tid;
+            const float2 r = (a == 0) ? v[j] : *rp;
+            *rp = (a == 0) ? r : make_float2(__fadd_rn(r.x, v[j].x), __fadd_rn(r.y, v[j].y));
+          }
         }
-        c.record(v, Q.rec[1 + a]);
-        c.r2c(v, Q.S[a]);
+        if (aborted) break;
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          if (c.ok) {
+            v[j] = make_float2(__fmul_rn(r0v[j].x, div[j].x), __fmul_rn(r0v[j].y, div[j].y));
+          } else {
+            v[j] = make_float2(0.f, 0.f);
+          }
+        }
+        c.r2c(v, Q.S[0]);
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          v[j] = rsm[j * CT + tid];
+          if (c.ok) st2(Q.rho_sum, c.rbase + t + P * j, v[j]);
+        }
+        if (Q.disp) c.r2c(v, Q.S[1]);
       }
     }
     if (tid == 0) counters[1] = (int)it;
@@ -201,16 +295,15 @@ __global__ void __launch_bounds__(160, 2) k_rows_u_tma(const __grid_constant__ R
   }
 }
 
-static constexpr int kRowNst = 4;
-
-static size_t rows_u_tma_smem(int M, int E, int P, int Hp, int ex_stride) {
+static size_t rows_tma_smem(int stage, int M, int E, int P, int Hp, int ex_stride) {
   const int R = 128 / P;
   const size_t spec_row = (size_t)Hp * 8, fld_row = (size_t)M * 8;
   const size_t slot = ((R * (spec_row > fld_row ? spec_row : fld_row)) + 127) & ~(size_t)127;
-  return kRowNst * slot + sizeof(float2) * (2 * (size_t)M + 1 + (size_t)R * ex_stride) + 8 + 2 * kRowNst * 8 + 16;
+  const size_t nrs = stage == ST_RHO_PL ? (size_t)128 * E : 0;
+  return kRowNst * slot + sizeof(float2) * (2 * (size_t)M + 1 + (size_t)R * ex_stride + nrs) + 8 + 2 * kRowNst * 8 + 16;
 }
 
-#define KW_RU_SWITCH(m, CALL)              \
+#define KW_RT_SWITCH(m, CALL)              \
   switch (m) {                             \
     case 64: return CALL(16, 4);           \
     case 128: return CALL(16, 8);          \
@@ -220,22 +313,36 @@ static size_t rows_u_tma_smem(int M, int E, int P, int Hp, int ex_stride) {
     default: return cudaErrorInvalidValue; \
   }
 
-cudaError_t kw_rows_u_tma_attr(int m, int Hp, int ex_stride) {
+template <int STAGE>
+static cudaError_t rows_tma_attr(int m, int Hp, int ex_stride) {
   int E, P;
   if (!kw_reg_shape(m, &E, &P)) return cudaErrorInvalidValue;
-  const int smem = (int)rows_u_tma_smem(m, E, P, Hp, ex_stride);
-#define KW_R(E_, P_) cudaFuncSetAttribute(k_rows_u_tma<E_, P_, kRowNst>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-  KW_RU_SWITCH(m, KW_R)
+  const int smem = (int)rows_tma_smem(STAGE, m, E, P, Hp, ex_stride);
+#define KW_R(E_, P_) \
+  cudaFuncSetAttribute(k_rows_tma<E_, P_, kRowNst, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+  KW_RT_SWITCH(m, KW_R)
 #undef KW_R
 }
 
-cudaError_t kw_rows_u_tma_launch(int m, int nsm, cudaStream_t st, const RowsParams& Q, int* err) {
+template <int STAGE>
+static cudaError_t rows_tma_launch(int m, int nsm, cudaStream_t st, const RowsParams& Q, int* err) {
   int E, P;
   if (!kw_reg_shape(m, &E, &P)) return cudaErrorInvalidValue;
   const int R = 128 / P, nblk = (Q.nrows + R - 1) / R;
   const int grid = nblk < 2 * nsm ? nblk : 2 * nsm;
-  const size_t smem = rows_u_tma_smem(m, E, P, Q.Hp, Q.ex_stride);
-#define KW_R(E_, P_) (k_rows_u_tma<E_, P_, kRowNst><<<grid, 160, smem, st>>>(Q, err), cudaGetLastError())
-  KW_RU_SWITCH(m, KW_R)
+  const size_t smem = rows_tma_smem(STAGE, m, E, P, Q.Hp, Q.ex_stride);
+#define KW_R(E_, P_) (k_rows_tma<E_, P_, kRowNst, STAGE><<<grid, 160, smem, st>>>(Q, err), cudaGetLastError())
+  KW_RT_SWITCH(m, KW_R)
 #undef KW_R
+}
+
+cudaError_t kw_rows_tma_attr(int m, int Hp, int ex_stride) {
+  cudaError_t e = rows_tma_attr<ST_U>(m, Hp, ex_stride);
+  return e == cudaSuccess ? rows_tma_attr<ST_RHO_PL>(m, Hp, ex_stride) : e;
+}
+
+cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err) {
+  if (stage == ST_U) return rows_tma_launch<ST_U>(m, nsm, st, Q, err);
+  if (stage == ST_RHO_PL) return rows_tma_launch<ST_RHO_PL>(m, nsm, st, Q, err);
+  return cudaErrorInvalidValue;
 }
