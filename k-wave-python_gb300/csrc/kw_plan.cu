@@ -674,6 +674,8 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
       CK(kw_rows_tma_launch(p->Mfft, ST_U, p->nsm, st, P, kw_device_error_ptr()));
     else if (stage == ST_RHO && dsm && !extra && p->rows_tma)
       CK(kw_rows_tma_launch(p->Mfft, ST_RHO_PL, p->nsm, st, P, kw_device_error_ptr()));
+    else if (stage == ST_EOS && p->rows_tma)
+      CK(kw_rows_tma_launch(p->Mfft, ST_EOS, p->nsm, st, P, kw_device_error_ptr()));
     else
       CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
   } else {

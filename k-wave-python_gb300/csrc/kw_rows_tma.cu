@@ -16,6 +16,9 @@
 //             S_a, rho_a; split-density update with power-law absorption
 //             (kspace_solver.py:709-717, :498, :524), as the register
 //             kernel's ST_RHO_PL
+//   ST_EOS    the two fractional-Laplacian spectra, sum rho, tau, eta, rho0,
+//             B/A, c0 (those that are grids); equation of state with
+//             absorption and dispersion (kspace_solver.py:719-723)
 //
 // Launches with k-space corrected sources, velocity-on-pressure-grid records
 // or the t = 0 half step keep the register kernel.  All waits are bounded
@@ -51,6 +54,18 @@ __device__ __forceinline__ const void* row_load(const RowsParams& Q, int idx, bo
     const int a = idx / 3, q = idx - 3 * a;
     spec = q == 0;
     return q == 0 ? (const void*)Q.S[a] : q == 1 ? (const void*)Q.u[a] : (const void*)Q.dtrsg[a];
+  } else if constexpr (STAGE == ST_EOS) {
+    spec = idx < 2;
+    switch (idx) {
+      case 0: return Q.S[0];
+      case 1: return Q.disp ? Q.S[1] : nullptr;
+      case 2: return Q.rho_sum;
+      case 3: return Q.tau;
+      case 4: return Q.disp ? Q.eta : nullptr;
+      case 5: return Q.nonlin ? Q.rho0 : nullptr;
+      case 6: return Q.nonlin ? Q.bona : nullptr;
+      default: return Q.c0;
+    }
   } else {
     if (idx == 0) {
       spec = false;
@@ -69,7 +84,7 @@ __device__ __forceinline__ const void* row_load(const RowsParams& Q, int idx, bo
 
 template <int STAGE>
 __device__ __forceinline__ int row_nloads(const RowsParams& Q) {
-  return STAGE == ST_U ? 3 * Q.ndim : 2 + 2 * Q.ndim;
+  return STAGE == ST_U ? 3 * Q.ndim : STAGE == ST_EOS ? 8 : 2 + 2 * Q.ndim;
 }
 
 }  // namespace
@@ -204,6 +219,88 @@ __global__ void __launch_bounds__(160, 2) k_rows_tma(const __grid_constant__ Row
           c.record(v, Q.rec[1 + a]);
           c.r2c(v, Q.S[a]);
         }
+      } else if constexpr (STAGE == ST_EOS) {
+        // p = c0^2 (sum rho + tau L1 - eta L2 + B/A (sum rho)^2 / (2 rho0)), the
+        // terms added in the register kernel's order; each field row is read
+        // once and its slot released before the next is waited for
+        float2 w[E], rsum[E];
+        const float2* sp = wait_item(it);
+        if (!sp) break;
+        c.c2r_row(sp + row * Hp, v);
+        release(it++);
+        if (Q.disp) {
+          sp = wait_item(it);
+          if (!sp) break;
+          c.c2r_row(sp + row * Hp, w);
+          release(it++);
+        }
+        sp = wait_item(it);
+        if (!sp) break;
+#pragma unroll
+        for (int j = 0; j < E; ++j) rsum[j] = sp[row * M + t + P * j];
+        release(it++);
+        const float2* sf = nullptr;
+        if (Q.tau) {
+          sf = wait_item(it);
+          if (!sf) break;
+        }
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const float2 tau = sf ? sf[row * M + t + P * j] : make_float2(Q.tau_s, Q.tau_s);
+          v[j] = make_float2(__fadd_rn(rsum[j].x, __fmul_rn(tau.x, v[j].x)), __fadd_rn(rsum[j].y, __fmul_rn(tau.y, v[j].y)));
+        }
+        if (sf) release(it++);
+        if (Q.disp) {
+          sf = nullptr;
+          if (Q.eta) {
+            sf = wait_item(it);
+            if (!sf) break;
+          }
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const float2 eta = sf ? sf[row * M + t + P * j] : make_float2(Q.eta_s, Q.eta_s);
+            v[j] = make_float2(__fsub_rn(v[j].x, __fmul_rn(eta.x, w[j].x)), __fsub_rn(v[j].y, __fmul_rn(eta.y, w[j].y)));
+          }
+          if (sf) release(it++);
+        }
+        if (Q.nonlin) {
+          const float2* sr0 = nullptr;
+          const float2* sb = nullptr;
+          const uint32_t i0 = it;
+          if (Q.rho0) {
+            sr0 = wait_item(it++);
+            if (!sr0) break;
+          }
+          if (Q.bona) {
+            sb = wait_item(it++);
+            if (!sb) break;
+          }
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int n = row * M + t + P * j;
+            const float2 r0v = sr0 ? sr0[n] : make_float2(Q.rho0_s, Q.rho0_s);
+            const float2 b = sb ? sb[n] : make_float2(Q.bona_s, Q.bona_s);
+            v[j] = make_float2(
+                __fadd_rn(v[j].x, __fdiv_rn(__fmul_rn(b.x, __fmul_rn(rsum[j].x, rsum[j].x)), __fmul_rn(2.f, r0v.x))),
+                __fadd_rn(v[j].y, __fdiv_rn(__fmul_rn(b.y, __fmul_rn(rsum[j].y, rsum[j].y)), __fmul_rn(2.f, r0v.y))));
+          }
+          for (uint32_t i = i0; i < it; ++i) release(i);
+        }
+        sf = nullptr;
+        if (Q.c0) {
+          sf = wait_item(it);
+          if (!sf) break;
+        }
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const float2 cc = sf ? sf[row * M + t + P * j] : make_float2(Q.c0_s, Q.c0_s);
+          v[j] = c.ok ? make_float2(__fmul_rn(__fmul_rn(cc.x, cc.x), v[j].x), __fmul_rn(__fmul_rn(cc.y, cc.y), v[j].y))
+                      : make_float2(0.f, 0.f);
+          if (c.ok && Q.write_p) st2(Q.p, c.rbase + t + P * j, v[j]);
+        }
+        if (sf) release(it++);
+        c.record(v, Q.rec[0]);
+        c.r2c(v, Q.S[3]);
       } else {
         // w = dt rho0 (2 sum rho + rho0) / rho0 per pair (nonlinear factor from
         // the previous step's density sum), rho0 kept for rho0 * div
@@ -338,11 +435,13 @@ static cudaError_t rows_tma_launch(int m, int nsm, cudaStream_t st, const RowsPa
 
 cudaError_t kw_rows_tma_attr(int m, int Hp, int ex_stride) {
   cudaError_t e = rows_tma_attr<ST_U>(m, Hp, ex_stride);
-  return e == cudaSuccess ? rows_tma_attr<ST_RHO_PL>(m, Hp, ex_stride) : e;
+  if (e == cudaSuccess) e = rows_tma_attr<ST_RHO_PL>(m, Hp, ex_stride);
+  return e == cudaSuccess ? rows_tma_attr<ST_EOS>(m, Hp, ex_stride) : e;
 }
 
 cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err) {
   if (stage == ST_U) return rows_tma_launch<ST_U>(m, nsm, st, Q, err);
   if (stage == ST_RHO_PL) return rows_tma_launch<ST_RHO_PL>(m, nsm, st, Q, err);
+  if (stage == ST_EOS) return rows_tma_launch<ST_EOS>(m, nsm, st, Q, err);
   return cudaErrorInvalidValue;
 }
