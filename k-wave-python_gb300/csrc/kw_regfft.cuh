@@ -70,6 +70,12 @@ __device__ __forceinline__ float2 w32(int j) {
   return make_float2(C, -S);
 }
 
+// Complex add / subtract as packed two-lane float operations (FADD2 / FFMA2
+// on sm_100+): one instruction each, component-wise identical to the scalar
+// forms (a - b is formed as b * (-1) + a, which is exact before the rounding).
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
 template <int R>
 struct Dft;
 
@@ -81,19 +87,20 @@ template <>
 struct Dft<2> {
   __device__ __forceinline__ static void run(float2* v) {
     const float2 a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
+    v[0] = padd(a, b);
+    v[1] = psub(a, b);
   }
 };
 template <>
 struct Dft<4> {
   __device__ __forceinline__ static void run(float2* v) {
-    const float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
-    const float2 b0 = cadd(v[1], v[3]), b1 = cmul_mi(csub(v[1], v[3]));
-    v[0] = cadd(a0, b0);
-    v[2] = csub(a0, b0);
-    v[1] = cadd(a1, b1);
-    v[3] = csub(a1, b1);
+    const float2 a0 = padd(v[0], v[2]), a1 = psub(v[0], v[2]);
+    const float2 b0 = padd(v[1], v[3]), d = psub(v[1], v[3]);
+    v[0] = padd(a0, b0);
+    v[2] = psub(a0, b0);
+    // a1 -/+ i d
+    v[1] = make_float2(a1.x + d.y, a1.y - d.x);
+    v[3] = make_float2(a1.x - d.y, a1.y + d.x);
   }
 };
 
