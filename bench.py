@@ -183,8 +183,8 @@ def measured_peaks():
 # DRAM bytes (read + write) per launch of each kernel class, measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the 256^3 headline
 # workload; profiles/timeloop_256cubed_kernels.md has the capture and command.
-NCU_TRAFFIC_256 = {"rows_rho": 914.7e6, "rows_u": 957.6e6, "rows_eos": 566.2e6, "axis_ops": 267.7e6,
-                   "axis_plain": 263.4e6}
+NCU_TRAFFIC_256 = {"rows_rho": 886.8e6, "rows_u": 957.5e6, "rows_eos": 530.2e6, "axis_ops": 268.5e6,
+                   "axis_plain": 263.2e6}
 
 
 def launch_bytes(S):
