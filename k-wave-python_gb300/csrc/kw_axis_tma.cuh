@@ -18,7 +18,9 @@
 //   KK_PLAIN  forward or inverse transforms of whole buffers (no operator);
 //   KK_GEN    any job list (operator chosen per job at run time);
 //   KK_GRAD   one input, D jobs: out a = gradient along axis a (the common
-//             kappa(|k|) / N is folded into the spectrum once);
+//             kappa(|k|) / N is folded into the spectrum once; the y and z
+//             gradients share one inverse transform, their 1-D operators
+//             being constant along x);
 //   KK_DIV    D inputs, job a: in a -> out a, derivative along axis a; kappa
 //             is evaluated once per tile and kept in registers for all items;
 //   KK_NAB    one or two inputs: in 0 -> |k|^pow1, in 1 -> |k|^pow2;
@@ -352,19 +354,32 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
               const float kp = kappa_kk(A, kk_of(k0s, A.ndim, t + P * m + E * k2, g)) * A.scale;
               v[m * P + k2] = make_float2(v[m * P + k2].x * kp, v[m * P + k2].y * kp);
             }
-#pragma unroll 1
-          for (int a = 0; a < A.ndim; ++a) {
-            const float2 fcol = col_factor_of(A, OP_GRAD, a, g);
+          // x derivative: its 1-D operator varies along x
+          {
             float2 y[E];
 #pragma unroll
             for (int m = 0; m < E / P; ++m)
 #pragma unroll
               for (int k2 = 0; k2 < P; ++k2) {
                 const int r = m * P + k2;
-                const float2 f = (a == 0) ? f0s.grad[t + P * m + E * k2] : fcol;
-                y[r] = on ? cconj(kwreg::cmulf(f, v[r])) : make_float2(0.f, 0.f);
+                y[r] = on ? cconj(kwreg::cmulf(f0s.grad[t + P * m + E * k2], v[r])) : make_float2(0.f, 0.f);
               }
-            rev_store<E, P>(y, t, exr, tw, sync, act, A.bufs[a], base, xs);
+            rev_store<E, P>(y, t, exr, tw, sync, act, A.bufs[0], base, xs);
+          }
+          // y and z derivatives: their 1-D operators are constant along x and
+          // commute with the x transform, so one inverse transform of
+          // kappa F / N serves both: out_a = op_a(column) * G
+#pragma unroll
+          for (int r = 0; r < E; ++r) v[r] = on ? cconj(v[r]) : make_float2(0.f, 0.f);
+          kwreg::Reg<E, P>::rev(v, t, exr, 1, tw, sync);
+          if (act) {
+#pragma unroll 1
+            for (int a = 1; a < A.ndim; ++a) {
+              const float2 fcol = col_factor_of(A, OP_GRAD, a, g);
+              float2* out = A.bufs[a];
+#pragma unroll
+              for (int j = 0; j < E; ++j) out[base + (t + P * j) * xs] = kwreg::cmulf(fcol, cconj(v[j]));
+            }
           }
         } else if constexpr (KIND == KK_DIV) {
           // item q is the velocity spectrum of axis q; its derivative replaces it
