@@ -29,7 +29,11 @@
 namespace {
 
 constexpr uint64_t kRowWaitNs = 2000000000ull;
-constexpr int kRowNst = 4;
+// Ring depth and resident CTAs per SM per stage: the density stage keeps its
+// density-sum slots in shared memory and needs more registers (2 CTAs, 4
+// slots); the velocity and EOS stages run 3 CTAs of 3 slots.
+__host__ __device__ constexpr int row_nst(int stage) { return stage == ST_RHO_PL ? 4 : 3; }
+__host__ __device__ constexpr int row_ctas(int stage) { return stage == ST_RHO_PL ? 2 : 3; }
 
 __device__ __forceinline__ bool consumers_any_rows(bool pred, int n) {
   uint32_t r;
@@ -90,7 +94,7 @@ __device__ __forceinline__ int row_nloads(const RowsParams& Q) {
 }  // namespace
 
 template <int E, int P, int NST, int STAGE>
-__global__ void __launch_bounds__(160, 2) k_rows_tma(const __grid_constant__ RowsParams Q, int* err) {
+__global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_constant__ RowsParams Q, int* err) {
   using namespace kwrows;
   constexpr int M = E * P, R = 128 / P, CT = 128;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -397,7 +401,8 @@ static size_t rows_tma_smem(int stage, int M, int E, int P, int Hp, int ex_strid
   const size_t spec_row = (size_t)Hp * 8, fld_row = (size_t)M * 8;
   const size_t slot = ((R * (spec_row > fld_row ? spec_row : fld_row)) + 127) & ~(size_t)127;
   const size_t nrs = stage == ST_RHO_PL ? (size_t)128 * E : 0;
-  return kRowNst * slot + sizeof(float2) * (2 * (size_t)M + 1 + (size_t)R * ex_stride + nrs) + 8 + 2 * kRowNst * 8 + 16;
+  const int nst = row_nst(stage);
+  return nst * slot + sizeof(float2) * (2 * (size_t)M + 1 + (size_t)R * ex_stride + nrs) + 8 + 2 * nst * 8 + 16;
 }
 
 #define KW_RT_SWITCH(m, CALL)              \
@@ -416,7 +421,7 @@ static cudaError_t rows_tma_attr(int m, int Hp, int ex_stride) {
   if (!kw_reg_shape(m, &E, &P)) return cudaErrorInvalidValue;
   const int smem = (int)rows_tma_smem(STAGE, m, E, P, Hp, ex_stride);
 #define KW_R(E_, P_) \
-  cudaFuncSetAttribute(k_rows_tma<E_, P_, kRowNst, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+  cudaFuncSetAttribute(k_rows_tma<E_, P_, row_nst(STAGE), STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
   KW_RT_SWITCH(m, KW_R)
 #undef KW_R
 }
@@ -426,9 +431,10 @@ static cudaError_t rows_tma_launch(int m, int nsm, cudaStream_t st, const RowsPa
   int E, P;
   if (!kw_reg_shape(m, &E, &P)) return cudaErrorInvalidValue;
   const int R = 128 / P, nblk = (Q.nrows + R - 1) / R;
-  const int grid = nblk < 2 * nsm ? nblk : 2 * nsm;
+  const int per_sm = row_ctas(STAGE);
+  const int grid = nblk < per_sm * nsm ? nblk : per_sm * nsm;
   const size_t smem = rows_tma_smem(STAGE, m, E, P, Q.Hp, Q.ex_stride);
-#define KW_R(E_, P_) (k_rows_tma<E_, P_, kRowNst, STAGE><<<grid, 160, smem, st>>>(Q, err), cudaGetLastError())
+#define KW_R(E_, P_) (k_rows_tma<E_, P_, row_nst(STAGE), STAGE><<<grid, 160, smem, st>>>(Q, err), cudaGetLastError())
   KW_RT_SWITCH(m, KW_R)
 #undef KW_R
 }
