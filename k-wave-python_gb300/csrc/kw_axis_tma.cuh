@@ -217,12 +217,21 @@ __device__ __forceinline__ void rev_store(float2 (&y)[E], int t, float2* exr, co
 
 }  // namespace kwtmak
 
+// Stride (complex values) between the exchange regions of adjacent columns.
+// Consumer thread tid = t * T + cc; a half warp holds 16 / T values of t for
+// each of T columns, and its 64-bit exchange accesses hit bank pairs
+// (cc * RS + t) mod 16.  With T = 8 they are distinct when RS = 2 (mod 16);
+// with T >= 16 (one t per half warp) when RS is odd.  N + E + 1 is odd.
+__host__ __device__ constexpr int kw_tma_rs(int N, int E, int T) {
+  return T == 8 ? N + E + 1 + ((2 - (N + E + 1) % 16) + 16) % 16 : N + E + 1;
+}
+
 // T columns per tile, CT = T * P consumer threads plus one producer warp.
 template <int E, int P, int NST, int MINB, int T, int KIND>
 __global__ void __launch_bounds__(T * P + 32, MINB)
     k_axis_tma(const __grid_constant__ AxisParams A, const __grid_constant__ TmaMaps maps, const TmaWork W) {
   using namespace kwtmak;
-  constexpr int N = E * P, RS = N + E + 1, CT = T * P;
+  constexpr int N = E * P, RS = kw_tma_rs(E * P, E, T), CT = T * P;
   constexpr bool OPS = KIND != KK_PLAIN;
   constexpr uint32_t kStageBytes = N * T * sizeof(float2);
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -488,7 +497,7 @@ inline int kw_tma_stages(int n, int kind) { return 2; }
 #define KW_NST_S 2
 
 inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
-  const int T = kw_tma_tile_cols(n, P, axis, kind), RS = n + E + 1, NST = kw_tma_stages(n, kind);
+  const int T = kw_tma_tile_cols(n, P, axis, kind), RS = kw_tma_rs(n, E, T), NST = kw_tma_stages(n, kind);
   const size_t nt = (n <= 512 && kind != KK_PLAIN) ? (size_t)n : 0;
   return sizeof(float2) * ((size_t)NST * n * T + (size_t)T * RS + n + 3 * nt) + sizeof(float) * nt +
          2 * NST * sizeof(uint64_t) + 16;
