@@ -122,6 +122,18 @@ int32_t kw_plan_set_sensor_interp(kw_plan* plan, int32_t n_points, int32_t n_cor
  * the KW_T_WCOORD tables and window is linearly interpolated from n samples on
  * [-radius, radius] (the rotated Blackman window of kwave/utils/signals.py:222-283). */
 int32_t kw_plan_set_p0_smoothing(kw_plan* plan, const float* window, int32_t n, double radius);
+/* Derive on the device, at kw_plan_finalize, the medium grids that the host
+ * would otherwise compute and upload (kspace_solver.py:655-666, :471-524):
+ *   what & 1: dt / rho0 on the three staggered grids (KW_F_DTRSG0..2) from the
+ *             KW_F_RHO0 grid, as the reference forms them in float32;
+ *   what & 2: tau = -2 a c0^(y-1) (power law) or -2 a c0 (Stokes);
+ *   what & 4: eta = 2 a c0^y tan(pi y / 2);
+ * with a = db2neper(alpha, y) (kwave/utils/conversion.py:20-35) from `alpha`
+ * (n = grid size values, dB/(MHz^y cm)) or the scalar alpha_s when alpha is
+ * NULL.  absorb_mode: 1 power law, 2 Stokes.  Fields derived this way must
+ * not also be set with kw_plan_set_field. */
+int32_t kw_plan_derive_medium(kw_plan* plan, int32_t what, const float* alpha, int64_t n, double alpha_s,
+                              double alpha_power, int32_t absorb_mode);
 /* Allocates device memory, uploads all inputs and resets the state to t = 0. */
 int32_t kw_plan_finalize(kw_plan* plan);
 /* Advances min(nsteps, Nt - t) steps of Simulation.step (kspace_solver.py:691-747)

@@ -735,3 +735,47 @@ __global__ void k_series_reduce(const float* __restrict__ series, int npts, int 
     out[pt] = m;
   }
 }
+
+// Medium grids of the time loop derived from c0 / rho0 / alpha on the device,
+// following the reference's float32 arithmetic (kspace_solver.py:655-666 with
+// float32 rho0: rho_sg = 0.5 (rho_i + rho_i+1), the last plane copied, then
+// dt / rho_sg; :471-524 and kwave/utils/conversion.py:20-35 for tau / eta,
+// whose db2neper divides by a float64 scalar, so they are formed in double).
+__global__ void k_derive_medium(const __grid_constant__ DeriveParams D) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long st[3] = {1, 1, 1};
+  if (D.ndim == 3) {
+    st[0] = (long long)D.N[1] * D.N[2];
+    st[1] = D.N[2];
+  } else {
+    st[0] = D.N[1];
+  }
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.ntot; i += stride) {
+    if (D.dtrsg[0]) {
+      const float r = D.rho0[i];
+      long long rem = i;
+      for (int a = 0; a < D.ndim; ++a) {
+        const long long ca = rem / st[a];
+        rem -= ca * st[a];
+        float rs = r;
+        if (D.use_sg && ca < D.N[a] - 1) rs = __fmul_rn(0.5f, __fadd_rn(r, D.rho0[i + st[a]]));
+        D.dtrsg[a][i] = __fdiv_rn(D.dt_f, rs);
+      }
+    }
+    if (D.tau || D.eta) {
+      const float c = D.c0 ? D.c0[i] : D.c0_s;
+      double a_np;
+      if (D.alpha) {
+        // float32 array arithmetic of db2neper up to its float64 divisor
+        a_np = (double)__fmul_rn(__fmul_rn(100.f, D.alpha[i]), D.db_fac_f) / D.db_div;
+      } else {
+        a_np = 100.0 * D.alpha_s * D.db_fac / D.db_div;
+      }
+      if (D.tau) {
+        const double cp = (D.absorb == 2) ? (double)c : (double)powf(c, (float)(D.y - 1.0));
+        D.tau[i] = (float)(-2.0 * a_np * cp);
+      }
+      if (D.eta) D.eta[i] = (float)(2.0 * a_np * (double)powf(c, (float)D.y) * D.tan_fac);
+    }
+  }
+}

@@ -182,6 +182,25 @@ __device__ __forceinline__ float window_at(const float* tab, int n, float rad, f
 __global__ void k_absmax(const float* __restrict__ x, long long n, unsigned int* out);
 // out = a / b for two float bit patterns (restore-max factor)
 __global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out);
+// Medium grids derived on the device (kw_plan_derive_medium); any output may be null.
+struct DeriveParams {
+  int ndim, N[3];
+  long long ntot;
+  float dt_f;          // dt as float32
+  int use_sg;
+  const float* rho0;
+  const float* c0;
+  float c0_s;
+  const float* alpha;  // null: alpha_s
+  double alpha_s;
+  double y, db_fac, db_div, tan_fac;  // (1e-6 / (2 pi))^y, 20 log10(e), tan(pi y / 2)
+  float db_fac_f;
+  int absorb;          // 1 power law, 2 Stokes
+  float* dtrsg[3];
+  float* tau;
+  float* eta;
+};
+__global__ void k_derive_medium(const __grid_constant__ DeriveParams D);
 // Returns and clears the device error word (nonzero: a bounded device wait timed out).
 int kw_device_error_take();
 // Device address of that word on the current device (nullptr on failure).

@@ -102,6 +102,11 @@ struct kw_plan {
   void* tma = nullptr;
   bool tma_axis[3] = {false, false, false};
   bool rows_tma = false;  // velocity / power-law density stages through kw_rows_tma
+  // kw_plan_derive_medium request
+  int derive_what = 0;
+  std::vector<float> halpha;
+  double alpha_s = 0.0, alpha_y = 0.0;
+  int derive_absorb = 0;
   int nsm = 0;
   int rows_regP = 0, rows_regE = 0, rows_R = 0, rows_RS = 0;
   // p0 smoothing on the device
@@ -270,6 +275,25 @@ int32_t kw_plan_set_field(kw_plan* p, int32_t field, const float* host, int64_t 
   return KW_OK;
 }
 
+int32_t kw_plan_derive_medium(kw_plan* p, int32_t what, const float* alpha, int64_t n, double alpha_s, double alpha_power,
+                              int32_t absorb_mode) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
+  if (what < 0 || what > 7) return fail(KW_ERR_INVALID, "derive_medium: bad selection %d", what);
+  if ((what & 6) && absorb_mode != 1 && absorb_mode != 2) return fail(KW_ERR_INVALID, "derive_medium: absorb_mode %d", absorb_mode);
+  if ((what & 4) && absorb_mode != 1) return fail(KW_ERR_INVALID, "derive_medium: eta needs the power law");
+  if (alpha && n != p->ntot) return fail(KW_ERR_INVALID, "derive_medium: alpha has %lld values, grid has %lld", (long long)n, p->ntot);
+  p->derive_what = what;
+  if (alpha)
+    p->halpha.assign(alpha, alpha + n);
+  else
+    p->halpha.clear();
+  p->alpha_s = alpha_s;
+  p->alpha_y = alpha_power;
+  p->derive_absorb = absorb_mode;
+  return KW_OK;
+}
+
 int32_t kw_plan_set_table(kw_plan* p, int32_t table, int32_t axis, const float* host, int64_t n_floats) {
   if (!p || !host) return fail(KW_ERR_INVALID, "null argument");
   if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
@@ -372,6 +396,8 @@ static int zero_state(kw_plan* p) {
   return KW_OK;
 }
 
+static void dfree_last(kw_plan* p, void* ptr);
+
 int32_t kw_plan_finalize(kw_plan* p) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");
   if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
@@ -411,6 +437,49 @@ int32_t kw_plan_finalize(kw_plan* p) {
   for (int f = 0; f < 9; ++f)
     if (!p->hfield[f].empty())
       if ((rc = upload(p, &p->d_field[f], p->hfield[f].data(), p->hfield[f].size()))) return rc;
+  if (p->derive_what) {
+    DeriveParams Dp;
+    memset(&Dp, 0, sizeof(Dp));
+    Dp.ndim = D;
+    for (int a = 0; a < 3; ++a) Dp.N[a] = a < D ? p->N[a] : 1;
+    Dp.ntot = p->ntot;
+    Dp.dt_f = (float)p->g.dt;
+    Dp.use_sg = p->g.use_sg;
+    Dp.rho0 = p->d_field[KW_F_RHO0];
+    Dp.c0 = p->d_field[KW_F_C0];
+    Dp.c0_s = p->hscalar[KW_F_C0];
+    Dp.alpha_s = p->alpha_s;
+    Dp.y = p->alpha_y;
+    const double kPi = 3.14159265358979323846;
+    Dp.db_fac = std::pow(1e-6 / (2.0 * kPi), p->alpha_y);
+    Dp.db_fac_f = (float)Dp.db_fac;
+    Dp.db_div = 20.0 * std::log10(std::exp(1.0));
+    Dp.tan_fac = std::tan(kPi * p->alpha_y / 2.0);
+    Dp.absorb = p->derive_absorb;
+    float* dalpha = nullptr;
+    if (!p->halpha.empty() && (rc = upload(p, &dalpha, p->halpha.data(), p->halpha.size()))) return rc;
+    Dp.alpha = dalpha;
+    if (p->derive_what & 1) {
+      if (!Dp.rho0) return fail(KW_ERR_INVALID, "derive_medium: dt/rho0 needs a rho0 grid");
+      for (int a = 0; a < D; ++a) {
+        if (!p->d_field[KW_F_DTRSG0 + a] && (rc = dalloc(p, &p->d_field[KW_F_DTRSG0 + a], p->ntot))) return rc;
+        Dp.dtrsg[a] = p->d_field[KW_F_DTRSG0 + a];
+      }
+    }
+    if (p->derive_what & 2) {
+      if (!p->d_field[KW_F_TAU] && (rc = dalloc(p, &p->d_field[KW_F_TAU], p->ntot))) return rc;
+      Dp.tau = p->d_field[KW_F_TAU];
+    }
+    if (p->derive_what & 4) {
+      if (!p->d_field[KW_F_ETA] && (rc = dalloc(p, &p->d_field[KW_F_ETA], p->ntot))) return rc;
+      Dp.eta = p->d_field[KW_F_ETA];
+    }
+    const int grid = (int)std::min<long long>((p->ntot + 255) / 256, 4096);
+    k_derive_medium<<<grid, 256>>>(Dp);
+    CK(cudaGetLastError());
+    CK(cudaDeviceSynchronize());
+    if (dalpha) dfree_last(p, dalpha);
+  }
   // p0 smoothing
   if (p->smooth) {
     if (!p->d_field[KW_F_P0]) return fail(KW_ERR_INVALID, "p0 smoothing requested without a p0 grid");

@@ -73,6 +73,7 @@ _PROTOS = {
     "kw_plan_set_sensor": (C.c_int32, [_P, _P, C.c_int32, C.c_int32]),
     "kw_plan_set_sensor_interp": (C.c_int32, [_P, C.c_int32, C.c_int32, _P, _P]),
     "kw_plan_set_p0_smoothing": (C.c_int32, [_P, _P, C.c_int32, C.c_double]),
+    "kw_plan_derive_medium": (C.c_int32, [_P, C.c_int32, _P, C.c_int64, C.c_double, C.c_double, C.c_int32]),
     "kw_plan_finalize": (C.c_int32, [_P]),
     "kw_plan_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_plan_sync": (C.c_int32, [_P, _P]),

@@ -276,6 +276,12 @@ class Setup:
     nonlinear: int = 0
     alpha_power: float = 0.0
     sources: list = field(default_factory=list)
+    # medium grids left to the device (kw_plan_derive_medium): bit 0 dt/rho_sg,
+    # bit 1 tau, bit 2 eta; with the absorption-coefficient grid (float32) or
+    # scalar and the absorption mode
+    derive: int = 0
+    derive_alpha: object = None
+    derive_alpha_s: float = 0.0
     sensor_kind: str = "all"                          # all | binary | cartesian
     slots: np.ndarray = None                          # int64 flat indices sampled every recorded step
     n_points: int = 0
@@ -350,8 +356,11 @@ def _cartesian_stencil(cart, shape, spacing):
     return slots.astype(np.int64), inv.reshape(npts, nc).astype(np.int32), wt
 
 
-def build_setup(prob) -> Setup:
-    """FP64 precompute of everything the device plan needs."""
+def build_setup(prob, derive_on_device=False) -> Setup:
+    """FP64 precompute of everything the device plan needs.  With
+    ``derive_on_device`` the grids of dt/rho0 on the staggered grids and of
+    tau / eta are left to the device (``Setup.derive``), which forms them from
+    the uploaded float32 c0 / rho0 / alpha as the reference does."""
     shape = tuple(int(n) for n in prob["shape"])
     spacing = tuple(float(d) for d in prob["spacing"])
     ndim = len(shape)
@@ -447,30 +456,42 @@ def build_setup(prob) -> Setup:
     if _enabled(ac):
         y = float(np.asarray(prob.get("alpha_power", 1.5), dtype=np.float64).ravel()[0])
         alpha = expand_to_grid(ac, shape, "alpha_coeff")
-        a_np = db2neper(alpha, y) if isinstance(alpha, float) else db2neper(np.asarray(alpha), y)
         S.alpha_power = y
         stokes = abs(y - 2.0) < 1e-10
         if mode == "no_absorption":
             S.absorb_mode = 0
-        elif stokes:
-            S.absorb_mode = 2
-            S.fields["tau"] = _cell_field(shape, lambda sl: -2 * _sl(a_np, sl) * _sl(c0, sl), a_np, c0)
         else:
-            S.absorb_mode = 1
-            S.fields["tau"] = _cell_field(
-                shape, lambda sl: -2 * _sl(a_np, sl) * _pow(_sl(c0, sl), y - 1), a_np, c0)
-            if mode not in ("no_absorption", "no_dispersion"):
-                S.dispersion = 1
-                tn = math.tan(math.pi * y / 2)
-                S.fields["eta"] = _cell_field(
-                    shape, lambda sl: 2 * _sl(a_np, sl) * _pow(_sl(c0, sl), y) * tn, a_np, c0)
+            S.absorb_mode = 2 if stokes else 1
+            S.dispersion = int(not stokes and mode not in ("no_absorption", "no_dispersion"))
+            grid_in = not (isinstance(alpha, float) and isinstance(c0, float))
+            if derive_on_device and grid_in:
+                S.derive |= 2 | (4 if S.dispersion else 0)
+                if isinstance(alpha, float):
+                    S.derive_alpha_s = alpha
+                else:
+                    S.derive_alpha = _par_fill(tuple(shape), lambda i, j: alpha[i:j])
+            elif stokes:
+                a_np = db2neper(alpha, y) if isinstance(alpha, float) else db2neper(np.asarray(alpha), y)
+                S.fields["tau"] = _cell_field(shape, lambda sl: -2 * _sl(a_np, sl) * _sl(c0, sl), a_np, c0)
+            else:
+                a_np = db2neper(alpha, y) if isinstance(alpha, float) else db2neper(np.asarray(alpha), y)
+                S.fields["tau"] = _cell_field(
+                    shape, lambda sl: -2 * _sl(a_np, sl) * _pow(_sl(c0, sl), y - 1), a_np, c0)
+                if S.dispersion:
+                    tn = math.tan(math.pi * y / 2)
+                    S.fields["eta"] = _cell_field(
+                        shape, lambda sl: 2 * _sl(a_np, sl) * _pow(_sl(c0, sl), y) * tn, a_np, c0)
     B = prob.get("BonA", 0)
     if _enabled(B):
         S.nonlinear = 1
         S.fields["BonA"] = f32(expand_to_grid(B, shape, "BonA"))
 
     # --- dt / rho0 on the staggered grids (kspace_solver.py:655-666) ---
+    if derive_on_device and not isinstance(rho0, float):
+        S.derive |= 1
     for a in range(ndim):
+        if S.derive & 1:
+            continue
         if isinstance(rho0, float):
             S.fields[f"dtrsg{a}"] = dt / rho0
         elif not S.use_sg:

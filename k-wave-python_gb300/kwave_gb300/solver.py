@@ -83,6 +83,14 @@ class DevicePlan:
                 a = np.ascontiguousarray(v, dtype=np.float32).ravel()
                 nbytes += a.nbytes
                 K.check(lib.kw_plan_set_field(h, fid, K.ptr(a), a.size, C.c_float(0.0)))
+        if S.derive:
+            al = S.derive_alpha
+            if al is not None:
+                al = np.ascontiguousarray(al, dtype=np.float32).ravel()
+                nbytes += al.nbytes
+            K.check(lib.kw_plan_derive_medium(h, S.derive, K.ptr(al) if al is not None else None,
+                                              0 if al is None else al.size, C.c_double(S.derive_alpha_s),
+                                              C.c_double(S.alpha_power), S.absorb_mode))
         for (name, axis), tb in S.tables.items():
             a = np.ascontiguousarray(tb, dtype=np.float32)
             nbytes += a.nbytes
@@ -204,7 +212,7 @@ class Simulation:
 
     # -- setup / stepping ---------------------------------------------------
     def setup(self):
-        self.S = build_setup(self.prob)
+        self.S = build_setup(self.prob, derive_on_device=True)
         self._plan = DevicePlan(self.S, stream=self.stream)
         self.t = 0
         return self

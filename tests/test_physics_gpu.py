@@ -100,3 +100,30 @@ def test_power_of_two_physics(kind, shape):
         for a, (x, y) in enumerate(zip(mine, theirs)):
             e = rel_l2(x, y)
             assert e <= TOL, (name, a, e)
+
+
+@pytest.mark.parametrize("kind,shape", [("powerlaw", (64, 32, 64)), ("stokes", (48, 40)),
+                                        ("powerlaw_nodisp", (32, 64, 128))])
+def test_device_derived_medium(kind, shape):
+    """dt/rho_sg, tau and eta formed on the device (kw_plan_derive_medium)
+    against the same grids formed on the host in FP64: the two runs agree to
+    float32 rounding of the medium arrays."""
+    from kwave_gb300.precompute import build_setup
+    from kwave_gb300.solver import DevicePlan
+    from kwave_gb300 import _lib as K
+
+    rng = np.random.default_rng(zlib.crc32(f"derive{kind}{shape}".encode()))
+    prob = problem(kind, shape, rng)
+    outs = []
+    for dev in (False, True):
+        S = build_setup(prob, derive_on_device=dev)
+        assert bool(S.derive) == dev
+        plan = DevicePlan(S)
+        try:
+            plan.run(S.Nt)
+            plan.sync()
+            outs.append([plan.read_field(K.KW_FLD_P)] + [plan.read_field(K.KW_FLD_U0 + a) for a in range(len(shape))])
+        finally:
+            plan.close()
+    for a, b in zip(*outs):
+        assert rel_l2(b, a) <= 2e-6, rel_l2(b, a)
