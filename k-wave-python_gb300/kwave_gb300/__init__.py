@@ -10,12 +10,14 @@ Entry points:
   * ``unified.kspaceFirstOrder`` — the unified entry point
     (``kwave.kspaceFirstOrder.kspaceFirstOrder``) for ``backend="gb300"``;
   * ``backend.kspaceFirstOrder2D`` / ``3D`` — the legacy signatures;
-  * ``reconstruction.TimeReversal`` — time-reversal reconstruction.
+  * ``reconstruction.TimeReversal`` — time-reversal reconstruction, with
+    ``conversion.cart2grid`` for Cartesian sensors.
 """
 __version__ = "0.1.0"
 
 from .backend import (BACKEND, execution_options, install, kspaceFirstOrder2D, kspaceFirstOrder3D,  # noqa: F401
                       run_gb300_backend, uninstall)
+from .conversion import cart2grid  # noqa: F401
 from .reconstruction import TimeReversal  # noqa: F401
 from .solver import Simulation, run_problem  # noqa: F401
 from .unified import get_optimal_pml_size, kspaceFirstOrder, reshape_to_grid  # noqa: F401

@@ -230,3 +230,57 @@ def test_time_reversal_rejections():
     tr = TimeReversal(kgrid, medium, NS(mask=mask, record=None))
     with pytest.raises(ValueError, match="recorded pressure"):
         tr(_oracle_legacy, NS(), None)
+
+
+# ---------------------------------------------------------------------------
+# cart2grid (kwave/utils/conversion.py:164-325)
+# ---------------------------------------------------------------------------
+
+def _circle(n, r):
+    th = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    return np.stack([r * np.cos(th), r * np.sin(th)])
+
+
+def test_cart2grid_values():
+    from kwave_gb300 import cart2grid
+
+    kg = NS(N=np.array([32, 40]), spacing=np.array([1e-4, 1e-4]))
+    pts = _circle(24, 1.2e-3)
+    grid, order_index, reorder = cart2grid(kg, pts, order="C")
+    assert grid.shape == (32, 40) and grid.dtype.kind == "i"
+    # every point lands where rounding puts it, and the reorder index lists the
+    # points in C order of their grid positions
+    ix = np.round(pts[0] / 1e-4).astype(int) + 16
+    iy = np.round(pts[1] / 1e-4).astype(int) + 20
+    assert grid[ix, iy].all() and grid.sum() == len(set(zip(ix, iy)))
+    flat = np.ravel_multi_index((ix, iy), (32, 40))
+    assert np.array_equal(np.sort(flat[reorder[:, 0].astype(int) - 1]), flat[reorder[:, 0].astype(int) - 1])
+    assert sorted(order_index[:, 0]) == list(range(1, reorder.size + 1))
+    with pytest.warns(FutureWarning, match="cart2grid"):
+        cart2grid(kg, pts)
+    with pytest.raises(AssertionError, match="within the grid"):
+        cart2grid(kg, pts * 100, order="C")
+
+
+def test_cart2grid_matches_reference():
+    import kwave_shim
+
+    if not kwave_shim.reference_available():
+        pytest.skip("reference checkout not present")
+    kwave_shim.install()
+    from kwave.kgrid import kWaveGrid
+    from kwave.utils.conversion import cart2grid as ref
+
+    from kwave_gb300 import cart2grid
+
+    rng = np.random.default_rng(3)
+    cases = [([48, 40], _circle(60, 1.5e-3)), ([20, 24, 18], rng.uniform(-7e-4, 7e-4, size=(3, 30))),
+             ([50], rng.uniform(-2e-3, 2e-3, size=(1, 12)))]
+    for N, pts in cases:
+        kg = kWaveGrid(N, [1e-4] * len(N))
+        for order in ("C", "F"):
+            mine = cart2grid(kg, pts, order=order)
+            theirs = ref(kg, pts, order=order)
+            for a, b in zip(mine, theirs):
+                assert np.asarray(a).shape == np.asarray(b).shape
+                assert np.array_equal(np.asarray(a), np.asarray(b)), (N, order)
