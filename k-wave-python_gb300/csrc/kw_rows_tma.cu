@@ -32,8 +32,8 @@ constexpr uint64_t kRowWaitNs = 2000000000ull;
 // Ring depth and resident CTAs per SM per stage: the density stage keeps its
 // density-sum slots in shared memory and needs more registers (2 CTAs, 4
 // slots); the velocity and EOS stages run 3 CTAs of 3 slots.
-__host__ __device__ constexpr int row_nst(int stage) { return stage == ST_RHO_PL ? 4 : 3; }
-__host__ __device__ constexpr int row_ctas(int stage) { return stage == ST_RHO_PL ? 2 : 3; }
+__host__ __device__ constexpr int row_nst(int stage) { return stage == ST_RHO_PL ? 2 : 3; }
+__host__ __device__ constexpr int row_ctas(int stage) { return 3; }
 
 __device__ __forceinline__ bool consumers_any_rows(bool pred, int n) {
   uint32_t r;
@@ -79,16 +79,19 @@ __device__ __forceinline__ const void* row_load(const RowsParams& Q, int idx, bo
       spec = false;
       return Q.nonlin ? Q.rho_sum : nullptr;
     }
+    if (idx == 2 + 2 * D) {
+      spec = false;
+      return Q.rho0;  // again, for rho0 * div
+    }
     const int a = (idx - 2) >> 1, q = (idx - 2) & 1;
     spec = q == 0;
-    (void)D;
     return q == 0 ? (const void*)Q.S[a] : (const void*)Q.rho[a];
   }
 }
 
 template <int STAGE>
 __device__ __forceinline__ int row_nloads(const RowsParams& Q) {
-  return STAGE == ST_U ? 3 * Q.ndim : STAGE == ST_EOS ? 8 : 2 + 2 * Q.ndim;
+  return STAGE == ST_U ? 3 * Q.ndim : STAGE == ST_EOS ? 8 : 3 + 2 * Q.ndim;
 }
 
 }  // namespace
@@ -308,7 +311,7 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
       } else {
         // w = dt rho0 (2 sum rho + rho0) / rho0 per pair (nonlinear factor from
         // the previous step's density sum), rho0 kept for rho0 * div
-        float2 w[E], r0v[E], div[E];
+        float2 w[E], div[E];
         const float2* s0 = nullptr;
         const float2* s1 = nullptr;
         const uint32_t i0 = it;
@@ -323,12 +326,12 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int n = t + P * j;
-          r0v[j] = s0 ? s0[row * M + n] : make_float2(Q.rho0_s, Q.rho0_s);
-          w[j] = make_float2(__fmul_rn(Q.dt, r0v[j].x), __fmul_rn(Q.dt, r0v[j].y));
+          const float2 r0 = s0 ? s0[row * M + n] : make_float2(Q.rho0_s, Q.rho0_s);
+          w[j] = make_float2(__fmul_rn(Q.dt, r0.x), __fmul_rn(Q.dt, r0.y));
           if (Q.nonlin) {
             const float2 sr = s1[row * M + n];
-            w[j] = make_float2(__fmul_rn(w[j].x, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.x), r0v[j].x), r0v[j].x)),
-                               __fmul_rn(w[j].y, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0v[j].y), r0v[j].y)));
+            w[j] = make_float2(__fmul_rn(w[j].x, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.x), r0.x), r0.x)),
+                               __fmul_rn(w[j].y, __fdiv_rn(__fadd_rn(__fmul_rn(2.f, sr.y), r0.y), r0.y)));
           }
         }
         for (uint32_t i = i0; i < it; ++i) release(i);
@@ -367,14 +370,17 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
           }
         }
         if (aborted) break;
+        const float2* s2 = nullptr;
+        if (Q.rho0) {
+          s2 = wait_item(it);
+          if (!s2) break;
+        }
 #pragma unroll
         for (int j = 0; j < E; ++j) {
-          if (c.ok) {
-            v[j] = make_float2(__fmul_rn(r0v[j].x, div[j].x), __fmul_rn(r0v[j].y, div[j].y));
-          } else {
-            v[j] = make_float2(0.f, 0.f);
-          }
+          const float2 r0 = s2 ? s2[row * M + t + P * j] : make_float2(Q.rho0_s, Q.rho0_s);
+          v[j] = c.ok ? make_float2(__fmul_rn(r0.x, div[j].x), __fmul_rn(r0.y, div[j].y)) : make_float2(0.f, 0.f);
         }
+        if (s2) release(it++);
         c.r2c(v, Q.S[0]);
 #pragma unroll
         for (int j = 0; j < E; ++j) {
