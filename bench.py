@@ -183,7 +183,7 @@ def measured_peaks():
 # DRAM bytes (read + write) per launch of each kernel class, measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the 256^3 headline
 # workload; profiles/timeloop_256cubed_kernels.md has the capture and command.
-NCU_TRAFFIC_256 = {"rows_rho": 886.8e6, "rows_u": 957.5e6, "rows_eos": 530.2e6, "axis_ops": 268.5e6,
+NCU_TRAFFIC_256 = {"rows_rho": 908.3e6, "rows_u": 956.3e6, "rows_eos": 529.7e6, "axis_ops": 268.6e6,
                    "axis_plain": 263.2e6}
 
 
