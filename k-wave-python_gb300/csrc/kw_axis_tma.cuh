@@ -251,7 +251,8 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       kwtma::mbar_init(&full[s], 1);
-      kwtma::mbar_init(&empty[s], CT / 32);
+      // plain passes: the slot is freed by the thread that stores it back with TMA
+      kwtma::mbar_init(&empty[s], OPS ? CT / 32 : 1);
     }
     counters[0] = counters[1] = 0;
     kwtma::fence_barrier_init();
@@ -333,25 +334,36 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
 #pragma unroll
           for (int j = 0; j < E; ++j) v[j] = st[(t + P * j) * T + cc];
         }
-        __syncwarp();
-        if (lane == 0) kwtma::mbar_arrive(&empty[s]);
+        if constexpr (OPS) {
+          __syncwarp();
+          if (lane == 0) kwtma::mbar_arrive(&empty[s]);
+        }
 
         if constexpr (KIND == KK_PLAIN) {
-          float2* buf = A.bufs[A.plain[b]];
+          // transform, write the results back into the stage slot in the
+          // tile's layout and store the tile with TMA (the slot is freed once
+          // the store has read it)
+          float2* so = stages + (size_t)s * N * T;
           if (A.mode == 0) {
             kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
-            if (act) {
 #pragma unroll
-              for (int m = 0; m < E / P; ++m)
+            for (int m = 0; m < E / P; ++m)
 #pragma unroll
-                for (int k2 = 0; k2 < P; ++k2) buf[base + (t + P * m + E * k2) * xs] = v[m * P + k2];
-            }
+              for (int k2 = 0; k2 < P; ++k2) so[(t + P * m + E * k2) * T + cc] = v[m * P + k2];
           } else {
             kwreg::Reg<E, P>::rev(v, t, exr, 1, tw, sync);
-            if (act) {
 #pragma unroll
-              for (int j = 0; j < E; ++j) buf[base + (t + P * j) * xs] = cconj(v[j]);
-            }
+            for (int j = 0; j < E; ++j) so[(t + P * j) * T + cc] = cconj(v[j]);
+          }
+          kwtma::fence_proxy_async_smem();
+          kwtma::named_sync(CT);
+          if (tid == 0) {
+            const CUtensorMap* map = &maps.m[A.plain[b]];
+#pragma unroll
+            for (int n0 = 0; n0 < N; n0 += 256) kwtma::tma_store_3d(map, so + n0 * T, tile * T, n0, outer);
+            kwtma::bulk_commit();
+            kwtma::bulk_wait_read_all();
+            kwtma::mbar_arrive(&empty[s]);
           }
         } else if constexpr (KIND == KK_GRAD) {
           kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
@@ -469,7 +481,10 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
         }
       }
     }
-    if (tid == 0) counters[1] = (int)it;
+    if (tid == 0) {
+      counters[1] = (int)it;
+      if constexpr (!OPS) kwtma::bulk_wait_all();  // tile stores complete before the CTA exits
+    }
   }
   __syncthreads();
   // loads issued but never consumed (only after a timeout): wait for them, bounded
