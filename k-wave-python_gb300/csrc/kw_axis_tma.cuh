@@ -233,6 +233,8 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
   using namespace kwtmak;
   constexpr int N = E * P, RS = kw_tma_rs(E * P, E, T), CT = T * P;
   constexpr bool OPS = KIND != KK_PLAIN;
+  // kinds whose single result per item goes back through the stage slot and a TMA store
+  constexpr bool TSTORE = KIND == KK_PLAIN || KIND == KK_DIV || KIND == KK_NAB;
   constexpr uint32_t kStageBytes = N * T * sizeof(float2);
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* stages = reinterpret_cast<float2*>(smem_raw);  // NST * N * T
@@ -251,8 +253,8 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
       kwtma::mbar_init(&full[s], 1);
-      // plain passes: the slot is freed by the thread that stores it back with TMA
-      kwtma::mbar_init(&empty[s], OPS ? CT / 32 : 1);
+      // tile-store kinds: the slot is freed by the thread that stores it back with TMA
+      kwtma::mbar_init(&empty[s], TSTORE ? 1 : CT / 32);
     }
     counters[0] = counters[1] = 0;
     kwtma::fence_barrier_init();
@@ -334,10 +336,27 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
 #pragma unroll
           for (int j = 0; j < E; ++j) v[j] = st[(t + P * j) * T + cc];
         }
-        if constexpr (OPS) {
+        if constexpr (!TSTORE) {
           __syncwarp();
           if (lane == 0) kwtma::mbar_arrive(&empty[s]);
         }
+        // write the item's result (inverse-transformed, conjugated back) into
+        // the slot and store it with TMA to buffer `ob`; frees the slot
+        auto store_rev = [&](float2 (&y)[E], int ob) {
+          float2* so = stages + (size_t)s * N * T;
+          kwreg::Reg<E, P>::rev(y, t, exr, 1, tw, sync);
+#pragma unroll
+          for (int j = 0; j < E; ++j) so[(t + P * j) * T + cc] = cconj(y[j]);
+          kwtma::fence_proxy_async_smem();
+          kwtma::named_sync(CT);
+          if (tid == 0) {
+#pragma unroll
+            for (int n0 = 0; n0 < N; n0 += 256) kwtma::tma_store_3d(&maps.m[ob], so + n0 * T, tile * T, n0, outer);
+            kwtma::bulk_commit();
+            kwtma::bulk_wait_read_all();
+            kwtma::mbar_arrive(&empty[s]);
+          }
+        };
 
         if constexpr (KIND == KK_PLAIN) {
           // transform, write the results back into the stage slot in the
@@ -422,7 +441,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
               const float2 op = make_float2(f.x * kc[r], f.y * kc[r]);
               v[r] = on ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
             }
-          rev_store<E, P>(v, t, exr, tw, sync, act, A.bufs[W.inp[q]], base, xs);
+          store_rev(v, W.inp[q]);
         } else if constexpr (KIND == KK_NAB) {
           // item 0: |k|^pow1 on buffer 0, item 1: |k|^pow2 on buffer 1 (0 at k = 0)
           kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
@@ -439,7 +458,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
             const float2 op = make_float2(val * A.scale, 0.f);
             v[r] = on ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
           }
-          rev_store<E, P>(v, t, exr, tw, sync, act, A.bufs[W.inp[q]], base, xs);
+          store_rev(v, W.inp[q]);
         } else {
           // generic operator mode: forward FFT of this input, then every job reading it
           kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
@@ -483,7 +502,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
     }
     if (tid == 0) {
       counters[1] = (int)it;
-      if constexpr (!OPS) kwtma::bulk_wait_all();  // tile stores complete before the CTA exits
+      if constexpr (TSTORE) kwtma::bulk_wait_all();  // tile stores complete before the CTA exits
     }
   }
   __syncthreads();
