@@ -113,7 +113,9 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
   // (rsm[j * 128 + thread]) instead of registers
   float2* rsm = ex + R * Q.ex_stride;
   constexpr int NRS = STAGE == ST_RHO_PL ? 128 * E : 0;
-  uint64_t* full = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(rsm + NRS) + 7) & ~uintptr_t(7));
+  // the stage's PML profile along the last axis (2 M reals), read per element
+  float* pmlz = reinterpret_cast<float*>(rsm + NRS);
+  uint64_t* full = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(pmlz + 2 * M) + 7) & ~uintptr_t(7));
   uint64_t* empty = full + NST;
   int* counters = reinterpret_cast<int*>(empty + NST);
 
@@ -128,6 +130,10 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
   }
   for (int i = tid; i < M; i += blockDim.x) tw[i] = Q.tw[i];
   for (int i = tid; i <= M; i += blockDim.x) twp[i] = Q.twpost[i];
+  if constexpr (STAGE == ST_U || STAGE == ST_RHO_PL) {
+    const float* src = STAGE == ST_U ? Q.pmlsg[D - 1] : Q.pml[D - 1];
+    for (int i = tid; i < 2 * M; i += blockDim.x) pmlz[i] = src[i];
+  }
   __syncthreads();
 
   const int nblk = (Q.nrows + R - 1) / R;
@@ -210,7 +216,7 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
             if (!c.ok) continue;
             const float2 g = v[j];
             const float2 dtr = has_dtr ? drow[n] : make_float2(Q.dtrsg_s[a], Q.dtrsg_s[a]);
-            const float2 sg = c.pml2(Q.pmlsg[a], a, n);
+            const float2 sg = c.pml2(a == D - 1 ? pmlz : Q.pmlsg[a], a, n);
             const float2 u = urow[n];
             v[j] = make_float2(__fmul_rn(sg.x, __fsub_rn(__fmul_rn(sg.x, u.x), __fmul_rn(dtr.x, g.x))),
                                __fmul_rn(sg.y, __fsub_rn(__fmul_rn(sg.y, u.y), __fmul_rn(dtr.y, g.y))));
@@ -351,7 +357,7 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
             const float2 d0 = (a == 0) ? make_float2(0.f, 0.f) : div[j];
             div[j] = make_float2(__fadd_rn(d0.x, du.x), __fadd_rn(d0.y, du.y));
             if (!c.ok) continue;
-            const float2 pm = c.pml2(Q.pml[a], a, n);
+            const float2 pm = c.pml2(a == D - 1 ? pmlz : Q.pml[a], a, n);
             const float2 ro = rrow[n];
             const float tx = __fmul_rn(w[j].x, du.x);
             const float ty = __fmul_rn(w[j].y, du.y);
@@ -408,7 +414,8 @@ static size_t rows_tma_smem(int stage, int M, int E, int P, int Hp, int ex_strid
   const size_t slot = ((R * (spec_row > fld_row ? spec_row : fld_row)) + 127) & ~(size_t)127;
   const size_t nrs = stage == ST_RHO_PL ? (size_t)128 * E : 0;
   const int nst = row_nst(stage);
-  return nst * slot + sizeof(float2) * (2 * (size_t)M + 1 + (size_t)R * ex_stride + nrs) + 8 + 2 * nst * 8 + 16;
+  return nst * slot + sizeof(float2) * (2 * (size_t)M + 1 + (size_t)R * ex_stride + nrs) + sizeof(float) * 2 * M + 8 +
+         2 * nst * 8 + 16;
 }
 
 #define KW_RT_SWITCH(m, CALL)              \
