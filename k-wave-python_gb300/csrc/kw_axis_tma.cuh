@@ -206,9 +206,9 @@ __device__ __forceinline__ float2 col_factor(const AxisParams& A, const AxisJob&
 
 // Inverse transform of y (frequency layout) and store of column cc to `out`.
 template <int E, int P, class Sync>
-__device__ __forceinline__ void rev_store(float2 (&y)[E], int t, float2* exr, const float2* tw, Sync sync, bool act,
+__device__ __forceinline__ void rev_store(float2 (&y)[E], int t, float2* exr, const float2* twr, Sync sync, bool act,
                                           float2* out, uint32_t base, uint32_t xs) {
-  kwreg::Reg<E, P>::rev(y, t, exr, 1, tw, sync);
+  kwreg::Reg<E, P>::rev_t(y, t, exr, 1, twr, sync);
   if (act) {
 #pragma unroll
     for (int j = 0; j < E; ++j) out[base + (t + P * j) * xs] = cconj(y[j]);
@@ -239,11 +239,14 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* stages = reinterpret_cast<float2*>(smem_raw);  // NST * N * T
   float2* ex = stages + (size_t)NST * N * T;             // T * RS
-  float2* tw = ex + (size_t)T * RS;                      // N
+  // per-thread twiddle rows of the forward and inverse transforms (Reg::build_rows)
+  constexpr int TWR = kwreg::Reg<E, P>::TW_ROW;
+  float2* twf = ex + (size_t)T * RS;                     // P * TWR
+  float2* twrt = twf + P * TWR;                          // P * TWR
   // x-axis tables (k, op_grad, op_div, unstag) in shared memory when they fit
   constexpr bool kTablesInSmem = N <= 512 && KIND != KK_PLAIN;
   constexpr int NT = kTablesInSmem ? N : 0;
-  float* k0t = reinterpret_cast<float*>(tw + N);
+  float* k0t = reinterpret_cast<float*>(twrt + P * TWR);
   float2* f0t = reinterpret_cast<float2*>(k0t + NT);
   uint64_t* full = reinterpret_cast<uint64_t*>(f0t + 3 * NT);
   uint64_t* empty = full + NST;
@@ -259,8 +262,8 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
     counters[0] = counters[1] = 0;
     kwtma::fence_barrier_init();
   }
+  kwreg::Reg<E, P>::build_rows(twf, twrt, A.tw, tid, blockDim.x);
   for (int i = tid; i < N; i += blockDim.x) {
-    tw[i] = A.tw[i];
     if (kTablesInSmem && OPS) {
       k0t[i] = A.k[0][i];
       f0t[i] = A.fg[0][i];
@@ -300,6 +303,8 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
     // ---------------- consumers ----------------
     const int cc = tid % T, t = tid / T;
     auto sync = [] __device__() { kwtma::named_sync(CT); };
+    const float2* tw = twf + t * TWR;   // this thread's forward twiddles
+    const float2* twr = twrt + t * TWR;  // and inverse twiddles
     float2* exr = ex + cc * RS;
     uint32_t it = 0;
     bool aborted = false;
@@ -344,7 +349,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
         // the slot and store it with TMA to buffer `ob`; frees the slot
         auto store_rev = [&](float2 (&y)[E], int ob) {
           float2* so = stages + (size_t)s * N * T;
-          kwreg::Reg<E, P>::rev(y, t, exr, 1, tw, sync);
+          kwreg::Reg<E, P>::rev_t(y, t, exr, 1, twr, sync);
 #pragma unroll
           for (int j = 0; j < E; ++j) so[(t + P * j) * T + cc] = cconj(y[j]);
           kwtma::fence_proxy_async_smem();
@@ -364,13 +369,13 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
           // the store has read it)
           float2* so = stages + (size_t)s * N * T;
           if (A.mode == 0) {
-            kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
+            kwreg::Reg<E, P>::fwd_t(v, t, exr, 1, tw, sync);
 #pragma unroll
             for (int m = 0; m < E / P; ++m)
 #pragma unroll
               for (int k2 = 0; k2 < P; ++k2) so[(t + P * m + E * k2) * T + cc] = v[m * P + k2];
           } else {
-            kwreg::Reg<E, P>::rev(v, t, exr, 1, tw, sync);
+            kwreg::Reg<E, P>::rev_t(v, t, exr, 1, twr, sync);
 #pragma unroll
             for (int j = 0; j < E; ++j) so[(t + P * j) * T + cc] = cconj(v[j]);
           }
@@ -385,7 +390,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
             kwtma::mbar_arrive(&empty[s]);
           }
         } else if constexpr (KIND == KK_GRAD) {
-          kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
+          kwreg::Reg<E, P>::fwd_t(v, t, exr, 1, tw, sync);
           // the D gradients share kappa(|k|) / N: fold it into the spectrum once
 #pragma unroll
           for (int m = 0; m < E / P; ++m)
@@ -404,14 +409,14 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
                 const int r = m * P + k2;
                 y[r] = on ? cconj(kwreg::cmulf(f0s.grad[t + P * m + E * k2], v[r])) : make_float2(0.f, 0.f);
               }
-            rev_store<E, P>(y, t, exr, tw, sync, act, A.bufs[0], base, xs);
+            rev_store<E, P>(y, t, exr, twr, sync, act, A.bufs[0], base, xs);
           }
           // y and z derivatives: their 1-D operators are constant along x and
           // commute with the x transform, so one inverse transform of
           // kappa F / N serves both: out_a = op_a(column) * G
 #pragma unroll
           for (int r = 0; r < E; ++r) v[r] = on ? cconj(v[r]) : make_float2(0.f, 0.f);
-          kwreg::Reg<E, P>::rev(v, t, exr, 1, tw, sync);
+          kwreg::Reg<E, P>::rev_t(v, t, exr, 1, twr, sync);
           if (act) {
 #pragma unroll 1
             for (int a = 1; a < A.ndim; ++a) {
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
           }
         } else if constexpr (KIND == KK_DIV) {
           // item q is the velocity spectrum of axis q; its derivative replaces it
-          kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
+          kwreg::Reg<E, P>::fwd_t(v, t, exr, 1, tw, sync);
           if (q == 0) {
 #pragma unroll
             for (int m = 0; m < E / P; ++m)
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
           store_rev(v, W.inp[q]);
         } else if constexpr (KIND == KK_NAB) {
           // item 0: |k|^pow1 on buffer 0, item 1: |k|^pow2 on buffer 1 (0 at k = 0)
-          kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
+          kwreg::Reg<E, P>::fwd_t(v, t, exr, 1, tw, sync);
           if (q == 0) {
 #pragma unroll
             for (int m = 0; m < E / P; ++m)
@@ -461,7 +466,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
           store_rev(v, W.inp[q]);
         } else {
           // generic operator mode: forward FFT of this input, then every job reading it
-          kwreg::Reg<E, P>::fwd(v, t, exr, 1, tw, sync);
+          kwreg::Reg<E, P>::fwd_t(v, t, exr, 1, tw, sync);
           const int in = W.inp[q];
           int nj = 0, jlast = 0;
           bool all_kappa = true;
@@ -476,7 +481,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
             const AxisJob J = A.jobs[jlast];
             const float2 fcol = col_factor(A, J, g);
             apply_job<E, P>(A, J, t, g, k0s, f0s, fcol, true, on, v, v);
-            rev_store<E, P>(v, t, exr, tw, sync, act, A.bufs[J.out], base, xs);
+            rev_store<E, P>(v, t, exr, twr, sync, act, A.bufs[J.out], base, xs);
             continue;
           }
           if (all_kappa) {
@@ -495,7 +500,7 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
             const float2 fcol = col_factor(A, J, g);
             float2 y[E];
             apply_job<E, P>(A, J, t, g, k0s, f0s, fcol, !all_kappa, on, v, y);
-            rev_store<E, P>(y, t, exr, tw, sync, act, A.bufs[J.out], base, xs);
+            rev_store<E, P>(y, t, exr, twr, sync, act, A.bufs[J.out], base, xs);
           }
         }
       }
@@ -533,7 +538,7 @@ inline int kw_tma_stages(int n, int kind) { return 2; }
 inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
   const int T = kw_tma_tile_cols(n, P, axis, kind), RS = kw_tma_rs(n, E, T), NST = kw_tma_stages(n, kind);
   const size_t nt = (n <= 512 && kind != KK_PLAIN) ? (size_t)n : 0;
-  return sizeof(float2) * ((size_t)NST * n * T + (size_t)T * RS + n + 3 * nt) + sizeof(float) * nt +
+  return sizeof(float2) * ((size_t)NST * n * T + (size_t)T * RS + 2 * (size_t)P * (E + 2) + 3 * nt) + sizeof(float) * nt +
          2 * NST * sizeof(uint64_t) + 16;
 }
 

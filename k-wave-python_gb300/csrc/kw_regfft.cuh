@@ -199,6 +199,70 @@ struct Reg {
     sync();
     Dft<E>::run(v);
   }
+
+  // Per-thread twiddle rows: twf[k1] = W_N^{t k1} (k1 < E) for fwd_t,
+  // twr[m P + n2] = W_N^{n2 (t + P m)} (n2 < P, m < E / P) for rev_t, each row
+  // 16-byte aligned and read two values per load.
+  static constexpr int TW_ROW = E + 2;  // row stride (complex): aligned, bank-spread
+  __device__ __forceinline__ static void build_rows(float2* twf, float2* twr, const float2* tw, int tid, int nthr) {
+    for (int i = tid; i < P * E; i += nthr) {
+      const int t = i / E, k = i - t * E;
+      twf[t * TW_ROW + k] = tw[t * k];
+      const int m = k / P, n2 = k - m * P;
+      twr[t * TW_ROW + k] = tw[n2 * (t + P * m)];
+    }
+  }
+
+  template <class Sync>
+  __device__ __forceinline__ static void fwd_t(float2 (&v)[E], int t, float2* sm, int ss, const float2* twf, Sync sync) {
+    Dft<E>::run(v);
+    const float4* w4 = reinterpret_cast<const float4*>(twf);
+#pragma unroll
+    for (int h = 0; h < E / 2; ++h) {
+      const float4 w = w4[h];
+      if (h > 0) v[2 * h] = cmulf(v[2 * h], make_float2(w.x, w.y));
+      v[2 * h + 1] = cmulf(v[2 * h + 1], make_float2(w.z, w.w));
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) sm[(k1 * (P + 1) + t) * ss] = v[k1];
+    sync();
+#pragma unroll
+    for (int m = 0; m < E / P; ++m) {
+      float2 s[P];
+      const int k1 = t + P * m;
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) s[n2] = sm[(k1 * (P + 1) + n2) * ss];
+      Dft<P>::run(s);
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) v[m * P + k2] = s[k2];
+    }
+    sync();
+  }
+
+  template <class Sync>
+  __device__ __forceinline__ static void rev_t(float2 (&v)[E], int t, float2* sm, int ss, const float2* twr, Sync sync) {
+    const float4* w4 = reinterpret_cast<const float4*>(twr);
+#pragma unroll
+    for (int m = 0; m < E / P; ++m) {
+      float2 s[P];
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) s[k2] = v[m * P + k2];
+      Dft<P>::run(s);
+      const int k1 = t + P * m;
+#pragma unroll
+      for (int h = 0; h < P / 2; ++h) {
+        const float4 w = w4[(m * P) / 2 + h];
+        const int n2 = 2 * h;
+        sm[(n2 * (E + 1) + k1) * ss] = n2 == 0 ? s[n2] : cmulf(s[n2], make_float2(w.x, w.y));
+        sm[((n2 + 1) * (E + 1) + k1) * ss] = cmulf(s[n2 + 1], make_float2(w.z, w.w));
+      }
+    }
+    sync();
+#pragma unroll
+    for (int k1 = 0; k1 < E; ++k1) v[k1] = sm[(t * (E + 1) + k1) * ss];
+    sync();
+    Dft<E>::run(v);
+  }
 };
 
 }  // namespace kwreg
