@@ -53,7 +53,11 @@ bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long 
   KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
   EncodeTiledFn fn = encode_fn();
   if (!fn || !base) return false;
-  const int T = kw_tma_tile_cols(n, P, axis, axis == 1 ? KK_PLAIN : KK_GEN);
+  const int kind = axis == 1 ? KK_PLAIN : KK_GEN;
+  int Ek, Pk;
+  if (!kw_tma_shape(n, kind, &Ek, &Pk)) return false;
+  (void)P;
+  const int T = kw_tma_tile_cols(n, Pk, axis, kind);
   cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)n, (cuuint64_t)nouter};
   cuuint64_t strides[2] = {(cuuint64_t)xs * 8, (cuuint64_t)(nouter > 1 ? os : xs * n) * 8};
   cuuint32_t box[3] = {(cuuint32_t)T, (cuuint32_t)(n < 256 ? n : 256), 1};
@@ -102,8 +106,8 @@ cudaError_t kw_tma_attr(int n, int axis) {
 cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A) {
   KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
   int E, P;
-  if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
   const int kind = A.mode < 2 ? KK_PLAIN : ops_kind(A);
+  if (!kw_tma_shape(n, kind, &E, &P)) return cudaErrorInvalidValue;
   const int T = kw_tma_tile_cols(n, P, axis, kind);
   TmaWork W;
   W.err = device_error_ptr();

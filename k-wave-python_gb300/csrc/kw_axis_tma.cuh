@@ -524,12 +524,26 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
 // launch geometry (shared by the host side of every translation unit)
 // ---------------------------------------------------------------------------
 
+// (E, P) of a pass: plain passes of length 256 use 32 points per thread and 8
+// threads per column (16-column tiles, 128-byte rows); everything else the
+// register-FFT shape of the length (kw_reg_shape).
+inline bool kw_tma_shape(int n, int kind, int* E, int* P) {
+  if (n == 256 && kind == KK_PLAIN) {
+    *E = 32;
+    *P = 8;
+    return true;
+  }
+  return kw_reg_shape(n, E, P);
+}
+
 // Tile width: lengths up to 256 use tiles of 128 / P columns (128 consumer
 // threads plus the producer warp) at three CTAs per SM, which leaves each
 // thread 128 registers; 512 and 1024 use 256 / P columns at one CTA per SM.
 inline bool kw_tma_narrow(int n, int axis, int kind) { return n <= 256; }
 inline int kw_tma_tile_cols(int n, int P, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 128 / P : 256 / P; }
-inline int kw_tma_per_sm(int n, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 3 : 1; }
+inline int kw_tma_per_sm(int n, int axis, int kind) {
+  return (n == 256 && kind == KK_PLAIN) ? 2 : kw_tma_narrow(n, axis, kind) ? 3 : 1;
+}
 
 // Stages of the TMA ring (a third stage measured no faster for the plain passes).
 inline int kw_tma_stages(int n, int kind) { return 2; }
@@ -547,7 +561,9 @@ inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
   switch (n) {                               \
     case 64: return CALL(16, 4, KW_NST_S, 3, 32);   \
     case 128: return CALL(16, 8, KW_NST_S, 3, 16);  \
-    case 256: return CALL(16, 16, KW_NST_S, 3, 8);  \
+    case 256:                                       \
+      if constexpr (KIND == KK_PLAIN) return CALL(32, 8, KW_NST_S, 2, 16); \
+      return CALL(16, 16, KW_NST_S, 3, 8);          \
     case 512: return CALL(32, 16, 2, 1, 16); \
     case 1024: return CALL(32, 32, 2, 1, 8); \
     default: return cudaErrorInvalidValue;   \
@@ -558,7 +574,7 @@ inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
 template <int KIND>
 cudaError_t kw_tma_attr_kind(int n, int axis) {
   int E, P;
-  if (!kw_reg_shape(n, &E, &P)) return cudaErrorInvalidValue;
+  if (!kw_tma_shape(n, KIND, &E, &P)) return cudaErrorInvalidValue;
   const int smem = (int)kw_tma_smem(n, E, P, axis, KIND);
 #define KW_T(E_, P_, S_, B_, T_) \
   cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
