@@ -183,8 +183,8 @@ def measured_peaks():
 # DRAM bytes (read + write) per launch of each kernel class, measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the 256^3 headline
 # workload; profiles/timeloop_256cubed_kernels.md has the capture and command.
-NCU_TRAFFIC_256 = {"rows_rho": 908.3e6, "rows_u": 956.3e6, "rows_eos": 529.7e6, "axis_ops": 268.6e6,
-                   "axis_plain": 263.2e6}
+NCU_TRAFFIC_256 = {"rows_rho": 909.6e6, "rows_u": 956.3e6, "rows_eos": 530.1e6, "axis_ops": 269.2e6,
+                   "axis_plain": 262.7e6}
 
 
 def launch_bytes(S):
