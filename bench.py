@@ -8,7 +8,11 @@ synthetic inputs of those shapes.
 
 A bench "step" is one time step of that simulation over the whole grid
 (16.8 M cells).  ``value`` = cells x timed steps / device time (CUDA events on
-the launching stream), state resident in HBM.  ``e2e`` = the same metric
+the launching stream), state resident in HBM, steps run as ``kw_plan_run``
+runs them (replayed step graphs).  Per-kernel durations for the roofline come
+from a second, instrumented pass over the same steps (every launch bracketed
+by CUDA events).  ``--workload transmit`` measures 128 batched 2-D transmit
+events through ``SimulationBatch`` instead.  ``e2e`` = the same metric
 through the public bridge (``run_gb300_backend``, the kspaceFirstOrder3D
 path) for a full 1000-step simulation from host numpy inputs to host results,
 host set-up and host<->device copies included.
@@ -102,6 +106,71 @@ def config2_problem(n=256, nt=1000, seed=0, plane_z=20, pml=10):
                 alpha_coeff=0.75, alpha_power=1.5, BonA=6.0, p0=p0, smooth_p0=True,
                 sensor_mask=mask, record=("p", "p_max"), pml_size=(pml,) * 3, pml_alpha=(2.0,) * 3,
                 use_sg=True, use_kspace=True)
+
+
+def _five_smooth(lo, hi):
+    out = []
+    for n in range(lo, hi + 1):
+        m = n
+        for f in (2, 3, 5):
+            while m % f == 0:
+                m //= f
+        if m == 1:
+            out.append(n)
+    return out
+
+
+def transmit_problem(shape, seed, nt=2000, dx=5e-5, pml=20, n_elem=32, pitch=4, width=3, cycles=3, f0=1.5e6):
+    """One 2-D transmit event: a seeded speckle medium (c = 1540 (1 + 0.02 N(0,1))
+    m/s, rho = 1000 (1 + 0.02 N(0,1)) kg/m^3) with 3 random discs of +-10 % c,
+    power-law absorption 0.5 dB/(MHz^y cm) with y = 1.1, a linear array of
+    ``n_elem`` elements (``width`` px wide, ``pitch`` px apart, two points
+    inside the PML edge along x) driving a ``cycles``-cycle ``f0`` tone burst
+    (Gaussian envelope) steered at a random angle in [-30, 30] degrees as an
+    additive (k-space corrected) pressure source, and the array's points as a
+    binary sensor recording p.  dt from the CFL-0.3 rule at the maximum sound speed."""
+    rng = np.random.default_rng(seed)
+    nx, ny = shape
+    c = 1540.0 * (1 + 0.02 * rng.standard_normal(shape))
+    rho = 1000.0 * (1 + 0.02 * rng.standard_normal(shape))
+    gx, gy = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    for _ in range(3):
+        cx, cy = rng.uniform(pml + 10, nx - pml - 10), rng.uniform(pml + 10, ny - pml - 10)
+        r = rng.uniform(5, 20)
+        c[(gx - cx) ** 2 + (gy - cy) ** 2 <= r * r] *= 1 + rng.choice([-0.1, 0.1])
+    dt = 0.3 * dx / float(c.max())
+    x0 = pml + 2
+    aperture = n_elem * pitch
+    y0 = (ny - aperture) // 2
+    theta = np.deg2rad(rng.uniform(-30, 30))
+    yc = (np.arange(n_elem) * pitch + 0.5 * width) * dx
+    delays = (yc - yc.mean()) * np.sin(theta) / 1540.0
+    delays -= delays.min()
+    burst = cycles / f0
+    length = int(np.ceil((burst + delays.max()) / dt)) + 1
+    t = np.arange(length) * dt
+    mask = np.zeros(shape, bool)
+    elem_of = np.full(shape, -1)
+    for e in range(n_elem):
+        ys = slice(y0 + e * pitch, y0 + e * pitch + width)
+        mask[x0, ys] = True
+        elem_of[x0, ys] = e
+    points = elem_of[mask]  # element of each source point, C order
+    tt = t[None, :] - delays[points][:, None]
+    env = np.exp(-((tt - burst / 2) / (burst / 4)) ** 2) * ((tt >= 0) & (tt <= burst))
+    sig = 1e4 * env * np.sin(2 * np.pi * f0 * tt)
+    return dict(shape=tuple(shape), spacing=(dx, dx), dt=dt, Nt=nt, sound_speed=c, density=rho,
+                alpha_coeff=0.5, alpha_power=1.1, p_mask=mask, p=sig, p_mode="additive", sensor_mask=mask.copy(),
+                record=("p",), pml_size=(pml, pml), pml_alpha=(2.0, 2.0), use_sg=True, use_kspace=True, smooth_p0=False)
+
+
+def config3_problems(n_inst=128, nt=2000, seed=0, sizes=None):
+    """``n_inst`` transmit events with grid sizes drawn from the 5-smooth sizes in
+    [192, 512] per axis (20-point PML inside), dx = 0.05 mm."""
+    rng = np.random.default_rng(seed)
+    sizes = sizes or _five_smooth(192, 512)
+    return [transmit_problem((int(rng.choice(sizes)), int(rng.choice(sizes))), seed * 100003 + i, nt=nt)
+            for i in range(n_inst)]
 
 
 def kwave_objects(prob):
@@ -302,9 +371,9 @@ def run_gb300(args):
     torch.cuda.synchronize()
     cnt0 = C_int64()
     lib.kw_plan_launch_count(plan.handle, ctypes.byref(cnt0))
-    K.check(lib.kw_plan_set_timing(plan.handle, 1))
     barrier()
     torch.cuda.synchronize()
+    # timed region: K steps as kw_plan_run runs them (replayed step graphs)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         ev0.record(stream)
@@ -315,6 +384,17 @@ def run_gb300(args):
     ms = ev0.elapsed_time(ev1)
     cnt1 = C_int64()
     lib.kw_plan_launch_count(plan.handle, ctypes.byref(cnt1))
+    # instrumented pass over the same steps: every launch bracketed by CUDA
+    # events on the launching stream, for the per-kernel durations
+    K.check(lib.kw_plan_reset(plan.handle))
+    plan.run(W)
+    torch.cuda.synchronize()
+    K.check(lib.kw_plan_set_timing(plan.handle, 1))
+    ev0.record(stream)
+    plan.run(K_steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_instr = ev0.elapsed_time(ev1)
     kms = (ctypes.c_double * 6)()
     kcnt = (ctypes.c_int64 * 6)()
     K.check(lib.kw_plan_read_timing(plan.handle, kms, kcnt))
@@ -384,6 +464,9 @@ def run_gb300(args):
         "step_roofline": {"model_bytes_per_cell_step": A_MODEL_BYTES_PER_CELL_STEP, "achieved": step_gbs,
                           "peak": peak, "frac": step_gbs / peak, "unit": "GB/s"},
         "kernels": kernels,
+        "instrumented_pass": {"ms_per_step": ms_instr / K_steps,
+                              "note": "the same K steps as plain launches, each bracketed by CUDA events: source of "
+                                      "the per-kernel durations in roofline and kernels"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk.summary(),
@@ -392,6 +475,110 @@ def run_gb300(args):
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+TRANSMIT_WORKLOAD = ("batched 2-D transmit events: 128 simulations, grid sizes drawn from the 5-smooth sizes in "
+                     "[192,512]^2 incl. 20-pt PML, dx=0.05 mm, speckle c/rho +-2 % + 3 discs +-10 % c, power law "
+                     "0.5 dB/(MHz^y cm) y=1.1, 32-element array, steered 3-cycle 1.5 MHz burst (additive source), "
+                     "array points recording p, 2000 steps")
+TRANSMIT_A_MODEL = 132  # algorithmic bytes per cell-step of this configuration
+
+
+def run_transmit(args):
+    """Batched 2-D transmit events through ``SimulationBatch``: every step of
+    all members is one graph launch.  ``value`` = summed cells x timed steps /
+    device time; ``one_by_one`` = the same members and steps run one simulation
+    after another on the same stream; ``e2e`` = problem dicts in, results out
+    (set-up, uploads, the whole run and the result reads) for the full batch."""
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300 import _lib as K
+    from kwave_gb300.solver import SimulationBatch, run_batch
+
+    ninst, K_steps, W = args.instances, args.steps, args.warmup
+    nt = max(2000, W + K_steps + 1)
+    probs = config3_problems(ninst, nt=nt, seed=1)
+    cells = sum(int(np.prod(p["shape"])) for p in probs)
+    stream = torch.cuda.current_stream()
+    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream)
+    lib = K.lib()
+
+    def launches():
+        tot = 0
+        for s in b.sims:
+            c = C_int64()
+            lib.kw_plan_launch_count(s._plan.handle, ctypes.byref(c))
+            tot += c.value
+        return tot
+
+    b.run_steps(W)
+    torch.cuda.synchronize()
+    l0 = launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        b.run_steps(K_steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    nlaunch = launches() - l0
+    value = cells * K_steps / (ms / 1e3) / 1e6
+    # the same members one after another (each with its own step graphs)
+    k1 = min(K_steps, 100)
+    ev0.record(stream)
+    for s in b.sims:
+        s._plan.run(k1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms1 = ev0.elapsed_time(ev1)
+    one_by_one = cells * k1 / (ms1 / 1e3) / 1e6
+    b.close()
+    del b
+    e2e = None
+    if not args.no_e2e:
+        probs_e2e = config3_problems(ninst, nt=2000, seed=2)
+        cells_e2e = sum(int(np.prod(p["shape"])) for p in probs_e2e)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = run_batch(probs_e2e)
+        t1 = time.perf_counter()
+        assert len(res) == ninst and all(r["p"].shape[1] == 2000 for r in res)
+        h2d = sum(sum(np.asarray(v).nbytes for v in (p["sound_speed"], p["density"], p["p"], p["p_mask"]))
+                  for p in probs_e2e)
+        d2h = sum(r["p"].nbytes for r in res)
+        e2e = {"value": cells_e2e * 2000 / (t1 - t0) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d / 2000,
+               "d2h_bytes_per_step": d2h / 2000, "seconds": t1 - t0}
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle.kspace_oracle import OracleSimulation
+
+        prob = transmit_problem((352, 352), 7, nt=40)
+        sim = OracleSimulation(prob, dtype=np.float32).setup()
+        sim.step()
+        t0 = time.perf_counter()
+        for _ in range(30):
+            sim.step()
+        secs = time.perf_counter() - t0
+        cpu = {"value": 352 * 352 * 30 / secs / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"30 steps of one 352^2 transmit event ({secs:.1f} s), oracle restatement, single-threaded"}
+    peak, peak_kind = measured_peaks()
+    step_gbs = TRANSMIT_A_MODEL * cells * K_steps / (ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K_steps, "warmup": W,
+        "ms_per_step": ms / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded speckle media, discs, steering angles and grid sizes of the named ranges)",
+        "config": {"workload": TRANSMIT_WORKLOAD, "instances": ninst, "cells_per_step": cells, "nt": nt,
+                   "l2": f"inputs larger than L2 ({cells * 4 * 12 / 1e9:.1f} GB of state, medium and spectra)"},
+        "step_roofline": {"model_bytes_per_cell_step": TRANSMIT_A_MODEL, "achieved": step_gbs, "peak": peak,
+                          "frac": step_gbs / peak, "unit": "GB/s", "peak_source": peak_kind},
+        "one_by_one": {"value": one_by_one, "unit": UNIT, "steps": k1},
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(), "gpu_launches": int(nlaunch),
+    }
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -409,11 +596,16 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=256, help="grid edge (the headline workload is 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit"],
+                    help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events")
+    ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "transmit":
+        return run_transmit(args)
     return run_gb300(args)
 
 

@@ -137,8 +137,25 @@ int32_t kw_plan_derive_medium(kw_plan* plan, int32_t what, const float* alpha, i
 /* Allocates device memory, uploads all inputs and resets the state to t = 0. */
 int32_t kw_plan_finalize(kw_plan* plan);
 /* Advances min(nsteps, Nt - t) steps of Simulation.step (kspace_solver.py:691-747)
- * on `stream` (a cudaStream_t, NULL = default stream); returns after enqueueing. */
+ * on `stream` (a cudaStream_t, NULL = default stream); returns after enqueueing.
+ * Steps with the same launch sequence run as one CUDA graph, captured on first
+ * use and replayed with the step index held on the device; the last step of a
+ * call, the t = 0 initial-condition step and every step while timing is on are
+ * plain launches.  Use one stream per plan. */
 int32_t kw_plan_run(kw_plan* plan, int32_t nsteps, void* stream);
+/* enable == 0: every step as plain launches (default 1; the environment
+ * variable KWAVE_GB300_GRAPHS=0 sets 0 at kw_plan_finalize). */
+int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);
+/* Batch of independent finalized plans (any sizes, media, sources, sensors;
+ * no counterpart in the reference, which runs one Simulation at a time).
+ * kw_batch_run advances every plan by min(nsteps, Nt - t) steps; each step of
+ * all plans whose steps are graph steps is ONE graph launch holding the plans'
+ * step graphs as parallel branches.  Plans keep their own state, results and
+ * read functions.  Destroy the batch before its plans. */
+typedef struct kw_batch kw_batch;
+int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out);
+int32_t kw_batch_run(kw_batch* batch, int32_t nsteps, void* stream);
+int32_t kw_batch_destroy(kw_batch* batch);
 /* Waits for the plan's work on `stream`. */
 int32_t kw_plan_sync(kw_plan* plan, void* stream);
 /* Current step index t. */

@@ -223,11 +223,12 @@ __device__ __forceinline__ float fld(const float* p, float s, long long g) { ret
 
 // Apply a sparse source to rbuf for the block's rows (kspace_solver.py:86-109).
 __device__ void apply_source(const RowsParams& P, const KwSrcDev& S, float* rbuf, int r0, int nr) {
-  if (!S.active || P.t >= S.len) return;
+  const int t = kw_step_t(P);
+  if (!S.active || t >= S.len) return;
   const int e0 = S.row_ptr[r0], e1 = S.row_ptr[r0 + nr];
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int4 en = S.ent[e];
-    const float val = S.sig[(long long)P.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+    const float val = S.sig[(long long)t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
     float& f = rbuf[(en.x - r0) * P.L + en.y];
     if (S.mode == SRC_DIRICHLET)
       f = val;
@@ -239,17 +240,19 @@ __device__ void apply_source(const RowsParams& P, const KwSrcDev& S, float* rbuf
 // Scatter a source's values at step t into a zeroed rbuf (the field whose
 // k-space corrected version is added, kspace_solver.py:93-101).
 __device__ void scatter_source(const RowsParams& P, const KwSrcDev& S, float* rbuf, int r0, int nr) {
+  const int t = kw_step_t(P);
   const int e0 = S.row_ptr[r0], e1 = S.row_ptr[r0 + nr];
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int4 en = S.ent[e];
-    rbuf[(en.x - r0) * P.L + en.y] = S.sig[(long long)P.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+    rbuf[(en.x - r0) * P.L + en.y] = S.sig[(long long)t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
   }
 }
 
 __device__ void record_samples(const RowsParams& P, const float* rbuf, float* rec, int r0, int nr) {
-  if (rec == nullptr || P.rec_row < 0 || P.sens_row_ptr == nullptr) return;
+  const int rr = kw_rec_row(P);
+  if (rec == nullptr || rr < 0 || P.sens_row_ptr == nullptr) return;
   const int e0 = P.sens_row_ptr[r0], e1 = P.sens_row_ptr[r0 + nr];
-  float* out = rec + (long long)P.rec_row * P.nslots;
+  float* out = rec + (long long)rr * P.nslots;
   for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int4 en = P.sens_ent[e];
     out[en.z] = rbuf[(en.x - r0) * P.L + en.y];
@@ -678,6 +681,17 @@ cudaError_t kw_axis_reg_launch(int n, dim3 grid, size_t smem, cudaStream_t st, c
 #undef KW_A
 }
 
+
+// ---------------------------------------------------------------------------
+// device step counter of replayed step graphs
+// ---------------------------------------------------------------------------
+__global__ void k_step_set(int* tdev, int t) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *tdev = t;
+}
+
+__global__ void k_step_tick(int* tdev) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *tdev += 1;
+}
 
 // ---------------------------------------------------------------------------
 // p0 smoothing helpers (kwave/utils/filters.py:613-614, restore_max)

@@ -88,7 +88,14 @@ struct RowsParams {
   const int4* sens_ent;   // (row, pos, slot, 0)
   int nslots;
   float* rec[7];
+  // inside a replayed step graph: the plan's device step counter; t and
+  // rec_row are then offsets added to it (nullptr: t and rec_row as given)
+  const int* tdev;
 };
+
+// step index and record column of a row-stage launch
+__device__ __forceinline__ int kw_step_t(const RowsParams& P) { return P.tdev ? P.t + *P.tdev : P.t; }
+__device__ __forceinline__ int kw_rec_row(const RowsParams& P) { return P.tdev ? P.rec_row + *P.tdev : P.rec_row; }
 
 struct AxisJob {
   int in, out, op, axis;
@@ -182,6 +189,10 @@ __device__ __forceinline__ float window_at(const float* tab, int n, float rad, f
 __global__ void k_absmax(const float* __restrict__ x, long long n, unsigned int* out);
 // out = a / b for two float bit patterns (restore-max factor)
 __global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out);
+// device step counter of a plan: set before a run of graph steps, advanced by
+// the last node of each step graph
+__global__ void k_step_set(int* tdev, int t);
+__global__ void k_step_tick(int* tdev);
 // Medium grids derived on the device (kw_plan_derive_medium); any output may be null.
 struct DeriveParams {
   int ndim, N[3];

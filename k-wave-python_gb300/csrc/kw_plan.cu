@@ -119,6 +119,20 @@ struct kw_plan {
   unsigned int* d_maxes = nullptr;
   // per-step flags passed to the row stages
   int srcp_on = 0, srcu_on[3] = {0, 0, 0}, rec_us = 0, init_r2c = 0;
+  // step graphs: one captured step per distinct launch sequence, replayed with
+  // the step index read from d_tstep
+  struct StepGraph {
+    int key;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    long long nlaunch;
+  };
+  std::vector<StepGraph> graphs;
+  bool use_graphs = true;
+  bool capturing = false;
+  int* d_tstep = nullptr;
+  int tstep_val = -1;  // value d_tstep holds once the stream reaches the last enqueued work
+  cudaStream_t cap_stream = nullptr;
   // launch accounting / timing
   long long launches = 0;
   bool timing = false;
@@ -619,6 +633,11 @@ int32_t kw_plan_finalize(kw_plan* p) {
       }
     }
   }
+  if ((rc = dalloc(p, &p->d_tstep, 1))) return rc;
+  {
+    const char* env = getenv("KWAVE_GB300_GRAPHS");
+    if (env && env[0] == '0') p->use_graphs = false;
+  }
   CK(cudaDeviceSynchronize());
   p->finalized = true;
   p->t = 0;
@@ -721,6 +740,12 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   P.init = init;
   P.t = t;
   P.rec_row = (t >= p->g.record_start) ? t - p->g.record_start : -1;
+  if (p->capturing) {
+    // replayed for other steps: the step index comes from the device counter
+    P.tdev = p->d_tstep;
+    P.t = 0;
+    P.rec_row = (t >= p->g.record_start) ? -p->g.record_start : -(1 << 30);
+  }
   P.write_p = write_p;
   P.srcp_on = p->srcp_on;
   for (int a = 0; a < 3; ++a) P.srcu_on[a] = p->srcu_on[a];
@@ -981,6 +1006,93 @@ static int enqueue_step(kw_plan* p, int t, bool last, cudaStream_t st) {
   return KW_OK;
 }
 
+// ---------------------------------------------------------------------------
+// step graphs
+// ---------------------------------------------------------------------------
+// Launch sequence of step t as a key: two steps with the same key launch the
+// same kernels with the same arguments apart from the step index, which the
+// row stages of a captured step read from the device counter.
+static int step_key(kw_plan* p, int t) {
+  set_step_flags(p, t);
+  return p->srcp_on | (p->srcu_on[0] << 1) | (p->srcu_on[1] << 2) | (p->srcu_on[2] << 3) | (p->rec_us << 4) |
+         ((t >= p->g.record_start ? 1 : 0) << 7);
+}
+
+// Steps that run as plain launches: the last step of a run (it writes p to
+// real space), the t = 0 initial-condition override, and every step while
+// per-launch timing is on.
+static bool step_eager(const kw_plan* p, int t, int end) {
+  return !p->use_graphs || p->timing || t == end - 1 || (t == 0 && !p->hfield[KW_F_P0].empty());
+}
+
+static void drop_graphs(kw_plan* p) {
+  for (auto& g : p->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
+  p->graphs.clear();
+}
+
+// Captured step graph for the key of step t (captured on first use).
+static int step_graph(kw_plan* p, int t, kw_plan::StepGraph** out) {
+  const int key = step_key(p, t);
+  for (auto& g : p->graphs)
+    if (g.key == key) {
+      *out = &g;
+      return KW_OK;
+    }
+  if (!p->cap_stream) CK(cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking));
+  const long long l0 = p->launches;
+  CK(cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeRelaxed));
+  p->capturing = true;
+  int rc = enqueue_step(p, t, false, p->cap_stream);
+  p->capturing = false;
+  if (!rc) {
+    k_step_tick<<<1, 1, 0, p->cap_stream>>>(p->d_tstep);
+    if (cudaGetLastError() != cudaSuccess) rc = fail(KW_ERR_CUDA, "step counter launch failed during capture");
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(p->cap_stream, &graph);
+  const long long nl = p->launches - l0 + 1;
+  p->launches = l0;
+  if (!rc && ec != cudaSuccess) rc = fail(KW_ERR_CUDA, "step capture: %s", cudaGetErrorString(ec));
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(KW_ERR_CUDA, "step graph instantiation: %s", cudaGetErrorString(ei));
+  }
+  p->graphs.push_back(kw_plan::StepGraph{key, graph, exec, nl});
+  *out = &p->graphs.back();
+  return KW_OK;
+}
+
+// Point the device counter at step t (if the stream will not already hold t there).
+static int step_counter_to(kw_plan* p, int t, cudaStream_t st) {
+  if (p->tstep_val == t) return KW_OK;
+  k_step_set<<<1, 1, 0, st>>>(p->d_tstep, t);
+  CK(cudaGetLastError());
+  p->launches++;
+  p->tstep_val = t;
+  return KW_OK;
+}
+
+static int run_step(kw_plan* p, int t, int end, cudaStream_t st) {
+  if (step_eager(p, t, end)) return enqueue_step(p, t, t == end - 1, st);
+  kw_plan::StepGraph* g = nullptr;
+  int rc = step_graph(p, t, &g);
+  if (!rc) rc = step_counter_to(p, t, st);
+  if (rc) return rc;
+  CK(cudaGraphLaunch(g->exec, st));
+  p->tstep_val = t + 1;
+  p->launches += g->nlaunch;
+  return KW_OK;
+}
+
 int32_t kw_plan_run(kw_plan* p, int32_t nsteps, void* stream) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");
   if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_run before kw_plan_finalize");
@@ -988,10 +1100,130 @@ int32_t kw_plan_run(kw_plan* p, int32_t nsteps, void* stream) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int end = std::min(p->g.Nt, p->t + nsteps);
   for (int t = p->t; t < end; ++t) {
-    int rc = enqueue_step(p, t, t == end - 1, st);
+    int rc = run_step(p, t, end, st);
     if (rc) return rc;
+    p->t = t + 1;
   }
-  p->t = end;
+  return KW_OK;
+}
+
+int32_t kw_plan_set_graphs(kw_plan* p, int32_t enable) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  p->use_graphs = enable != 0;
+  return KW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batches: several plans advanced together, one graph launch per step
+// ---------------------------------------------------------------------------
+struct kw_batch {
+  std::vector<kw_plan*> plans;
+  struct Graph {
+    std::vector<int> keys;  // per plan: step key, or -1 when the plan does not step
+    cudaGraphExec_t exec;
+  };
+  std::vector<Graph> graphs;
+};
+
+int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
+  if (!out || n < 1 || !plans) return fail(KW_ERR_INVALID, "kw_batch_create: need at least one plan");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!plans[i]) return fail(KW_ERR_INVALID, "kw_batch_create: plan %d is null", i);
+    if (!plans[i]->finalized) return fail(KW_ERR_STATE, "kw_batch_create: plan %d is not finalized", i);
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return fail(KW_ERR_INVALID, "kw_batch_create: plan %d given twice", i);
+  }
+  kw_batch* b = new kw_batch;
+  b->plans.assign(plans, plans + n);
+  *out = b;
+  return KW_OK;
+}
+
+static int batch_graph(kw_batch* b, const std::vector<int>& keys, const std::vector<kw_plan::StepGraph*>& sg,
+                       cudaGraphExec_t* exec) {
+  for (auto& g : b->graphs)
+    if (g.keys == keys) {
+      *exec = g.exec;
+      return KW_OK;
+    }
+  cudaGraph_t graph = nullptr;
+  CK(cudaGraphCreate(&graph, 0));
+  for (size_t i = 0; i < keys.size(); ++i) {
+    if (keys[i] < 0) continue;
+    cudaGraphNode_t node;
+    const cudaError_t e = cudaGraphAddChildGraphNode(&node, graph, nullptr, 0, sg[i]->graph);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return fail(KW_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+    }
+  }
+  const cudaError_t ei = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return fail(KW_ERR_CUDA, "batch graph instantiation: %s", cudaGetErrorString(ei));
+  b->graphs.push_back(kw_batch::Graph{keys, *exec});
+  return KW_OK;
+}
+
+int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
+  if (!b) return fail(KW_ERR_INVALID, "null batch");
+  if (nsteps < 0) return fail(KW_ERR_INVALID, "nsteps < 0");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const size_t n = b->plans.size();
+  std::vector<int> end(n), keys(n);
+  std::vector<kw_plan::StepGraph*> sg(n, nullptr);
+  int span = 0;
+  for (size_t i = 0; i < n; ++i) {
+    kw_plan* p = b->plans[i];
+    end[i] = std::min(p->g.Nt, p->t + nsteps);
+    span = std::max(span, end[i] - p->t);
+  }
+  for (int s = 0; s < span; ++s) {
+    bool together = true;
+    for (size_t i = 0; i < n; ++i) {
+      kw_plan* p = b->plans[i];
+      keys[i] = -1;
+      if (p->t >= end[i]) continue;
+      if (step_eager(p, p->t, end[i])) {
+        together = false;
+        continue;
+      }
+      int rc = step_graph(p, p->t, &sg[i]);
+      if (rc) return rc;
+      keys[i] = sg[i]->key;
+    }
+    int rc;
+    if (!together) {
+      // a step with plain launches somewhere: each plan on its own, in order
+      for (size_t i = 0; i < n; ++i) {
+        kw_plan* p = b->plans[i];
+        if (p->t >= end[i]) continue;
+        if ((rc = run_step(p, p->t, end[i], st))) return rc;
+        p->t += 1;
+      }
+      continue;
+    }
+    for (size_t i = 0; i < n; ++i)
+      if (keys[i] >= 0 && (rc = step_counter_to(b->plans[i], b->plans[i]->t, st))) return rc;
+    cudaGraphExec_t exec = nullptr;
+    if ((rc = batch_graph(b, keys, sg, &exec))) return rc;
+    CK(cudaGraphLaunch(exec, st));
+    for (size_t i = 0; i < n; ++i) {
+      if (keys[i] < 0) continue;
+      kw_plan* p = b->plans[i];
+      p->tstep_val = p->t + 1;
+      p->launches += sg[i]->nlaunch;
+      p->t += 1;
+    }
+  }
+  return KW_OK;
+}
+
+int32_t kw_batch_destroy(kw_batch* b) {
+  if (!b) return KW_OK;
+  for (auto& g : b->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  delete b;
   return KW_OK;
 }
 
@@ -1152,6 +1384,8 @@ int32_t kw_plan_launch_count(const kw_plan* p, int64_t* count) {
 int32_t kw_plan_destroy(kw_plan* p) {
   if (!p) return KW_OK;
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  drop_graphs(p);
+  if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
   if (p->tma) kw_tma_plan_destroy(p->tma);
   for (void* a : p->allocs) cudaFree(a);
   delete p;

@@ -96,14 +96,15 @@ struct RowCtx {
 
   // sparse source on this row (kspace_solver.py:86-109): owner thread updates its pair
   __device__ __forceinline__ void source(const KwSrcDev& S, float2 (&v)[E]) const {
-    if (!S.active || Q.t >= S.len || !ok) return;
+    const int ts = kw_step_t(Q);
+    if (!S.active || ts >= S.len || !ok) return;
     const int e0 = S.row_ptr[grow], e1 = S.row_ptr[grow + 1];
     for (int e = e0; e < e1; ++e) {
       const int4 en = S.ent[e];
       const int n = en.y >> 1;
       if ((n % P) != t) continue;
       const int jj = n / P;
-      const float val = S.sig[(long long)Q.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+      const float val = S.sig[(long long)ts * S.nsig + (S.nsig == 1 ? 0 : en.z)];
 #pragma unroll
       for (int j = 0; j < E; ++j)
         if (j == jj) {
@@ -119,13 +120,14 @@ struct RowCtx {
 #pragma unroll
     for (int j = 0; j < E; ++j) v[j] = make_float2(0.f, 0.f);
     if (!ok) return;
+    const int ts = kw_step_t(Q);
     const int e0 = S.row_ptr[grow], e1 = S.row_ptr[grow + 1];
     for (int e = e0; e < e1; ++e) {
       const int4 en = S.ent[e];
       const int n = en.y >> 1;
       if ((n % P) != t) continue;
       const int jj = n / P;
-      const float val = S.sig[(long long)Q.t * S.nsig + (S.nsig == 1 ? 0 : en.z)];
+      const float val = S.sig[(long long)ts * S.nsig + (S.nsig == 1 ? 0 : en.z)];
 #pragma unroll
       for (int j = 0; j < E; ++j)
         if (j == jj) {
@@ -138,9 +140,10 @@ struct RowCtx {
   }
 
   __device__ __forceinline__ void record(const float2 (&v)[E], float* rec) const {
-    if (rec == nullptr || Q.rec_row < 0 || Q.sens_row_ptr == nullptr || !ok) return;
+    const int rr = kw_rec_row(Q);
+    if (rec == nullptr || rr < 0 || Q.sens_row_ptr == nullptr || !ok) return;
     const int e0 = Q.sens_row_ptr[grow], e1 = Q.sens_row_ptr[grow + 1];
-    float* out = rec + (long long)Q.rec_row * Q.nslots;
+    float* out = rec + (long long)rr * Q.nslots;
     for (int e = e0; e < e1; ++e) {
       const int4 en = Q.sens_ent[e];
       const int n = en.y >> 1;

@@ -11,7 +11,9 @@ Entry points:
     (``kwave.kspaceFirstOrder.kspaceFirstOrder``) for ``backend="gb300"``;
   * ``backend.kspaceFirstOrder2D`` / ``3D`` — the legacy signatures;
   * ``reconstruction.TimeReversal`` — time-reversal reconstruction, with
-    ``conversion.cart2grid`` for Cartesian sensors.
+    ``conversion.cart2grid`` for Cartesian sensors;
+  * ``solver.SimulationBatch`` / ``solver.run_batch`` — many independent
+    simulations of any sizes advanced together, one graph launch per step.
 """
 __version__ = "0.1.0"
 
@@ -19,5 +21,5 @@ from .backend import (BACKEND, execution_options, install, kspaceFirstOrder2D, k
                       run_gb300_backend, uninstall)
 from .conversion import cart2grid  # noqa: F401
 from .reconstruction import TimeReversal  # noqa: F401
-from .solver import Simulation, run_problem  # noqa: F401
+from .solver import Simulation, SimulationBatch, run_batch, run_problem  # noqa: F401
 from .unified import get_optimal_pml_size, kspaceFirstOrder, reshape_to_grid  # noqa: F401

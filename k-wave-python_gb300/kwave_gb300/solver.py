@@ -139,6 +139,10 @@ class DevicePlan:
         st = C.c_void_p(self.stream) if self.stream is not None else None
         K.check(self.lib.kw_plan_sync(self._h, st))
 
+    def set_graphs(self, enable):
+        """Run repeated steps as replayed CUDA graphs (default) or as plain launches."""
+        K.check(self.lib.kw_plan_set_graphs(self._h, int(bool(enable))))
+
     def time_index(self):
         t = C.c_int32()
         K.check(self.lib.kw_plan_time_index(self._h, C.byref(t)))
@@ -301,6 +305,72 @@ def acoustic_intensity(result):
         out[f"I{a}"] = p * us
         out[f"I{a}_avg"] = np.mean(out[f"I{a}"], axis=-1)
     return out
+
+
+class SimulationBatch:
+    """Independent simulations advanced together on one stream (kw_batch).
+
+    Each member keeps its own grid size, medium, sources, sensor and results;
+    every step of all members is one CUDA graph launch whose parallel branches
+    are the members' step graphs.  The reference has no batch object: it runs
+    ``Simulation.run()`` (kwave/solvers/kspace_solver.py:749-778) once per
+    simulation, and so does a loop over members here, with the same results.
+    """
+
+    def __init__(self, sims, stream=None):
+        self.sims = list(sims)
+        if not self.sims:
+            raise ValueError("SimulationBatch needs at least one simulation")
+        self.stream = stream
+        for s in self.sims:
+            if s._plan is None:
+                s.stream = stream
+                s.setup()
+        lib = K.lib()
+        self.lib = lib
+        handles = (C.c_void_p * len(self.sims))(*[s._plan.handle for s in self.sims])
+        self._h = C.c_void_p()
+        K.check(lib.kw_batch_create(handles, len(self.sims), C.byref(self._h)))
+
+    @classmethod
+    def from_problems(cls, problems, stream=None):
+        return cls([Simulation.from_problem(p, stream=stream) for p in problems], stream=stream)
+
+    def run_steps(self, nsteps):
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        K.check(self.lib.kw_batch_run(self._h, int(nsteps), st))
+        for s in self.sims:
+            s.t = s._plan.time_index()
+
+    def run(self):
+        """Run every member to its Nt and return the list of result dictionaries."""
+        self.run_steps(max(s.S.Nt - s.t for s in self.sims))
+        self.sims[0]._plan.sync()
+        return [s.results() for s in self.sims]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kw_batch_destroy(self._h)
+            self._h = None
+        for s in self.sims:
+            s.close()
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                self.lib.kw_batch_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def run_batch(problems, stream=None):
+    """Set up, run together and close the simulations described by plain problem dicts."""
+    b = SimulationBatch.from_problems(problems, stream=stream)
+    try:
+        return b.run()
+    finally:
+        b.close()
 
 
 def run_problem(prob, stream=None):
