@@ -496,7 +496,6 @@ def run_transmit(args):
     import __graft_entry__ as g
 
     g.build()
-    from kwave_gb300 import _lib as K
     from kwave_gb300.solver import SimulationBatch, run_batch
 
     ninst, K_steps, W = args.instances, args.steps, args.warmup
@@ -504,16 +503,10 @@ def run_transmit(args):
     probs = config3_problems(ninst, nt=nt, seed=1)
     cells = sum(int(np.prod(p["shape"])) for p in probs)
     stream = torch.cuda.current_stream()
-    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream)
-    lib = K.lib()
+    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped)
 
     def launches():
-        tot = 0
-        for s in b.sims:
-            c = C_int64()
-            lib.kw_plan_launch_count(s._plan.handle, ctypes.byref(c))
-            tot += c.value
-        return tot
+        return b.launch_count()
 
     b.run_steps(W)
     torch.cuda.synchronize()
@@ -527,17 +520,27 @@ def run_transmit(args):
     ms = ev0.elapsed_time(ev1)
     nlaunch = launches() - l0
     value = cells * K_steps / (ms / 1e3) / 1e6
-    # the same members one after another (each with its own step graphs)
+    b.close()
+    del b
+    # the same members one after another, each with the kernels picked for its
+    # grid and its own step graphs
+    from kwave_gb300.solver import Simulation
+
     k1 = min(K_steps, 100)
+    sims = [Simulation.from_problem(p, stream=stream.cuda_stream).setup() for p in probs]
+    for s in sims:
+        s._plan.run(W)
+    torch.cuda.synchronize()
     ev0.record(stream)
-    for s in b.sims:
+    for s in sims:
         s._plan.run(k1)
     ev1.record(stream)
     torch.cuda.synchronize()
     ms1 = ev0.elapsed_time(ev1)
     one_by_one = cells * k1 / (ms1 / 1e3) / 1e6
-    b.close()
-    del b
+    for s in sims:
+        s.close()
+    del sims
     e2e = None
     if not args.no_e2e:
         probs_e2e = config3_problems(ninst, nt=2000, seed=2)
@@ -572,6 +575,7 @@ def run_transmit(args):
         "ms_per_step": ms / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded speckle media, discs, steering angles and grid sizes of the named ranges)",
         "config": {"workload": TRANSMIT_WORKLOAD, "instances": ninst, "cells_per_step": cells, "nt": nt,
+                   "batch": "grouped launches" if args.grouped else "members as parallel graph branches",
                    "l2": f"inputs larger than L2 ({cells * 4 * 12 / 1e9:.1f} GB of state, medium and spectra)"},
         "step_roofline": {"model_bytes_per_cell_step": TRANSMIT_A_MODEL, "achieved": step_gbs, "peak": peak,
                           "frac": step_gbs / peak, "unit": "GB/s", "peak_source": peak_kind},
@@ -599,6 +603,7 @@ def main(argv=None):
     ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit"],
                     help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events")
     ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
+    ap.add_argument("--grouped", action="store_true", help="transmit workload: grouped launches across members")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

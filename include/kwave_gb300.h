@@ -42,9 +42,14 @@ typedef struct kw_grid_desc {
   int32_t absorb_mode;   /* 0 none, 1 power law (fractional Laplacian), 2 Stokes (y = 2) */
   int32_t dispersion;    /* 1: power-law dispersion term enabled (kspace_solver.py:500-524) */
   int32_t nonlinear;     /* 1: B/A enabled (kspace_solver.py:526-550) */
-  int32_t reserved;
+  int32_t flags;         /* KW_DESC_* bits */
   double alpha_power;    /* y */
 } kw_grid_desc;
+
+/* kw_grid_desc.flags: run every pass with the shared-memory FFT kernels that
+ * take their length at run time, so that kw_batch can fold the plan's passes
+ * into grouped launches with other plans of any size. */
+enum { KW_DESC_GENERIC_FFT = 1 };
 
 /* Grid-valued inputs.  n == 0 (or host == NULL) selects the scalar. */
 enum {
@@ -149,12 +154,17 @@ int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);
 /* Batch of independent finalized plans (any sizes, media, sources, sensors;
  * no counterpart in the reference, which runs one Simulation at a time).
  * kw_batch_run advances every plan by min(nsteps, Nt - t) steps; each step of
- * all plans whose steps are graph steps is ONE graph launch holding the plans'
- * step graphs as parallel branches.  Plans keep their own state, results and
- * read functions.  Destroy the batch before its plans. */
+ * all plans whose steps are graph steps is ONE graph launch.  Inside it the
+ * passes of plans created with KW_DESC_GENERIC_FFT are grouped: the k-th
+ * launch of every such plan's step runs in one grouped launch; other plans
+ * join as parallel branches holding their own step graphs.  Plans keep their
+ * own state, results and read functions.  Destroy the batch before its plans. */
 typedef struct kw_batch kw_batch;
 int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out);
 int32_t kw_batch_run(kw_batch* batch, int32_t nsteps, void* stream);
+/* Kernels launched through the batch and its plans since their creation (a
+ * grouped launch over several plans counts once). */
+int32_t kw_batch_launch_count(const kw_batch* batch, int64_t* count);
 int32_t kw_batch_destroy(kw_batch* batch);
 /* Waits for the plan's work on `stream`. */
 int32_t kw_plan_sync(kw_plan* plan, void* stream);

@@ -68,7 +68,8 @@ __device__ __forceinline__ float2 axis_op(const AxisParams& P, const AxisJob& J,
 // ---------------------------------------------------------------------------
 // strided-axis FFT kernel
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_axis(const __grid_constant__ AxisParams P) {
+// One block (bx, by, bz) of an axis pass.
+__device__ __forceinline__ void axis_block(const AxisParams& P, int bx, int by, int bz) {
   extern __shared__ float4 smem_f4[];
   float2* sm = reinterpret_cast<float2*>(smem_f4);
   const int n = P.n, T = P.T;
@@ -77,13 +78,13 @@ __global__ void __launch_bounds__(256) k_axis(const __grid_constant__ AxisParams
   float2* B = A + (size_t)n * T;
   float2* C = B + (size_t)n * T;
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = P.tw[i];
-  const int c0 = blockIdx.x * T;
+  const int c0 = bx * T;
   const int nc = min(T, P.ncols - c0);
-  const long long base = (long long)blockIdx.y * P.os + c0;
+  const long long base = (long long)by * P.os + c0;
   const int tot = n * T;
 
   if (P.mode < 2) {
-    float2* buf = P.bufs[P.plain[blockIdx.z]];
+    float2* buf = P.bufs[P.plain[bz]];
     const bool inv = P.mode == 1;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
       const int x = i / T, cc = i - x * T;
@@ -134,6 +135,52 @@ __global__ void __launch_bounds__(256) k_axis(const __grid_constant__ AxisParams
     }
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(256) k_axis(const __grid_constant__ AxisParams P) {
+  axis_block(P, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// ---------------------------------------------------------------------------
+// grouped launches: one launch runs the same kind of pass for several plans.
+// blk[i] = (first block of member i, grid x, grid y, 0), blk[n].x = total
+// blocks; each block copies its member's parameters into shared memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int group_member(const int4* __restrict__ blk, int n) {
+  __shared__ int s_member;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = n - 1;
+    const int b = blockIdx.x;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (blk[mid].x <= b)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    s_member = lo;
+  }
+  __syncthreads();
+  return s_member;
+}
+
+template <class T>
+__device__ __forceinline__ void copy_params(T& dst, const T* __restrict__ src) {
+  static_assert(sizeof(T) % 4 == 0, "parameter block size");
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(&dst);
+  for (int w = threadIdx.x; w < (int)(sizeof(T) / 4); w += blockDim.x) d[w] = s[w];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_axis_group(const AxisParams* __restrict__ Ps, const int4* __restrict__ blk,
+                                                    int n) {
+  __shared__ __align__(16) AxisParams sp;
+  const int i = group_member(blk, n);
+  copy_params(sp, Ps + i);
+  const int4 g = blk[i];
+  const int b = blockIdx.x - g.x;
+  axis_block(sp, b % g.y, (b / g.y) % g.z, b / (g.y * g.z));
 }
 
 // ---------------------------------------------------------------------------
@@ -276,9 +323,9 @@ struct GenericRowFFT {
 // The stage physics of one block of R rows; rb[q] are R*L real buffers in
 // shared memory.  Every rf call starts and ends with a block-wide barrier.
 template <class RF>
-__device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, float* const* rb) {
+__device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, float* const* rb, int bx) {
   const int L = P.L, R = P.R;
-  const int r0 = blockIdx.x * R;
+  const int r0 = bx * R;
   const int nr = min(R, P.nrows - r0);
   const int tot = R * L;
   const int D = P.ndim;
@@ -510,7 +557,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
   rf.r2c(P, rb[0], P.S[3], r0, nr);
 }
 
-__global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams P) {
+__device__ __forceinline__ void rows_block(const RowsParams& P, int bx) {
   extern __shared__ float4 smem_f4[];
   const int M = P.Mfft, L = P.L, R = P.R;
   GenericRowFFT rf;
@@ -525,7 +572,22 @@ __global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams
   if (P.even)
     for (int i = threadIdx.x; i <= L / 2; i += blockDim.x) s.twp[i] = P.twpost[i];
   __syncthreads();  // the row transforms read twp before their first barrier
-  rows_body(P, rf, s.rb);
+  rows_body(P, rf, s.rb, bx);
+}
+
+__global__ void __launch_bounds__(256) k_rows(const __grid_constant__ RowsParams P) { rows_block(P, blockIdx.x); }
+
+__global__ void __launch_bounds__(256) k_rows_group(const RowsParams* __restrict__ Ps, const int4* __restrict__ blk,
+                                                    int n) {
+  __shared__ __align__(16) RowsParams sp;
+  const int i = group_member(blk, n);
+  copy_params(sp, Ps + i);
+  rows_block(sp, blockIdx.x - blk[i].x);
+}
+
+__global__ void k_step_tick_group(int* const* __restrict__ tdev, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) *tdev[i] += 1;
 }
 
 // ---------------------------------------------------------------------------

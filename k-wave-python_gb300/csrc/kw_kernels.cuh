@@ -193,6 +193,10 @@ __global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out
 // the last node of each step graph
 __global__ void k_step_set(int* tdev, int t);
 __global__ void k_step_tick(int* tdev);
+__global__ void k_step_tick_group(int* const* tdev, int n);
+// grouped generic passes over several plans (blk: per member first block and grid shape)
+__global__ void k_axis_group(const AxisParams* Ps, const int4* blk, int n);
+__global__ void k_rows_group(const RowsParams* Ps, const int4* blk, int n);
 // Medium grids derived on the device (kw_plan_derive_medium); any output may be null.
 struct DeriveParams {
   int ndim, N[3];

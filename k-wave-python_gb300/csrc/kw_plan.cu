@@ -119,6 +119,16 @@ struct kw_plan {
   unsigned int* d_maxes = nullptr;
   // per-step flags passed to the row stages
   int srcp_on = 0, srcu_on[3] = {0, 0, 0}, rec_us = 0, init_r2c = 0;
+  // grouping: when set, the generic passes of a step are recorded here
+  // instead of launched (kw_batch folds them into grouped launches)
+  struct LaunchRec {
+    int kind;  // 0 generic rows, 1 generic axis pass, 2 another kernel
+    RowsParams rp;
+    AxisParams ap;
+    int gx, gy, gz;
+    size_t smem;
+  };
+  std::vector<LaunchRec>* rec_list = nullptr;
   // step graphs: one captured step per distinct launch sequence, replayed with
   // the step index read from d_tstep
   struct StepGraph {
@@ -577,9 +587,11 @@ int32_t kw_plan_finalize(kw_plan* p) {
   }
   CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   CK(cudaFuncSetAttribute(k_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  CK(cudaFuncSetAttribute(k_rows_group, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  CK(cudaFuncSetAttribute(k_axis_group, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   {
     const char* env = getenv("KWAVE_GB300_GENERIC_FFT");
-    p->generic_only = env && env[0] == '1';
+    p->generic_only = (env && env[0] == '1') || (p->g.flags & KW_DESC_GENERIC_FFT);
   }
   {
     int dev = 0;
@@ -751,6 +763,16 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   for (int a = 0; a < 3; ++a) P.srcu_on[a] = p->srcu_on[a];
   P.rec_us = p->rec_us;
   P.init_r2c = p->init_r2c;
+  if (p->rec_list) {
+    kw_plan::LaunchRec r{};
+    r.kind = p->rows_reg ? 2 : 0;
+    r.rp = P;
+    r.gx = (p->nrows + p->R - 1) / p->R;
+    r.gy = r.gz = 1;
+    r.smem = p->smem_rows;
+    p->rec_list->push_back(r);
+    return KW_OK;
+  }
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
@@ -817,6 +839,17 @@ static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int
   A.mode = inv ? 1 : 0;
   for (int i = 0; i < nb; ++i) A.plain[i] = bufs[i];
   const int nouter = (p->D == 3 && axis == 1) ? p->N[0] : 1;
+  if (p->rec_list) {
+    kw_plan::LaunchRec r{};
+    r.kind = (p->tma_axis[axis] || p->axis_reg[axis]) ? 2 : 1;
+    r.ap = A;
+    r.gx = (A.ncols + A.T - 1) / A.T;
+    r.gy = nouter;
+    r.gz = nb;
+    r.smem = p->smem_axis_plain[axis];
+    p->rec_list->push_back(r);
+    return KW_OK;
+  }
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
@@ -866,6 +899,16 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
   A.pow1 = (float)(p->g.alpha_power - 2.0);
   A.pow2 = (float)(p->g.alpha_power - 1.0);
   A.scale = (float)(1.0 / (double)p->ntot);
+  if (p->rec_list) {
+    kw_plan::LaunchRec r{};
+    r.kind = (p->tma_axis[0] || p->axis_reg[0]) ? 2 : 1;
+    r.ap = A;
+    r.gx = (A.ncols + A.T - 1) / A.T;
+    r.gy = r.gz = 1;
+    r.smem = p->smem_axis_ops;
+    p->rec_list->push_back(r);
+    return KW_OK;
+  }
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
@@ -1119,10 +1162,16 @@ int32_t kw_plan_set_graphs(kw_plan* p, int32_t enable) {
 struct kw_batch {
   std::vector<kw_plan*> plans;
   struct Graph {
-    std::vector<int> keys;  // per plan: step key, or -1 when the plan does not step
+    std::vector<int> keys;     // per plan: step key, or -1 when the plan does not step
+    std::vector<char> grouped; // per plan: its passes run inside the grouped launches
+    std::vector<long long> nl; // per ungrouped plan: launches of its step graph
     cudaGraphExec_t exec;
+    long long nlaunch;         // grouped launches per replay
   };
   std::vector<Graph> graphs;
+  std::vector<void*> allocs;
+  cudaStream_t cap = nullptr;
+  long long launches = 0;
 };
 
 int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
@@ -1140,17 +1189,126 @@ int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
   return KW_OK;
 }
 
-static int batch_graph(kw_batch* b, const std::vector<int>& keys, const std::vector<kw_plan::StepGraph*>& sg,
-                       cudaGraphExec_t* exec) {
+static int batch_upload(kw_batch* b, const void* host, size_t bytes, void** out) {
+  void* d = nullptr;
+  CK(cudaMalloc(&d, bytes));
+  b->allocs.push_back(d);
+  CK(cudaMemcpy(d, host, bytes, cudaMemcpyHostToDevice));
+  *out = d;
+  return KW_OK;
+}
+
+// The graph of one batch step for the given per-plan keys (built on first use).
+// The steps of plans whose passes are all generic are recorded, and launch k
+// of every such plan runs in one grouped launch (rows and axis passes apart);
+// the other plans join as child graphs of their own step graphs.
+static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Graph** out) {
   for (auto& g : b->graphs)
     if (g.keys == keys) {
-      *exec = g.exec;
+      *out = &g;
       return KW_OK;
     }
-  cudaGraph_t graph = nullptr;
-  CK(cudaGraphCreate(&graph, 0));
-  for (size_t i = 0; i < keys.size(); ++i) {
+  const size_t n = keys.size();
+  std::vector<std::vector<kw_plan::LaunchRec>> lists(n);
+  kw_batch::Graph G;
+  G.keys = keys;
+  G.grouped.assign(n, 0);
+  G.nl.assign(n, 0);
+  G.exec = nullptr;
+  G.nlaunch = 0;
+  int rc;
+  for (size_t i = 0; i < n; ++i) {
     if (keys[i] < 0) continue;
+    kw_plan* p = b->plans[i];
+    p->rec_list = &lists[i];
+    p->capturing = true;
+    rc = enqueue_step(p, p->t, false, nullptr);
+    p->rec_list = nullptr;
+    p->capturing = false;
+    if (rc) return rc;
+    bool ok = !lists[i].empty();
+    for (auto& r : lists[i]) ok = ok && r.kind != 2;
+    G.grouped[i] = ok;
+  }
+  struct Pending {
+    int kind, m, total;
+    size_t smem;
+    void* params;
+    int4* blk;
+  };
+  std::vector<Pending> pend;
+  std::vector<int*> ticks;
+  size_t maxlen = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (G.grouped[i]) {
+      maxlen = std::max(maxlen, lists[i].size());
+      ticks.push_back(b->plans[i]->d_tstep);
+    }
+  for (size_t j = 0; j < maxlen; ++j)
+    for (int kind = 0; kind < 2; ++kind) {
+      std::vector<RowsParams> rp;
+      std::vector<AxisParams> ap;
+      std::vector<int4> blk;
+      long long total = 0;
+      size_t smem = 0;
+      for (size_t i = 0; i < n; ++i) {
+        if (!G.grouped[i] || lists[i].size() <= j || lists[i][j].kind != kind) continue;
+        const kw_plan::LaunchRec& r = lists[i][j];
+        blk.push_back(make_int4((int)total, r.gx, r.gy, 0));
+        if (kind == 0)
+          rp.push_back(r.rp);
+        else
+          ap.push_back(r.ap);
+        total += (long long)r.gx * r.gy * r.gz;
+        smem = std::max(smem, r.smem);
+      }
+      if (blk.empty()) continue;
+      if (total >= (1LL << 31)) return fail(KW_ERR_UNSUPPORTED, "grouped launch of %lld blocks", total);
+      const int m = (int)blk.size();
+      blk.push_back(make_int4((int)total, 0, 0, 0));
+      Pending q{kind, m, (int)total, smem, nullptr, nullptr};
+      if (kind == 0)
+        rc = batch_upload(b, rp.data(), rp.size() * sizeof(RowsParams), &q.params);
+      else
+        rc = batch_upload(b, ap.data(), ap.size() * sizeof(AxisParams), &q.params);
+      void* dblk = nullptr;
+      if (!rc) rc = batch_upload(b, blk.data(), blk.size() * sizeof(int4), &dblk);
+      if (rc) return rc;
+      q.blk = static_cast<int4*>(dblk);
+      pend.push_back(q);
+    }
+  int** dticks = nullptr;
+  if (!ticks.empty()) {
+    void* d = nullptr;
+    if ((rc = batch_upload(b, ticks.data(), ticks.size() * sizeof(int*), &d))) return rc;
+    dticks = static_cast<int**>(d);
+  }
+  // ungrouped plans: their own step graphs
+  std::vector<kw_plan::StepGraph*> sg(n, nullptr);
+  for (size_t i = 0; i < n; ++i)
+    if (keys[i] >= 0 && !G.grouped[i]) {
+      if ((rc = step_graph(b->plans[i], b->plans[i]->t, &sg[i]))) return rc;
+      G.nl[i] = sg[i]->nlaunch;
+    }
+  if (!b->cap) CK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+  CK(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed));
+  for (const Pending& q : pend) {
+    if (q.kind == 0)
+      k_rows_group<<<q.total, kThreads, q.smem, b->cap>>>(static_cast<const RowsParams*>(q.params), q.blk, q.m);
+    else
+      k_axis_group<<<q.total, kThreads, q.smem, b->cap>>>(static_cast<const AxisParams*>(q.params), q.blk, q.m);
+  }
+  if (dticks) k_step_tick_group<<<((int)ticks.size() + 127) / 128, 128, 0, b->cap>>>(dticks, (int)ticks.size());
+  const cudaError_t el = cudaGetLastError();
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(b->cap, &graph);
+  if (el != cudaSuccess || ec != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return fail(KW_ERR_CUDA, "batch capture: %s", cudaGetErrorString(el != cudaSuccess ? el : ec));
+  }
+  G.nlaunch = (long long)pend.size() + (dticks ? 1 : 0);
+  for (size_t i = 0; i < n; ++i) {
+    if (!sg[i]) continue;
     cudaGraphNode_t node;
     const cudaError_t e = cudaGraphAddChildGraphNode(&node, graph, nullptr, 0, sg[i]->graph);
     if (e != cudaSuccess) {
@@ -1158,10 +1316,11 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, const std::vec
       return fail(KW_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
     }
   }
-  const cudaError_t ei = cudaGraphInstantiate(exec, graph, 0);
+  const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
   cudaGraphDestroy(graph);
   if (ei != cudaSuccess) return fail(KW_ERR_CUDA, "batch graph instantiation: %s", cudaGetErrorString(ei));
-  b->graphs.push_back(kw_batch::Graph{keys, *exec});
+  b->graphs.push_back(G);
+  *out = &b->graphs.back();
   return KW_OK;
 }
 
@@ -1171,7 +1330,6 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const size_t n = b->plans.size();
   std::vector<int> end(n), keys(n);
-  std::vector<kw_plan::StepGraph*> sg(n, nullptr);
   int span = 0;
   for (size_t i = 0; i < n; ++i) {
     kw_plan* p = b->plans[i];
@@ -1188,9 +1346,7 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
         together = false;
         continue;
       }
-      int rc = step_graph(p, p->t, &sg[i]);
-      if (rc) return rc;
-      keys[i] = sg[i]->key;
+      keys[i] = step_key(p, p->t);
     }
     int rc;
     if (!together) {
@@ -1203,19 +1359,28 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
       }
       continue;
     }
+    kw_batch::Graph* g = nullptr;
+    if ((rc = batch_graph(b, keys, &g))) return rc;
     for (size_t i = 0; i < n; ++i)
       if (keys[i] >= 0 && (rc = step_counter_to(b->plans[i], b->plans[i]->t, st))) return rc;
-    cudaGraphExec_t exec = nullptr;
-    if ((rc = batch_graph(b, keys, sg, &exec))) return rc;
-    CK(cudaGraphLaunch(exec, st));
+    CK(cudaGraphLaunch(g->exec, st));
+    b->launches += g->nlaunch;
     for (size_t i = 0; i < n; ++i) {
       if (keys[i] < 0) continue;
       kw_plan* p = b->plans[i];
       p->tstep_val = p->t + 1;
-      p->launches += sg[i]->nlaunch;
+      p->launches += g->nl[i];
       p->t += 1;
     }
   }
+  return KW_OK;
+}
+
+int32_t kw_batch_launch_count(const kw_batch* b, int64_t* count) {
+  if (!b || !count) return fail(KW_ERR_INVALID, "null argument");
+  long long c = b->launches;
+  for (const kw_plan* p : b->plans) c += p->launches;
+  *count = c;
   return KW_OK;
 }
 
@@ -1223,6 +1388,8 @@ int32_t kw_batch_destroy(kw_batch* b) {
   if (!b) return KW_OK;
   for (auto& g : b->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  for (void* a : b->allocs) cudaFree(a);
   delete b;
   return KW_OK;
 }

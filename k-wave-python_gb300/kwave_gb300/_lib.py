@@ -29,6 +29,7 @@ KW_R_P, KW_R_UX_ST, KW_R_UY_ST, KW_R_UZ_ST, KW_R_UX, KW_R_UY, KW_R_UZ = range(7)
 # fields
 KW_FLD_P, KW_FLD_U0, KW_FLD_U1, KW_FLD_U2, KW_FLD_RHO0, KW_FLD_RHO1, KW_FLD_RHO2 = range(7)
 KW_AGG_MAX, KW_AGG_MIN, KW_AGG_RMS = range(3)
+KW_DESC_GENERIC_FFT = 1
 
 
 class KwGridDesc(C.Structure):
@@ -45,7 +46,7 @@ class KwGridDesc(C.Structure):
         ("absorb_mode", C.c_int32),
         ("dispersion", C.c_int32),
         ("nonlinear", C.c_int32),
-        ("reserved", C.c_int32),
+        ("flags", C.c_int32),
         ("alpha_power", C.c_double),
     ]
 
@@ -80,6 +81,7 @@ _PROTOS = {
     "kw_batch_create": (C.c_int32, [_P, C.c_int32, C.POINTER(_P)]),
     "kw_batch_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_batch_destroy": (C.c_int32, [_P]),
+    "kw_batch_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "kw_plan_sync": (C.c_int32, [_P, _P]),
     "kw_plan_time_index": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "kw_plan_read_series": (C.c_int32, [_P, C.c_int32, _P, C.c_int64]),

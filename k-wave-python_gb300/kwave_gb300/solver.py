@@ -39,7 +39,7 @@ STATS = {"h2d_bytes": 0, "d2h_bytes": 0}
 class DevicePlan:
     """Owns one kw_plan (device state of one simulation)."""
 
-    def __init__(self, S: Setup, stream=None):
+    def __init__(self, S: Setup, stream=None, generic_fft=False):
         lib = K.lib()
         K.require_device()
         self.S = S
@@ -60,6 +60,7 @@ class DevicePlan:
         d.dispersion = S.dispersion
         d.nonlinear = S.nonlinear
         d.alpha_power = S.alpha_power
+        d.flags = K.KW_DESC_GENERIC_FFT if generic_fft else 0
         self._h = C.c_void_p()
         K.check(lib.kw_plan_create(C.byref(d), C.byref(self._h)))
         try:
@@ -215,9 +216,13 @@ class Simulation:
         return obj
 
     # -- setup / stepping ---------------------------------------------------
-    def setup(self):
+    def setup(self, generic_fft=False):
+        """Host set-up and device plan.  ``generic_fft`` runs every pass with
+        the run-time-length FFT kernels (what lets a batch group the plan's
+        passes with other plans); the default picks the fastest kernels for
+        the grid."""
         self.S = build_setup(self.prob, derive_on_device=True)
-        self._plan = DevicePlan(self.S, stream=self.stream)
+        self._plan = DevicePlan(self.S, stream=self.stream, generic_fft=generic_fft)
         self.t = 0
         return self
 
@@ -310,14 +315,19 @@ def acoustic_intensity(result):
 class SimulationBatch:
     """Independent simulations advanced together on one stream (kw_batch).
 
-    Each member keeps its own grid size, medium, sources, sensor and results;
-    every step of all members is one CUDA graph launch whose parallel branches
-    are the members' step graphs.  The reference has no batch object: it runs
-    ``Simulation.run()`` (kwave/solvers/kspace_solver.py:749-778) once per
-    simulation, and so does a loop over members here, with the same results.
+    Each member keeps its own grid size, medium, sources, sensor and results.
+    Every step of all members is one CUDA graph launch.  By default each
+    member uses the kernels picked for its grid and joins that graph as a
+    parallel branch holding its own step graph.  With ``grouped=True`` the
+    members set up here use the run-time-length FFT kernels, and the k-th pass
+    of every member runs in one grouped launch over all of them (a handful of
+    launches per step whatever the batch size).  The reference has no batch
+    object: it runs ``Simulation.run()`` (kwave/solvers/kspace_solver.py:
+    749-778) once per simulation, and a loop over members here gives the same
+    results.
     """
 
-    def __init__(self, sims, stream=None):
+    def __init__(self, sims, stream=None, grouped=False):
         self.sims = list(sims)
         if not self.sims:
             raise ValueError("SimulationBatch needs at least one simulation")
@@ -325,7 +335,7 @@ class SimulationBatch:
         for s in self.sims:
             if s._plan is None:
                 s.stream = stream
-                s.setup()
+                s.setup(generic_fft=grouped)
         lib = K.lib()
         self.lib = lib
         handles = (C.c_void_p * len(self.sims))(*[s._plan.handle for s in self.sims])
@@ -333,8 +343,13 @@ class SimulationBatch:
         K.check(lib.kw_batch_create(handles, len(self.sims), C.byref(self._h)))
 
     @classmethod
-    def from_problems(cls, problems, stream=None):
-        return cls([Simulation.from_problem(p, stream=stream) for p in problems], stream=stream)
+    def from_problems(cls, problems, stream=None, grouped=False):
+        return cls([Simulation.from_problem(p, stream=stream) for p in problems], stream=stream, grouped=grouped)
+
+    def launch_count(self):
+        c = C.c_int64()
+        K.check(self.lib.kw_batch_launch_count(self._h, C.byref(c)))
+        return c.value
 
     def run_steps(self, nsteps):
         st = C.c_void_p(self.stream) if self.stream is not None else None
@@ -364,9 +379,9 @@ class SimulationBatch:
             pass
 
 
-def run_batch(problems, stream=None):
+def run_batch(problems, stream=None, grouped=False):
     """Set up, run together and close the simulations described by plain problem dicts."""
-    b = SimulationBatch.from_problems(problems, stream=stream)
+    b = SimulationBatch.from_problems(problems, stream=stream, grouped=grouped)
     try:
         return b.run()
     finally:
