@@ -103,13 +103,15 @@ cudaError_t kw_tma_attr(int n, int axis) {
 
 // Launch one persistent pass along `axis` (0: operator or plain pass along x;
 // 1: plain pass along y of a 3-D grid) over `nb` plain buffers or A's jobs.
-cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A) {
+cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A,
+                          int pdl) {
   KwTmaPlan* tp = static_cast<KwTmaPlan*>(h);
   int E, P;
   const int kind = A.mode < 2 ? KK_PLAIN : ops_kind(A);
   if (!kw_tma_shape(n, kind, &E, &P)) return cudaErrorInvalidValue;
   const int T = kw_tma_tile_cols(n, P, axis, kind);
   TmaWork W;
+  W.pdl = pdl;
   W.err = device_error_ptr();
   if (!W.err) return cudaErrorInvalidSymbol;
   W.ntile = (A.ncols + T - 1) / T;

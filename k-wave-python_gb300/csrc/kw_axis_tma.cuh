@@ -51,6 +51,7 @@ struct TmaWork {
   // the grid stride gridDim.x as (buffer, outer, tile) digits, for the
   // division-free walk over units (UnitPos)
   int st_tile, st_outer, st_b;
+  int pdl;     // host: launch as a programmatic dependent of the previous kernel
 };
 
 // Position (b, outer, tile) of unit u = b * nouter * ntile + outer * ntile +
@@ -272,6 +273,9 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
     }
   }
   __syncthreads();
+  // everything above reads only tables; the spectra come from the previous launch
+  kwtma::grid_dep_wait();
+  kwtma::grid_dep_launch();
   const float* k0s = kTablesInSmem ? k0t : A.k[0];
   const TabX f0s{kTablesInSmem ? f0t : A.fg[0], kTablesInSmem ? f0t + N : A.fd[0], kTablesInSmem ? f0t + 2 * N : A.us[0]};
 
@@ -585,8 +589,9 @@ cudaError_t kw_tma_attr_kind(int n, int axis) {
 template <int KIND>
 cudaError_t kw_tma_launch_kind(int n, int axis, int grid, size_t smem, cudaStream_t st, const AxisParams& A,
                                const TmaMaps& maps, const TmaWork& W) {
-#define KW_T(E_, P_, S_, B_, T_) \
-  (k_axis_tma<E_, P_, S_, B_, T_, KIND><<<grid, T_ * P_ + 32, smem, st>>>(A, maps, W), cudaGetLastError())
+#define KW_T(E_, P_, S_, B_, T_)                                                                              \
+  kwtma::launch_k(k_axis_tma<E_, P_, S_, B_, T_, KIND>, dim3(grid), dim3(T_ * P_ + 32), smem, st, W.pdl != 0, A, \
+                  maps, W)
   KW_TMA_SWITCH(n, 0, KW_T)
 #undef KW_T
 }

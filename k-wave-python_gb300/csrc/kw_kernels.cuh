@@ -173,7 +173,10 @@ void kw_tma_plan_destroy(void* h);
 bool kw_tma_supported(int n);
 bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long long xs, int nouter, long long os, int P);
 cudaError_t kw_tma_attr(int n, int axis);
-cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A);
+// pdl != 0: launched as a programmatic dependent of the previous kernel of the
+// stream (its prologue overlaps that kernel's tail)
+cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A,
+                          int pdl);
 // Window value of the p0 smoothing at squared radius r2 (linear interpolation).
 __device__ __forceinline__ float window_at(const float* tab, int n, float rad, float r2) {
   float r = sqrtf(r2);
@@ -223,7 +226,7 @@ int* kw_device_error_ptr();
 // Velocity and power-law density stages fed by bulk copies (kw_rows_tma.cu),
 // power-of-two row lengths; stage is ST_U or ST_RHO_PL.
 cudaError_t kw_rows_tma_attr(int m, int Hp, int ex_stride);
-cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err);
+cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err, int pdl);
 __global__ void k_rows(const __grid_constant__ RowsParams P);
 __global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
                                 const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out);

@@ -139,6 +139,10 @@ struct kw_plan {
   };
   std::vector<StepGraph> graphs;
   bool use_graphs = true;
+  // TMA passes launched as programmatic dependents (KWAVE_GB300_PDL=1).  Off by
+  // default: at 256^3 the step took 1.083 ms with it against 1.054 ms without
+  // (early CTAs of the next persistent pass land unevenly across SMs).
+  bool pdl = false;
   bool capturing = false;
   int* d_tstep = nullptr;
   int tstep_val = -1;  // value d_tstep holds once the stream reaches the last enqueued work
@@ -150,6 +154,10 @@ struct kw_plan {
   std::vector<std::pair<int, size_t>> ev_used;  // (class, index of start event)
   size_t ev_next = 0;
 };
+
+// TMA passes start their prologue while the previous kernel drains, except
+// while every launch is bracketed by timing events.
+static int pdl_ok(const kw_plan* p) { return p->pdl && !p->timing; }
 
 // Bracket a launch with events when timing is on.
 static int ev_begin(kw_plan* p, cudaStream_t st, size_t* slot) {
@@ -649,6 +657,8 @@ int32_t kw_plan_finalize(kw_plan* p) {
   {
     const char* env = getenv("KWAVE_GB300_GRAPHS");
     if (env && env[0] == '0') p->use_graphs = false;
+    env = getenv("KWAVE_GB300_PDL");
+    if (env && env[0] == '1') p->pdl = true;
   }
   CK(cudaDeviceSynchronize());
   p->finalized = true;
@@ -787,11 +797,11 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
     const int grid = (p->nrows + p->rows_R - 1) / p->rows_R;
     const bool extra = P.srcp_on || P.srcu_on[0] || P.srcu_on[1] || P.srcu_on[2] || P.rec_us;
     if (stage == ST_U && !init && !extra && p->rows_tma)
-      CK(kw_rows_tma_launch(p->Mfft, ST_U, p->nsm, st, P, kw_device_error_ptr()));
+      CK(kw_rows_tma_launch(p->Mfft, ST_U, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
     else if (stage == ST_RHO && dsm && !extra && p->rows_tma)
-      CK(kw_rows_tma_launch(p->Mfft, ST_RHO_PL, p->nsm, st, P, kw_device_error_ptr()));
+      CK(kw_rows_tma_launch(p->Mfft, ST_RHO_PL, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
     else if (stage == ST_EOS && p->rows_tma)
-      CK(kw_rows_tma_launch(p->Mfft, ST_EOS, p->nsm, st, P, kw_device_error_ptr()));
+      CK(kw_rows_tma_launch(p->Mfft, ST_EOS, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
     else
       CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
   } else {
@@ -854,7 +864,7 @@ static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
   if (p->tma_axis[axis]) {
-    CK(kw_tma_launch(p->tma, axis, p->N[axis], nouter, nb, p->nsm, st, A));
+    CK(kw_tma_launch(p->tma, axis, p->N[axis], nouter, nb, p->nsm, st, A, pdl_ok(p)));
   } else if (p->axis_reg[axis]) {
     const int E = p->axis_regE[axis], Pt = p->axis_regP[axis], T = 256 / Pt, n = p->N[axis];
     dim3 grid((A.ncols + T - 1) / T, nouter, nb);
@@ -913,7 +923,7 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
   if (p->tma_axis[0]) {
-    CK(kw_tma_launch(p->tma, 0, p->N[0], 1, 0, p->nsm, st, A));
+    CK(kw_tma_launch(p->tma, 0, p->N[0], 1, 0, p->nsm, st, A, pdl_ok(p)));
   } else if (p->axis_reg[0]) {
     const int E = p->axis_regE[0], Pt = p->axis_regP[0], T = 256 / Pt, n = p->N[0];
     dim3 grid((A.ncols + T - 1) / T, 1, 1);
@@ -1185,6 +1195,13 @@ int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
   }
   kw_batch* b = new kw_batch;
   b->plans.assign(plans, plans + n);
+  // step graphs of batch members become child graphs: capture them with plain
+  // stream-order edges between their kernels
+  for (kw_plan* p : b->plans)
+    if (p->pdl) {
+      p->pdl = false;
+      drop_graphs(p);
+    }
   *out = b;
   return KW_OK;
 }
@@ -1226,7 +1243,9 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
     p->rec_list = nullptr;
     p->capturing = false;
     if (rc) return rc;
-    bool ok = !lists[i].empty();
+    // only plans created for grouping (KW_DESC_GENERIC_FFT): on the same
+    // kernels, separate branches measured faster than grouped launches
+    bool ok = !lists[i].empty() && (p->g.flags & KW_DESC_GENERIC_FFT);
     for (auto& r : lists[i]) ok = ok && r.kind != 2;
     G.grouped[i] = ok;
   }

@@ -135,6 +135,9 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
     for (int i = tid; i < 2 * M; i += blockDim.x) pmlz[i] = src[i];
   }
   __syncthreads();
+  // everything above reads only tables; the fields come from the previous launch
+  kwtma::grid_dep_wait();
+  kwtma::grid_dep_launch();
 
   const int nblk = (Q.nrows + R - 1) / R;
   const int nload = row_nloads<STAGE>(Q);
@@ -440,14 +443,15 @@ static cudaError_t rows_tma_attr(int m, int Hp, int ex_stride) {
 }
 
 template <int STAGE>
-static cudaError_t rows_tma_launch(int m, int nsm, cudaStream_t st, const RowsParams& Q, int* err) {
+static cudaError_t rows_tma_launch(int m, int nsm, cudaStream_t st, const RowsParams& Q, int* err, int pdl) {
   int E, P;
   if (!kw_reg_shape(m, &E, &P)) return cudaErrorInvalidValue;
   const int R = 128 / P, nblk = (Q.nrows + R - 1) / R;
   const int per_sm = row_ctas(STAGE);
   const int grid = nblk < per_sm * nsm ? nblk : per_sm * nsm;
   const size_t smem = rows_tma_smem(STAGE, m, E, P, Q.Hp, Q.ex_stride);
-#define KW_R(E_, P_) (k_rows_tma<E_, P_, row_nst(STAGE), STAGE><<<grid, 160, smem, st>>>(Q, err), cudaGetLastError())
+#define KW_R(E_, P_) \
+  kwtma::launch_k(k_rows_tma<E_, P_, row_nst(STAGE), STAGE>, dim3(grid), dim3(160), smem, st, pdl != 0, Q, err)
   KW_RT_SWITCH(m, KW_R)
 #undef KW_R
 }
@@ -458,9 +462,9 @@ cudaError_t kw_rows_tma_attr(int m, int Hp, int ex_stride) {
   return e == cudaSuccess ? rows_tma_attr<ST_EOS>(m, Hp, ex_stride) : e;
 }
 
-cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err) {
-  if (stage == ST_U) return rows_tma_launch<ST_U>(m, nsm, st, Q, err);
-  if (stage == ST_RHO_PL) return rows_tma_launch<ST_RHO_PL>(m, nsm, st, Q, err);
-  if (stage == ST_EOS) return rows_tma_launch<ST_EOS>(m, nsm, st, Q, err);
+cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err, int pdl) {
+  if (stage == ST_U) return rows_tma_launch<ST_U>(m, nsm, st, Q, err, pdl);
+  if (stage == ST_RHO_PL) return rows_tma_launch<ST_RHO_PL>(m, nsm, st, Q, err, pdl);
+  if (stage == ST_EOS) return rows_tma_launch<ST_EOS>(m, nsm, st, Q, err, pdl);
   return cudaErrorInvalidValue;
 }
