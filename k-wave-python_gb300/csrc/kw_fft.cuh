@@ -20,11 +20,44 @@
 
 #define KW_MAX_STAGES 16
 
+// x / d for 0 <= x < 2^31 and 1 <= d < 2^31 as a multiply-high, an add and a
+// shift: m = floor(2^32 (2^l - d) / d) + 1 with l = ceil(log2 d) (the
+// round-up reciprocal of Granlund and Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994).
+struct KwDivU {
+  uint32_t m, s;
+};
+
+__host__ __device__ inline KwDivU kw_divu_make(uint32_t d) {
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  KwDivU r;
+  r.s = l;
+  r.m = (uint32_t)(((((unsigned long long)1 << l) - d) << 32) / d + 1);
+  return r;
+}
+
+__device__ __forceinline__ int kw_divu(int x, KwDivU D) {
+  return (int)((__umulhi((uint32_t)x, D.m) + (uint32_t)x) >> D.s);
+}
+
 struct KwFftLen {
   int n;                      // transform length
   int nst;                    // number of stages
   int radix[KW_MAX_STAGES];   // radices in stage order
+  KwDivU dt[KW_MAX_STAGES];   // stage s: division by n / radix[s]
+  KwDivU dp[KW_MAX_STAGES];   // stage s: division by the product of the earlier radices
 };
+
+// Fill the per-stage divisors once the radices are set.
+inline void kw_fft_len_finish(KwFftLen& f) {
+  int p = 1;
+  for (int s = 0; s < f.nst; ++s) {
+    f.dt[s] = kw_divu_make((uint32_t)(f.n / f.radix[s]));
+    f.dp[s] = kw_divu_make((uint32_t)p);
+    p *= f.radix[s];
+  }
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
@@ -126,23 +159,24 @@ __device__ __forceinline__ void dft_small<7>(float2* v) {
 // Element x of sequence b lives at buf[x * xs + b * bs].
 // BATCH_FAST: consecutive threads walk consecutive b (interleaved layouts),
 // otherwise consecutive j (row-contiguous layouts).
+// BATCH_FAST needs B to be a power of two (lgB = log2 B).
 template <int R, bool BATCH_FAST>
 __device__ __forceinline__ void stockham_stage(const float2* __restrict__ in, float2* __restrict__ out, int n, int p,
-                                               int B, int xs, int bs, const float2* __restrict__ tw, int tid,
-                                               int nth) {
+                                               int B, int lgB, KwDivU dT, KwDivU dp, int xs, int bs,
+                                               const float2* __restrict__ tw, int tid, int nth) {
   const int T = n / R;
   const int tstep = n / (p * R);
   const int total = T * B;
   for (int idx = tid; idx < total; idx += nth) {
     int b, j;
     if (BATCH_FAST) {
-      b = idx % B;
-      j = idx / B;
+      b = idx & (B - 1);
+      j = idx >> lgB;
     } else {
-      j = idx % T;
-      b = idx / T;
+      b = kw_divu(idx, dT);
+      j = idx - b * T;
     }
-    const int k = j % p;
+    const int k = j - kw_divu(j, dp) * p;
     float2 v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) v[t] = in[(j + t * T) * xs + b * bs];
@@ -160,22 +194,25 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ in, fl
 // Full forward FFT of B sequences held in shared memory.  Data start in `a`;
 // `b` is scratch of the same size.  Returns the buffer holding the result.
 // Contains __syncthreads(); every thread of the block must call it.
+// BATCH_FAST layouts need B to be a power of two.
 template <bool BATCH_FAST>
 __device__ float2* fft_smem(float2* a, float2* b, const KwFftLen& L, int B, int xs, int bs,
                             const float2* __restrict__ tw) {
   const int tid = threadIdx.x, nth = blockDim.x;
+  const int lgB = __ffs(B) - 1;
   int p = 1;
   float2* src = a;
   float2* dst = b;
   for (int s = 0; s < L.nst; ++s) {
     __syncthreads();
     const int r = L.radix[s];
+    const KwDivU dT = L.dt[s], dp = L.dp[s];
     switch (r) {
-      case 4: stockham_stage<4, BATCH_FAST>(src, dst, L.n, p, B, xs, bs, tw, tid, nth); break;
-      case 2: stockham_stage<2, BATCH_FAST>(src, dst, L.n, p, B, xs, bs, tw, tid, nth); break;
-      case 3: stockham_stage<3, BATCH_FAST>(src, dst, L.n, p, B, xs, bs, tw, tid, nth); break;
-      case 5: stockham_stage<5, BATCH_FAST>(src, dst, L.n, p, B, xs, bs, tw, tid, nth); break;
-      default: stockham_stage<7, BATCH_FAST>(src, dst, L.n, p, B, xs, bs, tw, tid, nth); break;
+      case 4: stockham_stage<4, BATCH_FAST>(src, dst, L.n, p, B, lgB, dT, dp, xs, bs, tw, tid, nth); break;
+      case 2: stockham_stage<2, BATCH_FAST>(src, dst, L.n, p, B, lgB, dT, dp, xs, bs, tw, tid, nth); break;
+      case 3: stockham_stage<3, BATCH_FAST>(src, dst, L.n, p, B, lgB, dT, dp, xs, bs, tw, tid, nth); break;
+      case 5: stockham_stage<5, BATCH_FAST>(src, dst, L.n, p, B, lgB, dT, dp, xs, bs, tw, tid, nth); break;
+      default: stockham_stage<7, BATCH_FAST>(src, dst, L.n, p, B, lgB, dT, dp, xs, bs, tw, tid, nth); break;
     }
     p *= r;
     float2* t = src;

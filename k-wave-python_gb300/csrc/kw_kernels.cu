@@ -78,6 +78,7 @@ __device__ __forceinline__ void axis_block(const AxisParams& P, int bx, int by, 
   float2* B = A + (size_t)n * T;
   float2* C = B + (size_t)n * T;
   for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = P.tw[i];
+  const int lgT = __ffs(T) - 1;  // T is a power of two
   const int c0 = bx * T;
   const int nc = min(T, P.ncols - c0);
   const long long base = (long long)by * P.os + c0;
@@ -87,14 +88,14 @@ __device__ __forceinline__ void axis_block(const AxisParams& P, int bx, int by, 
     float2* buf = P.bufs[P.plain[bz]];
     const bool inv = P.mode == 1;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int x = i / T, cc = i - x * T;
+      const int x = i >> lgT, cc = i & (T - 1);
       float2 v = make_float2(0.f, 0.f);
       if (cc < nc) v = buf[base + (long long)x * P.xs + cc];
       A[i] = inv ? cconj(v) : v;
     }
     float2* res = fft_smem<true>(A, B, P.flen, T, T, 1, tw);
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int x = i / T, cc = i - x * T;
+      const int x = i >> lgT, cc = i & (T - 1);
       if (cc < nc) {
         const float2 v = res[i];
         buf[base + (long long)x * P.xs + cc] = inv ? cconj(v) : v;
@@ -110,7 +111,7 @@ __device__ __forceinline__ void axis_block(const AxisParams& P, int bx, int by, 
     if (J.in != cur) {
       const float2* in = P.bufs[J.in];
       for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-        const int x = i / T, cc = i - x * T;
+        const int x = i >> lgT, cc = i & (T - 1);
         A[i] = (cc < nc) ? in[base + (long long)x * P.xs + cc] : make_float2(0.f, 0.f);
       }
       X = fft_smem<true>(A, B, P.flen, T, T, 1, tw);
@@ -118,7 +119,7 @@ __device__ __forceinline__ void axis_block(const AxisParams& P, int bx, int by, 
     }
     float2* Y = (X == A) ? B : A;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int x = i / T, cc = i - x * T;
+      const int x = i >> lgT, cc = i & (T - 1);
       float2 v = make_float2(0.f, 0.f);
       if (cc < nc) {
         bool valid;
@@ -130,7 +131,7 @@ __device__ __forceinline__ void axis_block(const AxisParams& P, int bx, int by, 
     float2* res = fft_smem<true>(Y, C, P.flen, T, T, 1, tw);
     float2* out = P.bufs[J.out];
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int x = i / T, cc = i - x * T;
+      const int x = i >> lgT, cc = i & (T - 1);
       if (cc < nc) out[base + (long long)x * P.xs + cc] = cconj(res[i]);
     }
     __syncthreads();
@@ -200,7 +201,7 @@ __device__ void rows_c2r(const RowsParams& P, const RowSmem& s, const float2* __
   const int M = P.Mfft, L = P.L, R = P.R;
   const int tot = R * M;
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    const int row = i / M, k = i - row * M;
+    const int row = kw_divu(i, P.dM), k = i - row * M;
     float2 z = make_float2(0.f, 0.f);
     if (row < nr) {
       const float2* sr = S + (long long)(r0 + row) * P.Hp;
@@ -218,7 +219,7 @@ __device__ void rows_c2r(const RowsParams& P, const RowSmem& s, const float2* __
   }
   float2* res = fft_smem<false>(s.A, s.B, P.flen, R, 1, M, s.tw);
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    const int row = i / M, n = i - row * M;
+    const int row = kw_divu(i, P.dM), n = i - row * M;
     const float2 v = res[i];
     if (P.even) {
       rbuf[row * L + 2 * n] = v.x;
@@ -236,13 +237,13 @@ __device__ void rows_r2c(const RowsParams& P, const RowSmem& s, const float* rbu
   const int M = P.Mfft, L = P.L, R = P.R, H = P.H;
   const int tot = R * M;
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    const int row = i / M, n = i - row * M;
+    const int row = kw_divu(i, P.dM), n = i - row * M;
     s.A[i] = P.even ? make_float2(rbuf[row * L + 2 * n], rbuf[row * L + 2 * n + 1]) : make_float2(rbuf[row * L + n], 0.f);
   }
   float2* res = fft_smem<false>(s.A, s.B, P.flen, R, 1, M, s.tw);
   const int toth = R * H;
   for (int i = threadIdx.x; i < toth; i += blockDim.x) {
-    const int row = i / H, k = i - row * H;
+    const int row = kw_divu(i, P.dH), k = i - row * H;
     if (row >= nr) continue;
     float2 X;
     if (P.even) {
@@ -333,7 +334,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
   if (P.stage == ST_INIT) {
     // t = 0 with p0: p = p0, rho_i = p0 / (c0^2 D) (kspace_solver.py:729-733)
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int row = i / L, z = i - row * L;
+      const int row = kw_divu(i, P.dL), z = i - row * L;
       if (row >= nr) continue;
       const long long g = (long long)(r0 + row) * L + z;
       const float pv = P.p0_scale ? __fmul_rn(P.p0[g], *P.p0_scale) : P.p0[g];
@@ -356,7 +357,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
       rf.c2r(P, P.S[a], rb[0], r0, nr);
       float* u = P.u[a];
       for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-        const int row = i / L, z = i - row * L;
+        const int row = kw_divu(i, P.dL), z = i - row * L;
         if (row >= nr) continue;
         const long long g = (long long)(r0 + row) * L + z;
         const float gr = rb[0][i];
@@ -382,7 +383,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
       }
       __syncthreads();
       for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-        const int row = i / L, z = i - row * L;
+        const int row = kw_divu(i, P.dL), z = i - row * L;
         if (row >= nr) continue;
         u[(long long)(r0 + row) * L + z] = rb[0][i];
       }
@@ -397,7 +398,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
     // mass conservation with split density (kspace_solver.py:709-717)
     for (int a = 0; a < D; ++a) rf.c2r(P, P.S[a], rb[a], r0, nr);
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int row = i / L, z = i - row * L;
+      const int row = kw_divu(i, P.dL), z = i - row * L;
       if (row >= nr) continue;
       const long long g = (long long)(r0 + row) * L + z;
       const float r0v = fld(P.rho0, P.rho0_s, g);
@@ -430,7 +431,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
     __syncthreads();
     const bool powerlaw = P.absorb == 1;
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int row = i / L, z = i - row * L;
+      const int row = kw_divu(i, P.dL), z = i - row * L;
       if (row >= nr) continue;
       const long long g = (long long)(r0 + row) * L + z;
       float rs = rb[0][i];
@@ -504,7 +505,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
   if (P.stage == ST_P0FFT) {
     // spectrum of p0 for the smoothing window
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int row = i / L, z = i - row * L;
+      const int row = kw_divu(i, P.dL), z = i - row * L;
       rb[0][i] = (row < nr) ? P.p0w[(long long)(r0 + row) * L + z] : 0.f;
     }
     __syncthreads();
@@ -515,7 +516,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
   if (P.stage == ST_P0BACK) {
     rf.c2r(P, P.S[B_P], rb[0], r0, nr);
     for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-      const int row = i / L, z = i - row * L;
+      const int row = kw_divu(i, P.dL), z = i - row * L;
       if (row < nr) P.p0w[(long long)(r0 + row) * L + z] = rb[0][i];
     }
     return;
@@ -535,7 +536,7 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
   rf.c2r(P, P.S[0], rb[0], r0, nr);
   if (P.disp) rf.c2r(P, P.S[1], rb[1], r0, nr);
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    const int row = i / L, z = i - row * L;
+    const int row = kw_divu(i, P.dL), z = i - row * L;
     if (row >= nr) continue;
     const long long g = (long long)(r0 + row) * L + z;
     const float rs = P.rho_sum[g];

@@ -88,6 +88,7 @@ struct RowsParams {
   const int4* sens_ent;   // (row, pos, slot, 0)
   int nslots;
   float* rec[7];
+  KwDivU dM, dL, dH;      // division by Mfft, L and H (generic row kernels)
   // inside a replayed step graph: the plan's device step counter; t and
   // rec_row are then offsets added to it (nullptr: t and rec_row as given)
   const int* tdev;

@@ -83,6 +83,7 @@ bool na_factor(int n, KwFftLen& f) {
       f.radix[f.nst++] = r;
       m /= r;
     }
+  kw_fft_len_finish(f);
   return m == 1;
 }
 

@@ -195,6 +195,7 @@ static bool factor_len(int n, KwFftLen& f) {
       m /= r;
     }
   }
+  kw_fft_len_finish(f);
   return m == 1;
 }
 
@@ -681,6 +682,9 @@ static void fill_rows(const kw_plan* p, RowsParams& P) {
   P.even = p->even;
   P.nrows = p->nrows;
   P.R = p->R;
+  P.dM = kw_divu_make((uint32_t)p->Mfft);
+  P.dL = kw_divu_make((uint32_t)p->L);
+  P.dH = kw_divu_make((uint32_t)p->H);
   for (int b = 0; b < KW_NBUF; ++b) P.S[b] = p->d_S[b];
   for (int a = 0; a < 3; ++a) {
     P.inv_d[a] = a < p->D ? (float)(1.0 / p->g.spacing[a]) : 0.f;
