@@ -503,7 +503,9 @@ def run_transmit(args):
     probs = config3_problems(ninst, nt=nt, seed=1)
     cells = sum(int(np.prod(p["shape"])) for p in probs)
     stream = torch.cuda.current_stream()
-    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped)
+    t_setup = time.perf_counter()
+    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped, autotune=args.autotune)
+    t_setup = time.perf_counter() - t_setup
 
     def launches():
         return b.launch_count()
@@ -547,7 +549,7 @@ def run_transmit(args):
         cells_e2e = sum(int(np.prod(p["shape"])) for p in probs_e2e)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res = run_batch(probs_e2e)
+        res = run_batch(probs_e2e, grouped=args.grouped, autotune=args.autotune)
         t1 = time.perf_counter()
         assert len(res) == ninst and all(r["p"].shape[1] == 2000 for r in res)
         h2d = sum(sum(np.asarray(v).nbytes for v in (p["sound_speed"], p["density"], p["p"], p["p_mask"]))
@@ -576,6 +578,7 @@ def run_transmit(args):
         "data": "synthetic (seeded speckle media, discs, steering angles and grid sizes of the named ranges)",
         "config": {"workload": TRANSMIT_WORKLOAD, "instances": ninst, "cells_per_step": cells, "nt": nt,
                    "batch": "grouped launches" if args.grouped else "members as parallel graph branches",
+                   "autotune": bool(args.autotune), "setup_seconds": t_setup,
                    "l2": f"inputs larger than L2 ({cells * 4 * 12 / 1e9:.1f} GB of state, medium and spectra)"},
         "step_roofline": {"model_bytes_per_cell_step": TRANSMIT_A_MODEL, "achieved": step_gbs, "peak": peak,
                           "frac": step_gbs / peak, "unit": "GB/s", "peak_source": peak_kind},
@@ -604,6 +607,7 @@ def main(argv=None):
                     help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events")
     ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
     ap.add_argument("--grouped", action="store_true", help="transmit workload: grouped launches across members")
+    ap.add_argument("--autotune", action="store_true", help="transmit workload: autotune each member's launch geometry")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

@@ -148,6 +148,16 @@ int32_t kw_plan_finalize(kw_plan* plan);
  * call, the t = 0 initial-condition step and every step while timing is on are
  * plain launches.  Use one stream per plan. */
 int32_t kw_plan_run(kw_plan* plan, int32_t nsteps, void* stream);
+/* Autotuner of the run-time-length FFT kernels (the lengths that are not
+ * powers of two): times `nsteps` graph steps after the t = 0 step (at least
+ * 2, at most Nt - 1) for each candidate launch geometry -- tile columns T in
+ * {2, 4, 8, 16} of the axis passes, rows per block R in {R0/2, R0, 2 R0} of
+ * the row stages -- keeps the fastest and rewinds the plan to t = 0
+ * (kw_plan_reset).  The plan must be at
+ * t = 0.  Results are bit-identical for every choice.  *T_out / *R_out (may be
+ * NULL) receive the geometry in use; plans without such kernels are left as
+ * they are. */
+int32_t kw_plan_autotune(kw_plan* plan, int32_t nsteps, void* stream, int32_t* T_out, int32_t* R_out);
 /* enable == 0: every step as plain launches (default 1; the environment
  * variable KWAVE_GB300_GRAPHS=0 sets 0 at kw_plan_finalize). */
 int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);
@@ -162,6 +172,14 @@ int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);
 typedef struct kw_batch kw_batch;
 int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out);
 int32_t kw_batch_run(kw_batch* batch, int32_t nsteps, void* stream);
+/* Batch autotuner: one launch geometry of the run-time-length kernels for all
+ * members (T in {2, 4, 8, 16}, R = R0 * {1/2, 1, 2} of each member), each
+ * candidate timed on `nsteps` graph steps after the t = 0 step of the batch
+ * itself (fewer if a member is shorter; no tuning below 2); keeps the fastest
+ * and rewinds every plan to t = 0.  Every plan must be at t = 0.  Results are
+ * bit-identical for every choice. */
+int32_t kw_batch_autotune(kw_batch* batch, int32_t nsteps, void* stream, int32_t* T_out, int32_t* R_num,
+                          int32_t* R_den);
 /* Kernels launched through the batch and its plans since their creation (a
  * grouped launch over several plans counts once). */
 int32_t kw_batch_launch_count(const kw_batch* batch, int64_t* count);

@@ -431,6 +431,35 @@ static int zero_state(kw_plan* p) {
 
 static void dfree_last(kw_plan* p, void* ptr);
 
+static size_t rows_smem_bytes(const kw_plan* p, int R) {
+  return sizeof(float2) * ((size_t)p->Mfft + p->L / 2 + 1 + 2 * (size_t)R * p->Mfft) +
+         sizeof(float) * (size_t)KW_NREAL * R * p->L;
+}
+
+static int default_rows_per_block(const kw_plan* p) {
+  const int R = (p->L >= 2048) ? 1 : 2048 / p->L;
+  return R > 16 ? 16 : R;
+}
+
+// Launch geometry of the run-time-length kernels: R rows per row block and T
+// columns per axis tile (a power of two).  0 selects the defaults: 2048 / L
+// rows (at most 16) and 16 columns halved until a tile's buffers fit 100 KB.
+// Requested tiles are halved until they fit 200 KB.  The arithmetic of every
+// row and column transform is the same for any R and T.
+static void set_generic_geometry(kw_plan* p, int T_req, int R) {
+  p->R = R > 0 ? R : default_rows_per_block(p);
+  p->smem_rows = rows_smem_bytes(p, p->R);
+  for (int a = 0; a < p->D - 1; ++a) {
+    const int n = p->N[a];
+    int T = T_req > 0 ? T_req : 16;
+    const size_t cap = T_req > 0 ? 200 * 1024 : 100 * 1024;
+    while (T > 1 && (size_t)3 * n * T * sizeof(float2) > cap) T /= 2;
+    p->T_axis[a] = T;
+    p->smem_axis_plain[a] = sizeof(float2) * ((size_t)n + 2 * (size_t)n * T);
+    if (a == 0) p->smem_axis_ops = sizeof(float2) * ((size_t)n + 3 * (size_t)n * T);
+  }
+}
+
 int32_t kw_plan_finalize(kw_plan* p) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");
   if (p->finalized) return fail(KW_ERR_STATE, "plan already finalized");
@@ -581,19 +610,7 @@ int32_t kw_plan_finalize(kw_plan* p) {
   if ((rc = zero_state(p))) return rc;
 
   // launch geometry
-  p->R = (p->L >= 2048) ? 1 : 2048 / p->L;
-  if (p->R > 16) p->R = 16;
-  p->smem_rows = sizeof(float2) * ((size_t)p->Mfft + p->L / 2 + 1 + 2 * (size_t)p->R * p->Mfft) +
-                 sizeof(float) * (size_t)KW_NREAL * p->R * p->L;
-  for (int a = 0; a < D - 1; ++a) {
-    int n = p->N[a];
-    int T = 16;
-    while (T > 1 && (size_t)3 * n * T * sizeof(float2) > 100 * 1024) T /= 2;
-    p->T_axis[a] = T;
-    p->smem_axis_plain[a] = sizeof(float2) * ((size_t)n + 2 * (size_t)n * T);
-    size_t ops = sizeof(float2) * ((size_t)n + 3 * (size_t)n * T);
-    if (a == 0) p->smem_axis_ops = ops;
-  }
+  set_generic_geometry(p, 0, 0);
   CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   CK(cudaFuncSetAttribute(k_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   CK(cudaFuncSetAttribute(k_rows_group, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -1150,17 +1167,88 @@ static int run_step(kw_plan* p, int t, int end, cudaStream_t st) {
   return KW_OK;
 }
 
+// plain_last == false (autotuning only): the last step is a graph step too and
+// leaves p in spectral form only.
+static int plan_run(kw_plan* p, int nsteps, cudaStream_t st, bool plain_last) {
+  const int end = std::min(p->g.Nt, p->t + nsteps);
+  const int eend = plain_last ? end : end + 1;
+  for (int t = p->t; t < end; ++t) {
+    int rc = run_step(p, t, eend, st);
+    if (rc) return rc;
+    p->t = t + 1;
+  }
+  return KW_OK;
+}
+
 int32_t kw_plan_run(kw_plan* p, int32_t nsteps, void* stream) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");
   if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_run before kw_plan_finalize");
   if (nsteps < 0) return fail(KW_ERR_INVALID, "nsteps < 0");
+  return plan_run(p, nsteps, reinterpret_cast<cudaStream_t>(stream), true);
+}
+
+// Times the plan's first `nsteps` steps for each candidate geometry of the
+// run-time-length kernels (tile columns T in {2, 4, 8, 16}, rows per block
+// R in {R0/2, R0, 2 R0}), keeps the fastest and rewinds the plan to t = 0.
+// Results do not depend on the choice.
+int32_t kw_plan_autotune(kw_plan* p, int32_t nsteps, void* stream, int32_t* T_out, int32_t* R_out) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_autotune before kw_plan_finalize");
+  if (p->t != 0) return fail(KW_ERR_STATE, "kw_plan_autotune needs a plan at t = 0 (kw_plan_reset first)");
+  bool gen_axis = false;
+  for (int a = 0; a < p->D - 1; ++a) gen_axis |= !p->tma_axis[a] && !p->axis_reg[a];
+  const bool gen_rows = !p->rows_reg;
+  const int k = std::min(std::max(2, (int)nsteps), p->g.Nt - 1);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  const int end = std::min(p->g.Nt, p->t + nsteps);
-  for (int t = p->t; t < end; ++t) {
-    int rc = run_step(p, t, end, st);
+  if ((gen_axis || gen_rows) && k >= 2) {
+    const int R0 = default_rows_per_block(p);
+    std::vector<int> Ts = gen_axis ? std::vector<int>{2, 4, 8, 16} : std::vector<int>{0};
+    std::vector<int> Rs{R0};
+    if (gen_rows) {
+      if (R0 > 1) Rs.push_back(std::max(1, R0 / 2));
+      if (rows_smem_bytes(p, 2 * R0) <= 200 * 1024) Rs.push_back(2 * R0);
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestT = 0, bestR = R0, rc = KW_OK;
+    const bool timing = p->timing;
+    p->timing = false;
+    for (int T : Ts) {
+      for (int R : Rs) {
+        set_generic_geometry(p, T, R);
+        drop_graphs(p);
+        // one untimed pass captures the step graphs; the timed steps follow
+        // the t = 0 step and are all graph steps
+        if ((rc = plan_run(p, 1 + k, st, false)) || (rc = kw_plan_reset(p)) || (rc = plan_run(p, 1, st, false)))
+          break;
+        float ms = 0.f;
+        if (cudaEventRecord(e0, st) != cudaSuccess) rc = fail(KW_ERR_CUDA, "autotune event");
+        if (!rc) rc = plan_run(p, k, st, false);
+        if (!rc && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+          rc = fail(KW_ERR_CUDA, "autotune timing");
+        if (!rc) rc = kw_plan_reset(p);
+        if (rc) break;
+        if (ms < best) {
+          best = ms;
+          bestT = T;
+          bestR = R;
+        }
+      }
+      if (rc) break;
+    }
+    p->timing = timing;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    set_generic_geometry(p, bestT, bestR);
+    drop_graphs(p);
     if (rc) return rc;
-    p->t = t + 1;
+    if ((rc = kw_plan_reset(p))) return rc;
   }
+  if (T_out) *T_out = p->D > 1 ? p->T_axis[0] : 0;
+  if (R_out) *R_out = p->R;
   return KW_OK;
 }
 
@@ -1347,16 +1435,14 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
   return KW_OK;
 }
 
-int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
-  if (!b) return fail(KW_ERR_INVALID, "null batch");
-  if (nsteps < 0) return fail(KW_ERR_INVALID, "nsteps < 0");
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+static int batch_run(kw_batch* b, int nsteps, cudaStream_t st, bool plain_last) {
   const size_t n = b->plans.size();
-  std::vector<int> end(n), keys(n);
+  std::vector<int> end(n), eend(n), keys(n);
   int span = 0;
   for (size_t i = 0; i < n; ++i) {
     kw_plan* p = b->plans[i];
     end[i] = std::min(p->g.Nt, p->t + nsteps);
+    eend[i] = plain_last ? end[i] : end[i] + 1;
     span = std::max(span, end[i] - p->t);
   }
   for (int s = 0; s < span; ++s) {
@@ -1365,7 +1451,7 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
       kw_plan* p = b->plans[i];
       keys[i] = -1;
       if (p->t >= end[i]) continue;
-      if (step_eager(p, p->t, end[i])) {
+      if (step_eager(p, p->t, eend[i])) {
         together = false;
         continue;
       }
@@ -1377,7 +1463,7 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
       for (size_t i = 0; i < n; ++i) {
         kw_plan* p = b->plans[i];
         if (p->t >= end[i]) continue;
-        if ((rc = run_step(p, p->t, end[i], st))) return rc;
+        if ((rc = run_step(p, p->t, eend[i], st))) return rc;
         p->t += 1;
       }
       continue;
@@ -1397,6 +1483,102 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
     }
   }
   return KW_OK;
+}
+
+int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
+  if (!b) return fail(KW_ERR_INVALID, "null batch");
+  if (nsteps < 0) return fail(KW_ERR_INVALID, "nsteps < 0");
+  return batch_run(b, nsteps, reinterpret_cast<cudaStream_t>(stream), true);
+}
+
+static void batch_clear(kw_batch* b) {
+  cudaDeviceSynchronize();
+  for (auto& g : b->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  b->graphs.clear();
+  for (void* a : b->allocs) cudaFree(a);
+  b->allocs.clear();
+}
+
+static int batch_reset(kw_batch* b) {
+  for (kw_plan* p : b->plans) {
+    int rc = kw_plan_reset(p);
+    if (rc) return rc;
+  }
+  return KW_OK;
+}
+
+// Batch counterpart of kw_plan_autotune: one geometry for all members (tile
+// columns T, rows per block R = f * R0 of each member), timed on the batch
+// itself, since members running together favour other shapes than a member
+// alone.
+int32_t kw_batch_autotune(kw_batch* b, int32_t nsteps, void* stream, int32_t* T_out, int32_t* R_num,
+                          int32_t* R_den) {
+  if (!b) return fail(KW_ERR_INVALID, "null batch");
+  for (kw_plan* p : b->plans)
+    if (p->t != 0) return fail(KW_ERR_STATE, "kw_batch_autotune needs every plan at t = 0");
+  bool any = false;
+  for (kw_plan* p : b->plans) {
+    bool g = !p->rows_reg;
+    for (int a = 0; a < p->D - 1; ++a) g |= !p->tma_axis[a] && !p->axis_reg[a];
+    any |= g;
+  }
+  int bestT = 0, bestN = 1, bestD = 1;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc = KW_OK;
+  // timed steps: at most one less than the shortest member's Nt
+  int k = std::max(2, (int)nsteps);
+  for (kw_plan* p : b->plans) k = std::min(k, p->g.Nt - 1);
+  if (any && k >= 2) {
+    const int Ts[4] = {2, 4, 8, 16};
+    const int fr[3][2] = {{1, 2}, {1, 1}, {2, 1}};  // R = R0 * num / den
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int ti = 0; ti < 4 && !rc; ++ti)
+      for (int fi = 0; fi < 3 && !rc; ++fi) {
+        bool fits = true;
+        for (kw_plan* p : b->plans) {
+          const int R = std::max(1, default_rows_per_block(p) * fr[fi][0] / fr[fi][1]);
+          if (rows_smem_bytes(p, R) > 200 * 1024) fits = false;
+        }
+        if (!fits) continue;
+        for (kw_plan* p : b->plans) {
+          set_generic_geometry(p, Ts[ti], std::max(1, default_rows_per_block(p) * fr[fi][0] / fr[fi][1]));
+          drop_graphs(p);
+        }
+        batch_clear(b);
+        // one untimed pass builds the graphs; the timed steps follow the
+        // t = 0 step and are all graph steps
+        if ((rc = batch_run(b, 1 + k, st, false)) || (rc = batch_reset(b)) || (rc = batch_run(b, 1, st, false))) break;
+        float ms = 0.f;
+        if (cudaEventRecord(e0, st) != cudaSuccess) rc = fail(KW_ERR_CUDA, "autotune event");
+        if (!rc) rc = batch_run(b, k, st, false);
+        if (!rc && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+          rc = fail(KW_ERR_CUDA, "autotune timing");
+        if (!rc) rc = batch_reset(b);
+        if (!rc && ms < best) {
+          best = ms;
+          bestT = Ts[ti];
+          bestN = fr[fi][0];
+          bestD = fr[fi][1];
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (kw_plan* p : b->plans) {
+      set_generic_geometry(p, bestT, std::max(1, default_rows_per_block(p) * bestN / bestD));
+      drop_graphs(p);
+    }
+    batch_clear(b);
+    if (!rc) rc = batch_reset(b);
+  }
+  if (T_out) *T_out = bestT;
+  if (R_num) *R_num = bestN;
+  if (R_den) *R_den = bestD;
+  return rc;
 }
 
 int32_t kw_batch_launch_count(const kw_batch* b, int64_t* count) {

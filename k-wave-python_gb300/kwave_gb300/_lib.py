@@ -78,10 +78,13 @@ _PROTOS = {
     "kw_plan_finalize": (C.c_int32, [_P]),
     "kw_plan_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_plan_set_graphs": (C.c_int32, [_P, C.c_int32]),
+    "kw_plan_autotune": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "kw_batch_create": (C.c_int32, [_P, C.c_int32, C.POINTER(_P)]),
     "kw_batch_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_batch_destroy": (C.c_int32, [_P]),
     "kw_batch_launch_count": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
+    "kw_batch_autotune": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int32)]),
     "kw_plan_sync": (C.c_int32, [_P, _P]),
     "kw_plan_time_index": (C.c_int32, [_P, C.POINTER(C.c_int32)]),
     "kw_plan_read_series": (C.c_int32, [_P, C.c_int32, _P, C.c_int64]),

@@ -140,6 +140,16 @@ class DevicePlan:
         st = C.c_void_p(self.stream) if self.stream is not None else None
         K.check(self.lib.kw_plan_sync(self._h, st))
 
+    def autotune(self, nsteps=6):
+        """Pick the launch geometry of the run-time-length FFT kernels by timing
+        the first ``nsteps`` steps for each candidate (kw_plan_autotune); the
+        plan is left at t = 0 and results do not depend on the choice.
+        Returns (tile columns, rows per block)."""
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        T, R = C.c_int32(), C.c_int32()
+        K.check(self.lib.kw_plan_autotune(self._h, int(nsteps), st, C.byref(T), C.byref(R)))
+        return T.value, R.value
+
     def set_graphs(self, enable):
         """Run repeated steps as replayed CUDA graphs (default) or as plain launches."""
         K.check(self.lib.kw_plan_set_graphs(self._h, int(bool(enable))))
@@ -216,13 +226,16 @@ class Simulation:
         return obj
 
     # -- setup / stepping ---------------------------------------------------
-    def setup(self, generic_fft=False):
+    def setup(self, generic_fft=False, autotune=False):
         """Host set-up and device plan.  ``generic_fft`` runs every pass with
         the run-time-length FFT kernels (what lets a batch group the plan's
         passes with other plans); the default picks the fastest kernels for
-        the grid."""
+        the grid.  ``autotune`` times the candidate launch geometries of the
+        run-time-length kernels on the first steps and keeps the fastest."""
         self.S = build_setup(self.prob, derive_on_device=True)
         self._plan = DevicePlan(self.S, stream=self.stream, generic_fft=generic_fft)
+        if autotune:
+            self.tuned = self._plan.autotune()
         self.t = 0
         return self
 
@@ -321,13 +334,15 @@ class SimulationBatch:
     parallel branch holding its own step graph.  With ``grouped=True`` the
     members set up here use the run-time-length FFT kernels, and the k-th pass
     of every member runs in one grouped launch over all of them (a handful of
-    launches per step whatever the batch size).  The reference has no batch
-    object: it runs ``Simulation.run()`` (kwave/solvers/kspace_solver.py:
-    749-778) once per simulation, and a loop over members here gives the same
-    results.
+    launches per step whatever the batch size).  ``autotune=True`` times
+    candidate launch geometries of the run-time-length FFT kernels on the
+    batch's first steps and keeps the fastest (results do not depend on it).
+    The reference has no batch object: it runs ``Simulation.run()``
+    (kwave/solvers/kspace_solver.py:749-778) once per simulation, and a loop
+    over members here gives the same results.
     """
 
-    def __init__(self, sims, stream=None, grouped=False):
+    def __init__(self, sims, stream=None, grouped=False, autotune=False):
         self.sims = list(sims)
         if not self.sims:
             raise ValueError("SimulationBatch needs at least one simulation")
@@ -341,10 +356,25 @@ class SimulationBatch:
         handles = (C.c_void_p * len(self.sims))(*[s._plan.handle for s in self.sims])
         self._h = C.c_void_p()
         K.check(lib.kw_batch_create(handles, len(self.sims), C.byref(self._h)))
+        self.tuned = None
+        if autotune:
+            self.tuned = self.autotune()
+
+    def autotune(self, nsteps=8):
+        """One launch geometry of the run-time-length kernels for all members,
+        timed on the batch itself (kw_batch_autotune); every member must be at
+        t = 0 and is rewound there.  Returns (tile columns, rows-per-block factor)."""
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        T, num, den = C.c_int32(), C.c_int32(), C.c_int32()
+        K.check(self.lib.kw_batch_autotune(self._h, int(nsteps), st, C.byref(T), C.byref(num), C.byref(den)))
+        for s in self.sims:
+            s.t = s._plan.time_index()
+        return T.value, num.value / den.value
 
     @classmethod
-    def from_problems(cls, problems, stream=None, grouped=False):
-        return cls([Simulation.from_problem(p, stream=stream) for p in problems], stream=stream, grouped=grouped)
+    def from_problems(cls, problems, stream=None, grouped=False, autotune=False):
+        return cls([Simulation.from_problem(p, stream=stream) for p in problems], stream=stream, grouped=grouped,
+                   autotune=autotune)
 
     def launch_count(self):
         c = C.c_int64()
@@ -379,9 +409,9 @@ class SimulationBatch:
             pass
 
 
-def run_batch(problems, stream=None, grouped=False):
+def run_batch(problems, stream=None, grouped=False, autotune=False):
     """Set up, run together and close the simulations described by plain problem dicts."""
-    b = SimulationBatch.from_problems(problems, stream=stream, grouped=grouped)
+    b = SimulationBatch.from_problems(problems, stream=stream, grouped=grouped, autotune=autotune)
     try:
         return b.run()
     finally:

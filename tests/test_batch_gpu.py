@@ -138,6 +138,55 @@ def test_batch_uneven_chunks(golden_generic):
         b.close()
 
 
+def test_autotune_bit_exact():
+    """The autotuner changes only the launch geometry of the run-time-length
+    kernels: results stay bit-identical, the plan is rewound to t = 0, and a
+    power-of-two plan keeps its kernels."""
+    import bench
+    from kwave_gb300.solver import Simulation
+
+    prob = bench.transmit_problem((90, 150), 11, nt=40, n_elem=6, pml=12)
+    ref = plain_run(prob)
+    sim = Simulation.from_problem(prob)
+    sim.setup(autotune=True)
+    try:
+        T, R = sim.tuned
+        assert T in (2, 4, 8, 16) and R >= 1, sim.tuned
+        assert sim._plan.time_index() == 0
+        assert_same("autotuned", sim.run(), ref)
+    finally:
+        sim.close()
+    prob2 = bench.transmit_problem((64, 128), 12, nt=20, n_elem=6, pml=12)
+    sim = Simulation.from_problem(prob2)
+    sim.setup(autotune=True)
+    try:
+        assert_same("autotuned pow2", sim.run(), plain_run(prob2))
+    finally:
+        sim.close()
+
+
+def test_batch_autotune_bit_exact(golden_generic):
+    from kwave_gb300.solver import SimulationBatch
+
+    names = sorted(golden_generic)[:6]
+    for grouped in (False, True):
+        b = SimulationBatch.from_problems([golden_generic[n][0] for n in names], grouped=grouped, autotune=True)
+        try:
+            T, f = b.tuned
+            assert T in (0, 2, 4, 8, 16) and f in (0.5, 1.0, 2.0), b.tuned
+            assert all(s.t == 0 for s in b.sims)
+            for name, res in zip(names, b.run()):
+                if grouped:
+                    assert_same(name, res, golden_generic[name][1])
+                else:
+                    _, r32, r64, _ = load_case(name)
+                    for k in r32:
+                        e32, gap = rel_l2(res[k], r32[k]), rel_l2(r32[k], r64[k])
+                        assert e32 <= TOL or rel_l2(res[k], r64[k]) <= 1.5 * gap + 1e-6, (name, k, e32)
+        finally:
+            b.close()
+
+
 TRANSMIT = [((96, 120), 1), ((75, 135), 2), ((128, 100), 3), ((90, 144), 4), ((81, 96), 5), ((64, 128), 6)]
 
 
