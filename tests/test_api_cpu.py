@@ -284,3 +284,23 @@ def test_cart2grid_matches_reference():
             for a, b in zip(mine, theirs):
                 assert np.asarray(a).shape == np.asarray(b).shape
                 assert np.array_equal(np.asarray(a), np.asarray(b)), (N, order)
+
+
+def test_batch_host_checks():
+    """Host-side checks of the batch API that need no GPU: an empty batch is
+    refused before any device call, and the transmit-event generator gives
+    the shapes the batched workload is quoted on."""
+    import bench
+    from kwave_gb300.solver import SimulationBatch
+
+    with pytest.raises(ValueError):
+        SimulationBatch([])
+    sizes = bench._five_smooth(192, 512)
+    assert sizes[0] == 192 and sizes[-1] == 512 and 243 in sizes and 250 in sizes and 7 * 32 not in sizes
+    probs = bench.config3_problems(3, nt=50, seed=4)
+    for p in probs:
+        assert all(n in sizes for n in p["shape"])
+        n_src = int(p["p_mask"].sum())
+        assert n_src == 32 * 3 and p["p"].shape[0] == n_src
+        assert p["dt"] <= 0.3 * 5e-5 / p["sound_speed"].max() * (1 + 1e-12)
+        assert np.array_equal(p["sensor_mask"], p["p_mask"])
