@@ -506,6 +506,7 @@ def run_transmit(args):
     t_setup = time.perf_counter()
     b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped, autotune=args.autotune)
     t_setup = time.perf_counter() - t_setup
+    tuned = b.tuned
 
     def launches():
         return b.launch_count()
@@ -578,7 +579,7 @@ def run_transmit(args):
         "data": "synthetic (seeded speckle media, discs, steering angles and grid sizes of the named ranges)",
         "config": {"workload": TRANSMIT_WORKLOAD, "instances": ninst, "cells_per_step": cells, "nt": nt,
                    "batch": "grouped launches" if args.grouped else "members as parallel graph branches",
-                   "autotune": bool(args.autotune), "setup_seconds": t_setup,
+                   "autotune": bool(args.autotune), "tuned": tuned, "setup_seconds": t_setup,
                    "l2": f"inputs larger than L2 ({cells * 4 * 12 / 1e9:.1f} GB of state, medium and spectra)"},
         "step_roofline": {"model_bytes_per_cell_step": TRANSMIT_A_MODEL, "achieved": step_gbs, "peak": peak,
                           "frac": step_gbs / peak, "unit": "GB/s", "peak_source": peak_kind},

@@ -443,15 +443,17 @@ static int default_rows_per_block(const kw_plan* p) {
 
 // Launch geometry of the run-time-length kernels: R rows per row block and T
 // columns per axis tile (a power of two).  0 selects the defaults: 2048 / L
-// rows (at most 16) and 16 columns halved until a tile's buffers fit 100 KB.
-// Requested tiles are halved until they fit 200 KB.  The arithmetic of every
-// row and column transform is the same for any R and T.
+// rows (at most 16) and 4 columns (one 32-byte sector per tile row; what the
+// autotuner picked for batched 2-D events of 192..512 points) halved until a
+// tile's buffers fit 100 KB.  Requested tiles are halved until they fit
+// 200 KB.  The arithmetic of every row and column transform is the same for
+// any R and T.
 static void set_generic_geometry(kw_plan* p, int T_req, int R) {
   p->R = R > 0 ? R : default_rows_per_block(p);
   p->smem_rows = rows_smem_bytes(p, p->R);
   for (int a = 0; a < p->D - 1; ++a) {
     const int n = p->N[a];
-    int T = T_req > 0 ? T_req : 16;
+    int T = T_req > 0 ? T_req : 4;
     const size_t cap = T_req > 0 ? 200 * 1024 : 100 * 1024;
     while (T > 1 && (size_t)3 * n * T * sizeof(float2) > cap) T /= 2;
     p->T_axis[a] = T;
