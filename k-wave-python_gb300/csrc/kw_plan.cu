@@ -1276,6 +1276,13 @@ struct kw_batch {
   std::vector<void*> allocs;
   cudaStream_t cap = nullptr;
   long long launches = 0;
+  // steps whose key vector has no batch graph yet and differs from the
+  // previous step's: the members' own step graphs on side streams
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> side_done;
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<int> last_keys;
+  int repeat = 0;
 };
 
 int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
@@ -1437,6 +1444,52 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
   return KW_OK;
 }
 
+static kw_batch::Graph* find_batch_graph(kw_batch* b, const std::vector<int>& keys) {
+  for (auto& g : b->graphs)
+    if (g.keys == keys) return &g;
+  return nullptr;
+}
+
+// One step of every stepping member through its own step graph, members
+// spread over up to 16 side streams forked from and joined back into `st`.
+static int batch_step_streams(kw_batch* b, const std::vector<int>& keys, cudaStream_t st) {
+  const size_t n = b->plans.size();
+  if (b->side.empty()) {
+    const size_t ns = std::min<size_t>(n, 16);
+    for (size_t s = 0; s < ns; ++s) {
+      cudaStream_t x;
+      cudaEvent_t e;
+      CK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      b->side.push_back(x);
+      CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      b->side_done.push_back(e);
+    }
+    CK(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+  }
+  const size_t ns = b->side.size();
+  std::vector<kw_plan::StepGraph*> sg(n, nullptr);
+  int rc;
+  for (size_t i = 0; i < n; ++i)
+    if (keys[i] >= 0 && (rc = step_graph(b->plans[i], b->plans[i]->t, &sg[i]))) return rc;
+  CK(cudaEventRecord(b->fork_ev, st));
+  for (size_t s = 0; s < ns; ++s) CK(cudaStreamWaitEvent(b->side[s], b->fork_ev, 0));
+  for (size_t i = 0; i < n; ++i) {
+    if (keys[i] < 0) continue;
+    kw_plan* p = b->plans[i];
+    cudaStream_t x = b->side[i % ns];
+    if ((rc = step_counter_to(p, p->t, x))) return rc;
+    CK(cudaGraphLaunch(sg[i]->exec, x));
+    p->tstep_val = p->t + 1;
+    p->launches += sg[i]->nlaunch;
+    p->t += 1;
+  }
+  for (size_t s = 0; s < ns; ++s) {
+    CK(cudaEventRecord(b->side_done[s], b->side[s]));
+    CK(cudaStreamWaitEvent(st, b->side_done[s], 0));
+  }
+  return KW_OK;
+}
+
 static int batch_run(kw_batch* b, int nsteps, cudaStream_t st, bool plain_last) {
   const size_t n = b->plans.size();
   std::vector<int> end(n), eend(n), keys(n);
@@ -1470,8 +1523,23 @@ static int batch_run(kw_batch* b, int nsteps, cudaStream_t st, bool plain_last) 
       }
       continue;
     }
-    kw_batch::Graph* g = nullptr;
-    if ((rc = batch_graph(b, keys, &g))) return rc;
+    // a batch graph is built for a key vector seen on two steps in a row;
+    // while members switch sources off one by one the keys change every
+    // step, and those steps run on side streams instead of one-off graphs
+    kw_batch::Graph* g = find_batch_graph(b, keys);
+    if (!g) {
+      if (keys == b->last_keys) {
+        ++b->repeat;
+      } else {
+        b->last_keys = keys;
+        b->repeat = 0;
+      }
+      if (b->repeat >= 1 && (rc = batch_graph(b, keys, &g))) return rc;
+    }
+    if (!g) {
+      if ((rc = batch_step_streams(b, keys, st))) return rc;
+      continue;
+    }
     for (size_t i = 0; i < n; ++i)
       if (keys[i] >= 0 && (rc = step_counter_to(b->plans[i], b->plans[i]->t, st))) return rc;
     CK(cudaGraphLaunch(g->exec, st));
@@ -1596,6 +1664,9 @@ int32_t kw_batch_destroy(kw_batch* b) {
   for (auto& g : b->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
   if (b->cap) cudaStreamDestroy(b->cap);
+  for (cudaStream_t x : b->side) cudaStreamDestroy(x);
+  for (cudaEvent_t e : b->side_done) cudaEventDestroy(e);
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   for (void* a : b->allocs) cudaFree(a);
   delete b;
   return KW_OK;
