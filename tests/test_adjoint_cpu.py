@@ -1,0 +1,136 @@
+"""The FP64 adjoint oracle of the lossless time loop.
+
+The oracle is checked in four ways:
+
+* its forward map against the FP64 solver oracle (itself pinned to the
+  reference);
+* the dot-product test <F x, y> = <x, F^T y>;
+* central finite differences for the misfit gradients with respect to p0
+  and c;
+* PyTorch FP64 autograd through the same forward steps.
+
+It is what a GPU adjoint of the time loop will be checked against.
+"""
+import numpy as np
+import pytest
+
+from oracle.adjoint_oracle import AdjointOracle
+from oracle.kspace_oracle import OracleSimulation
+
+
+def circle(n, radius):
+    th = 2 * np.pi * np.arange(n) / n
+    return np.stack([radius * np.cos(th), radius * np.sin(th)])
+
+
+def problem(shape=(40, 44), nt=48, cartesian=True, record_start=1, seed=5):
+    rng = np.random.default_rng(seed)
+    gx, gy = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
+    p0 = np.zeros(shape)
+    for _ in range(3):
+        cx, cy = rng.uniform(14, shape[0] - 14), rng.uniform(14, shape[1] - 14)
+        p0 += rng.uniform(0.5, 2) * np.exp(-((gx - cx) ** 2 + (gy - cy) ** 2) / (2 * rng.uniform(1.5, 3) ** 2))
+    c = 1500.0 * (1 + 0.03 * np.tanh(rng.standard_normal(shape)))
+    rho = 1000.0 * (1 + 0.02 * np.tanh(rng.standard_normal(shape)))
+    if cartesian:
+        mask = circle(24, 1.3e-3)
+    else:
+        mask = np.zeros(shape, bool)
+        mask[10, 8:-8] = True
+        mask[-11, 8:-8] = True
+    return dict(shape=shape, spacing=(1e-4, 1e-4), dt=0.3 * 1e-4 / c.max(), Nt=nt, sound_speed=c, density=rho,
+                p0=p0, smooth_p0=False, sensor_mask=mask, record=("p",), record_start_index=record_start,
+                pml_size=(8, 8), pml_alpha=(2.0, 2.0), use_sg=True, use_kspace=True)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+
+
+@pytest.mark.parametrize("cartesian", [True, False])
+def test_forward_matches_solver_oracle(cartesian):
+    prob = problem(cartesian=cartesian)
+    A = AdjointOracle(prob)
+    ref = OracleSimulation(prob, np.float64).run()["p"]
+    assert rel(A.forward(prob["p0"]), ref) < 1e-12
+
+
+@pytest.mark.parametrize("cartesian,record_start", [(True, 1), (False, 6)])
+def test_dot_product(cartesian, record_start):
+    prob = problem(cartesian=cartesian, record_start=record_start)
+    A = AdjointOracle(prob)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(prob["shape"])
+    y = rng.standard_normal((A.S.shape[0], A.Nt - A.rs))
+    lhs = float(np.sum(A.forward(x) * y))
+    rhs = float(np.sum(x * A.adjoint(y)))
+    assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), 1e-300), (lhs, rhs)
+
+
+def test_gradients_against_finite_differences():
+    prob = problem()
+    A = AdjointOracle(prob)
+    rng = np.random.default_rng(2)
+    p_true = prob["p0"]
+    d_obs = A.forward(p_true) + 0.01 * rng.standard_normal((A.S.shape[0], A.Nt - A.rs))
+    p0 = 0.7 * p_true
+    c = A.c
+    L, g_p0, g_c = A.misfit_gradient(p0, d_obs, c)
+    # p0: the misfit is quadratic in p0, so central differences are exact to rounding
+    v = rng.standard_normal(p0.shape)
+    h = 1e-3
+    fd = (A.misfit_gradient(p0 + h * v, d_obs, c)[0] - A.misfit_gradient(p0 - h * v, d_obs, c)[0]) / (2 * h)
+    assert abs(fd - np.sum(g_p0 * v)) <= 1e-7 * abs(fd), (fd, np.sum(g_p0 * v))
+    # c: smooth perturbation, second-order differences
+    w = np.exp(-(((np.arange(p0.shape[0])[:, None] - 20) ** 2 + (np.arange(p0.shape[1])[None, :] - 22) ** 2) / 40.0))
+    h = 0.05
+    fd = (A.misfit_gradient(p0, d_obs, c + h * w)[0] - A.misfit_gradient(p0, d_obs, c - h * w)[0]) / (2 * h)
+    assert abs(fd - np.sum(g_c * w)) <= 1e-6 * abs(fd), (fd, np.sum(g_c * w))
+
+
+def test_gradients_against_torch_autograd():
+    torch = pytest.importorskip("torch")
+    prob = problem(shape=(36, 40), nt=40)
+    A = AdjointOracle(prob)
+    rng = np.random.default_rng(3)
+    d_obs = A.forward(prob["p0"]) + 0.01 * rng.standard_normal((A.S.shape[0], A.Nt - A.rs))
+    p0_np = 0.5 * prob["p0"]
+    L, g_p0, g_c = A.misfit_gradient(p0_np, d_obs)
+
+    T = lambda a: torch.as_tensor(np.asarray(a), dtype=torch.float64)  # noqa: E731
+    Tc = lambda a: torch.as_tensor(np.asarray(a), dtype=torch.complex128)  # noqa: E731
+    og, od = [Tc(o) for o in A.og], [Tc(o) for o in A.od]
+    m, sg, a = [T(x) for x in A.m], [T(x) for x in A.sg], [T(x) for x in A.a]
+    b, S = T(A.b), T(A.S)
+    p0 = T(p0_np).requires_grad_(True)
+    c = T(A.c).requires_grad_(True)
+    c2 = c * c
+    D = A.ndim
+    G = lambda i, f: torch.fft.ifftn(og[i] * torch.fft.fftn(f)).real  # noqa: E731
+    Dv = lambda i, f: torch.fft.ifftn(od[i] * torch.fft.fftn(f)).real  # noqa: E731
+    p = p0
+    rho = [p0 / (c2 * D) for _ in range(D)]
+    u = [(a[i] / 2) * G(i, p0) for i in range(D)]
+    rec = [S @ p.reshape(-1)]
+    for _ in range(1, A.Nt):
+        u = [sg[i] * (sg[i] * u[i] - a[i] * G(i, p)) for i in range(D)]
+        rho = [m[i] * (m[i] * rho[i] - b * Dv(i, u[i])) for i in range(D)]
+        s = rho[0]
+        for r in rho[1:]:
+            s = s + r
+        p = c2 * s
+        rec.append(S @ p.reshape(-1))
+    d = torch.stack(rec, dim=1)
+    loss = 0.5 * ((d - T(d_obs)) ** 2).sum()
+    loss.backward()
+    assert abs(loss.item() - L) <= 1e-12 * L
+    assert rel(g_p0, p0.grad.numpy()) < 1e-10
+    assert rel(g_c, c.grad.numpy()) < 1e-10
+
+
+def test_rejects_what_it_does_not_cover():
+    prob = problem()
+    with pytest.raises(ValueError):
+        AdjointOracle(dict(prob, alpha_coeff=0.5, alpha_power=1.5))
+    with pytest.raises(ValueError):
+        AdjointOracle(dict(prob, smooth_p0=True))
