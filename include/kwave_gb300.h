@@ -158,6 +158,16 @@ int32_t kw_plan_run(kw_plan* plan, int32_t nsteps, void* stream);
  * NULL) receive the geometry in use; plans without such kernels are left as
  * they are. */
 int32_t kw_plan_autotune(kw_plan* plan, int32_t nsteps, void* stream, int32_t* T_out, int32_t* R_out);
+/* Adjoint of the time loop (no counterpart in the reference): the gradient
+ * with respect to p0 of sum over sensor points and recorded steps of
+ * residual * recorded p, i.e. the transposed time loop applied to `residual`
+ * (sensor-major (n_points, Nt - record_start), the layout of
+ * kw_plan_read_series).  For the lossless, source-free loop with a binary
+ * sensor recording p and smoothing off; `grad` receives N_total float32 (C
+ * order).  With residual = recorded p - observed data it is the gradient of
+ * 1/2 ||recorded p - observed||^2.  The plan is reset (t = 0, zero state)
+ * before and after; its uploaded medium, PML and sensor are used. */
+int32_t kw_plan_adjoint_p0(kw_plan* plan, const float* residual, int64_t n, float* grad, void* stream);
 /* enable == 0: every step as plain launches (default 1; the environment
  * variable KWAVE_GB300_GRAPHS=0 sets 0 at kw_plan_finalize). */
 int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);

@@ -307,6 +307,21 @@ __device__ void record_samples(const RowsParams& P, const float* rbuf, float* re
   }
 }
 
+// lp += S^T r at this block's sensor points (binary sensor: one slot per grid
+// point; r is time-major in rec[0], row kw_rec_row(P)).
+__device__ void add_residual(const RowsParams& P, float* rbuf, int r0, int nr) {
+  const int rr = kw_rec_row(P);
+  const float* res = P.rec[0];
+  if (res == nullptr || rr < 0 || P.sens_row_ptr == nullptr) return;
+  const int e0 = P.sens_row_ptr[r0], e1 = P.sens_row_ptr[r0 + nr];
+  const float* in = res + (long long)rr * P.nslots;
+  for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int4 en = P.sens_ent[e];
+    float& f = rbuf[(en.x - r0) * P.L + en.y];
+    f = __fadd_rn(f, in[en.z]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // row stage kernels: one physics body, two row-FFT implementations
 // ---------------------------------------------------------------------------
@@ -320,6 +335,97 @@ struct GenericRowFFT {
     rows_r2c(P, s, rbuf, S, r0, nr);
   }
 };
+
+// Transposed step of the lossless, source-free time loop
+// (kspace_solver.py:700-723 with alpha = 0, B/A = 0).  With G_i = Re F^-1
+// [op_grad_i F .], D_i = Re F^-1[op_div_i F .] and G_i^T = -D_i, one step
+// back from the adjoint (lp, lu_i, lr_i) of the state after step t is
+//   ADJ_A: lp += S^T r_t; lr_i' = lr_i + c^2 lp; lr_i <- m_i^2 lr_i';
+//          S_i <- F[b m_i lr_i']                       (b = dt rho0)
+//   (x/y passes: S_i <- op_grad_i S_i)
+//   ADJ_B: lu_i' = lu_i + F^-1 S_i; lu_i <- sg_i^2 lu_i'; S_i <- F[a_i sg_i lu_i']
+//   (passes: S_i <- op_div_i S_i)
+//   ADJ_C: lp = sum_i F^-1 S_i
+// and the transpose of the t = 0 override p = p0, rho_i = p0 / (c^2 D),
+// u_i = (a_i / 2) G_i p0 gives the gradient with respect to p0:
+//   ADJ_D: lp += S^T r_0; S_i <- F[(a_i / 2) lu_i]   (passes: op_div)
+//   ADJ_E: g = lp + sum_i lr_i / (c^2 D) - sum_i F^-1 S_i   (into p)
+template <class RF>
+__device__ __forceinline__ void adjoint_body(const RowsParams& P, const RF& rf, float* const* rb, int r0, int nr) {
+  const int L = P.L, R = P.R;
+  const int tot = R * L;
+  const int D = P.ndim;
+  if (P.stage == ST_ADJ_A || P.stage == ST_ADJ_D) {
+    float* lpb = rb[D];
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = kw_divu(i, P.dL), z = i - row * L;
+      if (row < nr) lpb[i] = P.p[(long long)(r0 + row) * L + z];
+    }
+    __syncthreads();
+    add_residual(P, lpb, r0, nr);
+    __syncthreads();
+    for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+      const int row = kw_divu(i, P.dL), z = i - row * L;
+      if (row >= nr) continue;
+      const long long g = (long long)(r0 + row) * L + z;
+      const float lp = lpb[i];
+      if (P.stage == ST_ADJ_A) {
+        const float c = fld(P.c0, P.c0_s, g);
+        const float c2 = __fmul_rn(c, c);
+        const float b = __fmul_rn(P.dt, fld(P.rho0, P.rho0_s, g));
+        for (int a = 0; a < D; ++a) {
+          const float pm = P.pml[a][axis_index(P, a, r0 + row, z)];
+          const float lr = __fadd_rn(P.rho[a][g], __fmul_rn(c2, lp));
+          P.rho[a][g] = __fmul_rn(__fmul_rn(pm, pm), lr);
+          rb[a][i] = __fmul_rn(__fmul_rn(b, pm), lr);
+        }
+      } else {
+        P.p[g] = lp;
+        for (int a = 0; a < D; ++a)
+          rb[a][i] = __fmul_rn(__fmul_rn(fld(P.dtrsg[a], P.dtrsg_s[a], g), 0.5f), P.u[a][g]);
+      }
+    }
+    __syncthreads();
+    for (int a = 0; a < D; ++a) rf.r2c(P, rb[a], P.S[a], r0, nr);
+    return;
+  }
+  if (P.stage == ST_ADJ_B) {
+    for (int a = 0; a < D; ++a) {
+      rf.c2r(P, P.S[a], rb[0], r0, nr);
+      for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+        const int row = kw_divu(i, P.dL), z = i - row * L;
+        if (row >= nr) continue;
+        const long long g = (long long)(r0 + row) * L + z;
+        const float sg = P.pmlsg[a][axis_index(P, a, r0 + row, z)];
+        const float lu = __fadd_rn(P.u[a][g], rb[0][i]);
+        P.u[a][g] = __fmul_rn(__fmul_rn(sg, sg), lu);
+        rb[0][i] = __fmul_rn(__fmul_rn(fld(P.dtrsg[a], P.dtrsg_s[a], g), sg), lu);
+      }
+      __syncthreads();
+      rf.r2c(P, rb[0], P.S[a], r0, nr);
+      __syncthreads();
+    }
+    return;
+  }
+  // ST_ADJ_C / ST_ADJ_E
+  for (int a = 0; a < D; ++a) rf.c2r(P, P.S[a], rb[a], r0, nr);
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+    const int row = kw_divu(i, P.dL), z = i - row * L;
+    if (row >= nr) continue;
+    const long long g = (long long)(r0 + row) * L + z;
+    float s = rb[0][i];
+    for (int a = 1; a < D; ++a) s = __fadd_rn(s, rb[a][i]);
+    if (P.stage == ST_ADJ_C) {
+      P.p[g] = s;
+    } else {
+      const float c = fld(P.c0, P.c0_s, g);
+      const float den = __fmul_rn(__fmul_rn(c, c), (float)D);
+      float acc = P.p[g];
+      for (int a = 0; a < D; ++a) acc = __fadd_rn(acc, __fdiv_rn(P.rho[a][g], den));
+      P.p[g] = __fsub_rn(acc, s);
+    }
+  }
+}
 
 // The stage physics of one block of R rows; rb[q] are R*L real buffers in
 // shared memory.  Every rf call starts and ends with a block-wide barrier.
@@ -519,6 +625,11 @@ __device__ __forceinline__ void rows_body(const RowsParams& P, const RF& rf, flo
       const int row = kw_divu(i, P.dL), z = i - row * L;
       if (row < nr) P.p0w[(long long)(r0 + row) * L + z] = rb[0][i];
     }
+    return;
+  }
+
+  if (P.stage >= ST_ADJ_A) {
+    adjoint_body(P, rf, rb, r0, nr);
     return;
   }
 

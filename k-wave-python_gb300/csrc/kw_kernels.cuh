@@ -30,8 +30,11 @@ enum KwBuf { B_S0 = 0, B_P = 3, B_SRCP = 4, B_SRCU0 = 5, B_US0 = 8 };
 // ST_RHO_PL: ST_RHO with power-law absorption on the register row kernels,
 // where rho_sum holds the density sum of the previous step (written by ST_INIT
 // and by every ST_RHO_PL) and supplies the nonlinear factor.
+// ST_ADJ_*: the transposed step of the lossless time loop (run-time-length
+// row kernels only); p, u_i, rho_i then hold the adjoint state and rec[0] the
+// sensor residual.
 enum KwStage { ST_INIT = 0, ST_U = 1, ST_RHO = 2, ST_EOS = 3, ST_SRC = 4, ST_UREC = 5, ST_P0FFT = 6, ST_P0BACK = 7,
-               ST_RHO_PL = 8 };
+               ST_RHO_PL = 8, ST_ADJ_A = 9, ST_ADJ_B = 10, ST_ADJ_C = 11, ST_ADJ_D = 12, ST_ADJ_E = 13 };
 enum KwOp { OP_GRAD = 0, OP_DIV = 1, OP_NAB1 = 2, OP_NAB2 = 3, OP_SKAPPA = 4, OP_UNSTAG = 5, OP_WIN = 6 };
 enum KwSrcMode { SRC_DIRICHLET = 0, SRC_ADDITIVE = 1, SRC_ADDITIVE_NC = 2 };
 

@@ -773,7 +773,25 @@ static int check_rows(const kw_plan* p, int stage, int init) {
     if (p->g.absorb_mode == 1 && !p->d_rhosum) return fail(KW_ERR_STATE, "internal: density sum not allocated");
   }
   if ((p->rec_us || stage == ST_UREC) && p->nslots == 0) return fail(KW_ERR_STATE, "internal: no sensor slots");
+  if (stage >= ST_ADJ_A) {
+    for (int a = 0; a < D; ++a)
+      if ((rc = need_buf(p, a, "adjoint work"))) return rc;
+    if ((stage == ST_ADJ_A || stage == ST_ADJ_D) && (!p->d_rec[KW_R_P] || p->nslots == 0 || !p->d_sens_rowptr))
+      return fail(KW_ERR_STATE, "internal: adjoint stage without a residual buffer");
+  }
   return KW_OK;
+}
+
+// Timing class of a row-stage launch (KW_K_NCLASS classes; the stages other
+// than U, RHO and EOS count with INIT).
+static int rows_class(int stage) {
+  switch (stage) {
+    case ST_U: return KW_K_ROWS_U;
+    case ST_RHO:
+    case ST_RHO_PL: return KW_K_ROWS_RHO;
+    case ST_EOS: return KW_K_ROWS_EOS;
+    default: return KW_K_ROWS_INIT;
+  }
 }
 
 static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cudaStream_t st) {
@@ -798,7 +816,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   P.init_r2c = p->init_r2c;
   if (p->rec_list) {
     kw_plan::LaunchRec r{};
-    r.kind = p->rows_reg ? 2 : 0;
+    r.kind = (p->rows_reg && stage < ST_ADJ_A) ? 2 : 0;
     r.rp = P;
     r.gx = (p->nrows + p->R - 1) / p->R;
     r.gy = r.gz = 1;
@@ -809,7 +827,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
-  if (p->rows_reg) {
+  if (p->rows_reg && stage < ST_ADJ_A) {
     P.R = p->rows_R;
     P.ex_stride = p->rows_RS;
     // the power-law density stage keeps the divergence in shared memory (one
@@ -832,7 +850,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
     k_rows<<<grid, kThreads, p->smem_rows, st>>>(P);
   }
   CK(cudaGetLastError());
-  return ev_end(p, st, KW_K_ROWS_INIT + stage, slot);
+  return ev_end(p, st, rows_class(stage), slot);
 }
 
 static void fill_axis_geom(const kw_plan* p, int axis, AxisParams& A) {
@@ -1252,6 +1270,67 @@ int32_t kw_plan_autotune(kw_plan* p, int32_t nsteps, void* stream, int32_t* T_ou
   if (T_out) *T_out = p->D > 1 ? p->T_axis[0] : 0;
   if (R_out) *R_out = p->R;
   return KW_OK;
+}
+
+static int check_device_error();
+
+// Gradient with respect to p0 of <residual, recorded p> for the lossless,
+// source-free loop with a binary sensor: the transposed steps t = Nt-1 .. 1
+// and the transposed t = 0 override (adjoint_body in kw_kernels.cu), on the
+// run-time-length row kernels.  The plan is reset before and after.
+int32_t kw_plan_adjoint_p0(kw_plan* p, const float* residual, int64_t n, float* grad, void* stream) {
+  if (!p || !residual || !grad) return fail(KW_ERR_INVALID, "kw_plan_adjoint_p0: null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_adjoint_p0 before kw_plan_finalize");
+  if (p->g.absorb_mode != 0 || p->g.nonlinear)
+    return fail(KW_ERR_UNSUPPORTED, "the adjoint covers the lossless loop (no absorption, no B/A)");
+  for (int s = 0; s < 6; ++s)
+    if (p->hsrc[s].set) return fail(KW_ERR_UNSUPPORTED, "the adjoint covers the source-free loop");
+  if (!(p->record_mask & (1 << KW_R_P)) || p->nslots == 0 || p->interp_npts > 0)
+    return fail(KW_ERR_UNSUPPORTED, "the adjoint needs a binary sensor recording p");
+  if (n != (int64_t)p->nrec * p->nslots)
+    return fail(KW_ERR_INVALID, "residual has %lld values, expected %lld", (long long)n, (long long)p->nrec * p->nslots);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc = kw_plan_reset(p);
+  if (rc) return rc;
+  {
+    // sensor-major (n_points, n_rec) -> the time-major series layout
+    std::vector<float> tm((size_t)n);
+    for (int s = 0; s < p->nslots; ++s)
+      for (int t = 0; t < p->nrec; ++t) tm[(size_t)t * p->nslots + s] = residual[(size_t)s * p->nrec + t];
+    CK(cudaMemcpy(p->d_rec[KW_R_P], tm.data(), tm.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  const bool timing = p->timing;
+  p->timing = false;
+  const int D = p->D;
+  const bool three = D == 3;
+  const int SB[3] = {0, 1, 2};
+  AxisJob gj[3], dj[3];
+  for (int a = 0; a < D; ++a) {
+    gj[a] = AxisJob{a, a, OP_GRAD, a};
+    dj[a] = AxisJob{a, a, OP_DIV, a};
+  }
+  for (int t = p->g.Nt - 1; t >= 1 && !rc; --t) {
+    if ((rc = launch_rows(p, ST_ADJ_A, 0, t, 0, st))) break;
+    if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) break;
+    if ((rc = launch_axis_ops(p, gj, D, st))) break;
+    if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) break;
+    if ((rc = launch_rows(p, ST_ADJ_B, 0, t, 0, st))) break;
+    if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) break;
+    if ((rc = launch_axis_ops(p, dj, D, st))) break;
+    if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) break;
+    rc = launch_rows(p, ST_ADJ_C, 0, t, 0, st);
+  }
+  if (!rc) rc = launch_rows(p, ST_ADJ_D, 0, 0, 0, st);
+  if (!rc && three) rc = launch_axis_plain(p, 1, 0, SB, D, st);
+  if (!rc) rc = launch_axis_ops(p, dj, D, st);
+  if (!rc && three) rc = launch_axis_plain(p, 1, 1, SB, D, st);
+  if (!rc) rc = launch_rows(p, ST_ADJ_E, 0, 0, 0, st);
+  p->timing = timing;
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(st));
+  if ((rc = check_device_error())) return rc;
+  CK(cudaMemcpy(grad, p->d_p, (size_t)p->ntot * sizeof(float), cudaMemcpyDeviceToHost));
+  return kw_plan_reset(p);
 }
 
 int32_t kw_plan_set_graphs(kw_plan* p, int32_t enable) {
@@ -1814,6 +1893,7 @@ int32_t kw_plan_read_timing(kw_plan* p, double* ms, int64_t* count) {
   for (auto& u : p->ev_used) {
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, p->ev_pool[u.second], p->ev_pool[u.second + 1]));
+    if (u.first < 0 || u.first >= KW_K_NCLASS) continue;
     ms[u.first] += t;
     count[u.first] += 1;
   }

@@ -78,6 +78,7 @@ _PROTOS = {
     "kw_plan_finalize": (C.c_int32, [_P]),
     "kw_plan_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_plan_set_graphs": (C.c_int32, [_P, C.c_int32]),
+    "kw_plan_adjoint_p0": (C.c_int32, [_P, _P, C.c_int64, _P, _P]),
     "kw_plan_autotune": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "kw_batch_create": (C.c_int32, [_P, C.c_int32, C.POINTER(_P)]),
     "kw_batch_run": (C.c_int32, [_P, C.c_int32, _P]),

@@ -1,0 +1,81 @@
+"""Gradients of sensor-data misfits with respect to the initial pressure.
+
+The reference has no adjoint.  These functions run the transposed time loop
+of the lossless, source-free step (kwave/solvers/kspace_solver.py:691-747
+with alpha = 0, B/A = 0) on the GPU (``kw_plan_adjoint_p0``).  It is exact
+to float32 rounding, because the transpose of every spectral operator of the
+step is another operator of the step (G_i^T = -D_i).
+
+* ``p0_gradient(prob, p0, d_obs)`` returns the misfit 1/2 ||d(p0) - d_obs||^2
+  and its gradient with respect to p0, for a problem dict with a binary sensor
+  recording p and ``smooth_p0`` False.
+* ``SensorData`` is a ``torch.autograd.Function`` with p0 mapped to the
+  recorded pressure; its backward is the adjoint.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .solver import Simulation
+
+
+def _plan_for(prob):
+    q = dict(prob)
+    q["p0"] = None
+    q["record"] = ("p",)
+    sim = Simulation.from_problem(q)
+    sim.setup()
+    return sim
+
+
+def forward_p0(prob, p0):
+    """Recorded pressure (n_points, Nt - record_start) for initial pressure p0."""
+    q = dict(prob)
+    q["p0"] = np.asarray(p0, np.float64)
+    q["record"] = ("p",)
+    sim = Simulation.from_problem(q)
+    try:
+        return sim.run()["p"]
+    finally:
+        sim.close()
+
+
+def adjoint_p0(prob, residual):
+    """Gradient with respect to p0 of sum(residual * recorded p)."""
+    sim = _plan_for(prob)
+    try:
+        return sim._plan.adjoint_p0(residual)
+    finally:
+        sim.close()
+
+
+def p0_gradient(prob, p0, d_obs):
+    """(misfit, gradient) of 1/2 ||d(p0) - d_obs||^2 with respect to p0."""
+    if prob.get("smooth_p0", True):
+        raise ValueError("p0_gradient needs smooth_p0=False (restore-max smoothing is not linear)")
+    d = forward_p0(prob, p0)
+    r = d.astype(np.float64) - np.asarray(d_obs, np.float64)
+    return 0.5 * float(np.sum(r * r)), adjoint_p0(prob, r)
+
+
+try:
+    import torch
+
+    class SensorData(torch.autograd.Function):
+        """p0 (grid tensor) -> recorded pressure (n_points, n_rec); backward
+        through the GPU adjoint.  ``prob`` is a problem dict with a binary
+        sensor recording p and smooth_p0 False."""
+
+        @staticmethod
+        def forward(ctx, p0, prob):
+            ctx.prob = prob
+            ctx.device = p0.device
+            d = forward_p0(prob, p0.detach().cpu().double().numpy())
+            return torch.as_tensor(d, dtype=p0.dtype, device=p0.device)
+
+        @staticmethod
+        def backward(ctx, grad_d):
+            g = adjoint_p0(ctx.prob, grad_d.detach().cpu().double().numpy())
+            return torch.as_tensor(g, dtype=grad_d.dtype, device=ctx.device), None
+except ImportError:  # pragma: no cover - torch is part of the host stack
+    SensorData = None

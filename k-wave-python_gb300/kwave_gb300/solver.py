@@ -150,6 +150,16 @@ class DevicePlan:
         K.check(self.lib.kw_plan_autotune(self._h, int(nsteps), st, C.byref(T), C.byref(R)))
         return T.value, R.value
 
+    def adjoint_p0(self, residual):
+        """Transposed time loop applied to a sensor-major residual (n_points,
+        Nt - record_start): the gradient with respect to p0 of
+        sum(residual * recorded p) (kw_plan_adjoint_p0).  The plan is reset."""
+        r = np.ascontiguousarray(residual, dtype=np.float32)
+        g = np.empty(self.S.shape, np.float32)
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        K.check(self.lib.kw_plan_adjoint_p0(self._h, K.ptr(r), r.size, K.ptr(g), st))
+        return g
+
     def set_graphs(self, enable):
         """Run repeated steps as replayed CUDA graphs (default) or as plain launches."""
         K.check(self.lib.kw_plan_set_graphs(self._h, int(bool(enable))))

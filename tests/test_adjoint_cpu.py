@@ -23,7 +23,7 @@ def circle(n, radius):
     return np.stack([radius * np.cos(th), radius * np.sin(th)])
 
 
-def problem(shape=(40, 44), nt=48, cartesian=True, record_start=1, seed=5):
+def problem(shape=(40, 48), nt=48, cartesian=True, record_start=1, seed=5):
     rng = np.random.default_rng(seed)
     gx, gy = np.meshgrid(np.arange(shape[0]), np.arange(shape[1]), indexing="ij")
     p0 = np.zeros(shape)

@@ -1,0 +1,79 @@
+"""GPU adjoint of the lossless time loop (kw_plan_adjoint_p0) against the FP64
+adjoint oracle (itself checked by dot-product test, finite differences and
+torch autograd in test_adjoint_cpu.py).  FP32 against FP64 over tens of
+steps: 1e-4 relative L2."""
+import numpy as np
+import pytest
+
+from test_adjoint_cpu import problem, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300 import _lib
+
+    _lib.require_device()
+
+
+def box3d():
+    rng = np.random.default_rng(9)
+    shape = (16, 20, 24)
+    g = np.meshgrid(*[np.arange(n) for n in shape], indexing="ij")
+    p0 = np.exp(-sum((gi - n / 2) ** 2 for gi, n in zip(g, shape)) / 8.0)
+    c = 1500.0 * (1 + 0.02 * np.tanh(rng.standard_normal(shape)))
+    mask = np.zeros(shape, bool)
+    mask[:, :, 5] = True
+    return dict(shape=shape, spacing=(1e-4,) * 3, dt=0.3 * 1e-4 / c.max(), Nt=24, sound_speed=c, density=1000.0,
+                p0=p0, smooth_p0=False, sensor_mask=mask, record=("p",), pml_size=(4, 4, 4), pml_alpha=(2.0,) * 3)
+
+
+CASES = {
+    "2d-40x48": lambda: problem(cartesian=False),
+    "2d-64x64-record-start": lambda: problem(shape=(64, 64), cartesian=False, record_start=4),
+    "3d-16x20x24": box3d,
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_adjoint_matches_oracle(name):
+    from kwave_gb300.adjoint import adjoint_p0
+    from oracle.adjoint_oracle import AdjointOracle
+
+    prob = CASES[name]()
+    A = AdjointOracle(prob)
+    r = np.random.default_rng(4).standard_normal((A.S.shape[0], A.Nt - A.rs))
+    g = adjoint_p0(prob, r)
+    e = rel(g, A.adjoint(r))
+    print(f"{name}: adjoint vs FP64 oracle {e:.2e}")
+    assert e <= TOL, e
+
+
+def test_dot_product_and_autograd():
+    import torch
+    from kwave_gb300.adjoint import SensorData, adjoint_p0, forward_p0, p0_gradient
+    from oracle.adjoint_oracle import AdjointOracle
+
+    prob = problem(cartesian=False)
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal(prob["shape"])
+    d = forward_p0(prob, x)
+    y = rng.standard_normal(d.shape)
+    lhs = float(np.sum(d.astype(np.float64) * y))
+    rhs = float(np.sum(x * adjoint_p0(prob, y).astype(np.float64)))
+    assert abs(lhs - rhs) <= 1e-4 * abs(lhs), (lhs, rhs)
+    d_obs = forward_p0(prob, prob["p0"])
+    p0 = 0.6 * prob["p0"]
+    L, g = p0_gradient(prob, p0, d_obs)
+    L_ref, g_ref, _ = AdjointOracle(prob).misfit_gradient(p0, d_obs.astype(np.float64))
+    assert abs(L - L_ref) <= 1e-4 * L_ref and rel(g, g_ref) <= TOL
+    t = torch.tensor(p0, dtype=torch.float64, requires_grad=True)
+    loss = 0.5 * ((SensorData.apply(t, prob) - torch.as_tensor(d_obs, dtype=torch.float64)) ** 2).sum()
+    loss.backward()
+    assert rel(t.grad.numpy(), g) <= 1e-6
