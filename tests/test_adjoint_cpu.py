@@ -134,3 +134,13 @@ def test_rejects_what_it_does_not_cover():
         AdjointOracle(dict(prob, alpha_coeff=0.5, alpha_power=1.5))
     with pytest.raises(ValueError):
         AdjointOracle(dict(prob, smooth_p0=True))
+
+
+def test_gpu_wrapper_host_checks():
+    """The GPU wrapper refuses, before any device call, what the transposed
+    loop does not cover."""
+    from kwave_gb300.adjoint import p0_gradient
+
+    prob = problem(cartesian=False)
+    with pytest.raises(ValueError):
+        p0_gradient(dict(prob, smooth_p0=True), prob["p0"], np.zeros((1, 1)))
