@@ -61,7 +61,7 @@ def _random_rotation(rng):
     return q
 
 
-def config2_problem(n=256, nt=1000, seed=0, plane_z=20, pml=10):
+def ivp3d_problem(n=256, nt=1000, seed=0, plane_z=20, pml=10):
     """3-D heterogeneous absorbing IVP: n^3 grid including a ``pml``-point PML,
     dx = 0.1 mm, 8 random ellipsoids (c ~ U(1400,1800) m/s, rho ~ U(900,1200)
     kg/m^3, semi-axes 8-30 px at n=256, scaled with n), power-law absorption
@@ -164,7 +164,7 @@ def transmit_problem(shape, seed, nt=2000, dx=5e-5, pml=20, n_elem=32, pitch=4, 
                 record=("p",), pml_size=(pml, pml), pml_alpha=(2.0, 2.0), use_sg=True, use_kspace=True, smooth_p0=False)
 
 
-def config3_problems(n_inst=128, nt=2000, seed=0, sizes=None):
+def transmit_problems(n_inst=128, nt=2000, seed=0, sizes=None):
     """``n_inst`` transmit events with grid sizes drawn from the 5-smooth sizes in
     [192, 512] per axis (20-point PML inside), dx = 0.05 mm."""
     rng = np.random.default_rng(seed)
@@ -307,7 +307,7 @@ def cpu_baseline_sample(n=256, steps=1):
     workload: set-up and the t=0 step untimed, then ``steps`` timed steps."""
     from oracle.kspace_oracle import OracleSimulation
 
-    prob = config2_problem(n=n, nt=1 + steps)
+    prob = ivp3d_problem(n=n, nt=1 + steps)
     sim = OracleSimulation(prob, dtype=np.float32).setup()
     sim.step()
     t0 = time.perf_counter()
@@ -356,7 +356,7 @@ def run_gb300(args):
     n = args.n
     K_steps, W = args.steps, args.warmup
     nt = max(1000, K_steps + W)
-    prob = config2_problem(n=n, nt=nt, seed=rank)
+    prob = ivp3d_problem(n=n, nt=nt, seed=rank)
     S = build_setup(prob)
     stream = torch.cuda.current_stream()
     plan = DevicePlan(S, stream=stream.cuda_stream)
@@ -425,7 +425,7 @@ def run_gb300(args):
     # end to end through the public bridge (host inputs -> host results), one full simulation
     e2e = None
     if not args.no_e2e:
-        prob_e2e = config2_problem(n=n, nt=1000, seed=rank)
+        prob_e2e = ivp3d_problem(n=n, nt=1000, seed=rank)
         kg, med, src, sen, opts = kwave_objects(prob_e2e)
         from kwave_gb300.solver import STATS
 
@@ -500,7 +500,7 @@ def run_transmit(args):
 
     ninst, K_steps, W = args.instances, args.steps, args.warmup
     nt = max(2000, W + K_steps + 1)
-    probs = config3_problems(ninst, nt=nt, seed=1)
+    probs = transmit_problems(ninst, nt=nt, seed=1)
     cells = sum(int(np.prod(p["shape"])) for p in probs)
     stream = torch.cuda.current_stream()
     t_setup = time.perf_counter()
@@ -546,7 +546,7 @@ def run_transmit(args):
     del sims
     e2e = None
     if not args.no_e2e:
-        probs_e2e = config3_problems(ninst, nt=2000, seed=2)
+        probs_e2e = transmit_problems(ninst, nt=2000, seed=2)
         cells_e2e = sum(int(np.prod(p["shape"])) for p in probs_e2e)
         torch.cuda.synchronize()
         t0 = time.perf_counter()

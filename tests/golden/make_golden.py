@@ -109,8 +109,8 @@ def base(shape, spacing, dt, Nt, **kw):
 # cases
 # ---------------------------------------------------------------------------
 
-def case_cfg1():
-    """Config 1: 2-D homogeneous IVP, 128^2, two discs, 50-point Cartesian circle."""
+def case_ivp2d_128_circle():
+    """2-D homogeneous IVP, 128^2, two discs, 50-point Cartesian circle."""
     kwave_shim.install()
     from kwave.data import Vector
     from kwave.kgrid import kWaveGrid
@@ -297,15 +297,15 @@ def case_pow2_3d():
                 record=("p", "u", "p_rms", "p_final"), pml_size=(10, 10, 10))
 
 
-def case_cfg2_mini():
-    """Config-2 physics (heterogeneous, power law y=1.5, BonA 6, 10-pt PML, z-plane sensor) at 48^3."""
-    from bench import config2_problem
+def case_ivp3d_48_absorbing():
+    """The 256^3 absorbing IVP physics (heterogeneous, power law y=1.5, BonA 6, 10-pt PML, z-plane sensor) at 48^3."""
+    from bench import ivp3d_problem
 
-    return config2_problem(n=48, nt=40, seed=7, plane_z=12)
+    return ivp3d_problem(n=48, nt=40, seed=7, plane_z=12)
 
 
 CASES = {
-    "cfg1_2d_ivp": case_cfg1,
+    "ivp2d_128_circle": case_ivp2d_128_circle,
     "het2d_abs_nl": case_het2d,
     "src2d_additive": case_src_additive,
     "src2d_dirichlet": case_src_dirichlet,
@@ -316,7 +316,7 @@ CASES = {
     "opts2d_nosg": case_opts2d,
     "nodisp2d": case_nodisp2d,
     "nosensor2d": case_nosensor2d,
-    "cfg2_mini": case_cfg2_mini,
+    "ivp3d_48_absorbing": case_ivp3d_48_absorbing,
     "intensity2d": case_intensity2d,
     "src3d_additive": case_src3d,
     "pow2_2d_src": case_pow2_2d_src,

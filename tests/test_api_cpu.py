@@ -297,7 +297,7 @@ def test_batch_host_checks():
         SimulationBatch([])
     sizes = bench._five_smooth(192, 512)
     assert sizes[0] == 192 and sizes[-1] == 512 and 243 in sizes and 250 in sizes and 7 * 32 not in sizes
-    probs = bench.config3_problems(3, nt=50, seed=4)
+    probs = bench.transmit_problems(3, nt=50, seed=4)
     for p in probs:
         assert all(n in sizes for n in p["shape"])
         n_src = int(p["p_mask"].sum())

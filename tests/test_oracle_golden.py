@@ -32,5 +32,5 @@ def test_oracle_matches_reference(name, prec):
 
 
 def test_golden_cases_present():
-    for required in ("cfg1_2d_ivp", "het3d_abs_nl", "cfg2_mini", "src2d_additive", "src2d_dirichlet"):
+    for required in ("ivp2d_128_circle", "het3d_abs_nl", "ivp3d_48_absorbing", "src2d_additive", "src2d_dirichlet"):
         assert required in CASES
