@@ -49,7 +49,7 @@ def _enabled(x) -> bool:
     if x is None:
         return False
     if hasattr(x, "__len__"):
-        return not np.all(np.asarray(x) == 0)
+        return bool(np.any(np.asarray(x)))  # any non-zero (NaN included), without a temporary mask
     return x != 0
 
 
@@ -392,13 +392,14 @@ def build_setup(prob, derive_on_device=False) -> Setup:
         S.slots = np.arange(numel, dtype=np.int64)
         S.n_points = numel
     else:
-        m = np.asarray(mask_raw, dtype=float)
+        m = np.asarray(mask_raw)
         if m.ndim == 2 and m.shape[0] == ndim:
             S.sensor_kind = "cartesian"
+            m = np.asarray(m, dtype=float)
             S.slots, S.interp_slot, S.interp_w = _cartesian_stencil(m, shape, spacing)
             S.n_points = m.shape[1]
         elif m.size == 1 or m.size == numel:
-            b = np.asarray(m, dtype=bool).ravel()
+            b = (m.ravel() if m.dtype == bool else (m != 0).ravel())
             if b.size == 1:
                 b = np.full(numel, bool(b[0]))
             S.sensor_kind = "binary"
