@@ -161,10 +161,12 @@ int32_t kw_plan_autotune(kw_plan* plan, int32_t nsteps, void* stream, int32_t* T
 /* Adjoint of the time loop (no counterpart in the reference): the gradient
  * with respect to p0 of sum over sensor points and recorded steps of
  * residual * recorded p, i.e. the transposed time loop applied to `residual`
- * (sensor-major (n_points, Nt - record_start), the layout of
- * kw_plan_read_series).  For the lossless, source-free loop with a binary
- * sensor recording p and smoothing off; `grad` receives N_total float32 (C
- * order).  With residual = recorded p - observed data it is the gradient of
+ * (sensor-major (n_slots, Nt - record_start): one row per recorded grid
+ * point -- the sensor points of a binary sensor, the interpolation corners of
+ * a Cartesian one, whose residual the caller takes back through the
+ * transposed interpolation weights).  For the lossless, source-free loop
+ * with a sensor recording p and smoothing off; `grad` receives N_total
+ * float32 (C order).  With residual = recorded p - observed data it is the gradient of
  * 1/2 ||recorded p - observed||^2.  The plan is reset (t = 0, zero state)
  * before and after; its uploaded medium, PML and sensor are used. */
 int32_t kw_plan_adjoint_p0(kw_plan* plan, const float* residual, int64_t n, float* grad, void* stream);

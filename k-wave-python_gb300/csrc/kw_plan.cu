@@ -1285,8 +1285,8 @@ int32_t kw_plan_adjoint_p0(kw_plan* p, const float* residual, int64_t n, float* 
     return fail(KW_ERR_UNSUPPORTED, "the adjoint covers the lossless loop (no absorption, no B/A)");
   for (int s = 0; s < 6; ++s)
     if (p->hsrc[s].set) return fail(KW_ERR_UNSUPPORTED, "the adjoint covers the source-free loop");
-  if (!(p->record_mask & (1 << KW_R_P)) || p->nslots == 0 || p->interp_npts > 0)
-    return fail(KW_ERR_UNSUPPORTED, "the adjoint needs a binary sensor recording p");
+  if (!(p->record_mask & (1 << KW_R_P)) || p->nslots == 0)
+    return fail(KW_ERR_UNSUPPORTED, "the adjoint needs a sensor recording p");
   if (n != (int64_t)p->nrec * p->nslots)
     return fail(KW_ERR_INVALID, "residual has %lld values, expected %lld", (long long)n, (long long)p->nrec * p->nslots);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);

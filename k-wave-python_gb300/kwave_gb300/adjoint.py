@@ -7,8 +7,11 @@ to float32 rounding, because the transpose of every spectral operator of the
 step is another operator of the step (G_i^T = -D_i).
 
 * ``p0_gradient(prob, p0, d_obs)`` returns the misfit 1/2 ||d(p0) - d_obs||^2
-  and its gradient with respect to p0, for a problem dict with a binary sensor
-  recording p and ``smooth_p0`` False.
+  and its gradient with respect to p0, for a problem dict with a sensor
+  recording p and ``smooth_p0`` False.  A Cartesian sensor records grid
+  points ("slots") on the device and interpolates them multilinearly at the
+  end; its residual goes back to the slots through the transpose of that
+  interpolation (``slot_residual``) before the device adjoint.
 * ``SensorData`` is a ``torch.autograd.Function`` with p0 mapped to the
   recorded pressure; its backward is the adjoint.
 """
@@ -40,11 +43,27 @@ def forward_p0(prob, p0):
         sim.close()
 
 
+def slot_residual(S, residual):
+    """Residual at the sensor's recorded grid points: the identity for binary
+    sensors; for Cartesian ones the transpose of the multilinear
+    interpolation (``Setup.interp_slot`` / ``interp_w``, the weights of
+    kspace_solver.py:341-359)."""
+    r = np.asarray(residual, np.float64)
+    if S.sensor_kind != "cartesian":
+        return r
+    npts, nc = S.interp_slot.shape
+    if r.shape[0] != npts:
+        raise ValueError(f"residual has {r.shape[0]} rows, the sensor {npts} points")
+    out = np.zeros((S.slots.size, r.shape[1]))
+    np.add.at(out, S.interp_slot.ravel(), (S.interp_w[:, :, None] * r[:, None, :]).reshape(npts * nc, -1))
+    return out
+
+
 def adjoint_p0(prob, residual):
     """Gradient with respect to p0 of sum(residual * recorded p)."""
     sim = _plan_for(prob)
     try:
-        return sim._plan.adjoint_p0(residual)
+        return sim._plan.adjoint_p0(slot_residual(sim.S, residual))
     finally:
         sim.close()
 

@@ -151,9 +151,11 @@ class DevicePlan:
         return T.value, R.value
 
     def adjoint_p0(self, residual):
-        """Transposed time loop applied to a sensor-major residual (n_points,
-        Nt - record_start): the gradient with respect to p0 of
-        sum(residual * recorded p) (kw_plan_adjoint_p0).  The plan is reset."""
+        """Transposed time loop applied to a residual at the recorded grid
+        points (n_slots, Nt - record_start): the gradient with respect to p0
+        of sum(residual * recorded slot values) (kw_plan_adjoint_p0).  For a
+        Cartesian sensor, ``adjoint.slot_residual`` maps point residuals to
+        slots.  The plan is reset."""
         r = np.ascontiguousarray(residual, dtype=np.float32)
         g = np.empty(self.S.shape, np.float32)
         st = C.c_void_p(self.stream) if self.stream is not None else None
