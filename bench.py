@@ -173,6 +173,33 @@ def transmit_problems(n_inst=128, nt=2000, seed=0, sizes=None):
             for i in range(n_inst)]
 
 
+def vessel_problem(n=512, nt=1500, seed=0, pml=20, n_sensor=256, radius=11e-3, dx=5e-5):
+    """Initial-pressure reconstruction case: n^2 grid including a ``pml``-point
+    PML, dx = 0.05 mm, homogeneous c = 1500 m/s, rho = 1000 kg/m^3, lossless;
+    p0 of 15 smoothed line segments (width 1-4 px) and 5 discs with amplitudes
+    U(0.5, 2); ``n_sensor`` Cartesian points on a circle of ``radius``; p0
+    smoothing off (the reconstruction variable is p0 itself)."""
+    rng = np.random.default_rng(seed)
+    gx, gy = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    p0 = np.zeros((n, n))
+    lo, hi = pml + 0.25 * (n - 2 * pml), n - pml - 0.25 * (n - 2 * pml)
+    for _ in range(15):
+        x0, y0, x1, y1 = rng.uniform(lo, hi, 4)
+        w = rng.uniform(1, 4) / 2
+        vx, vy = x1 - x0, y1 - y0
+        t = np.clip(((gx - x0) * vx + (gy - y0) * vy) / max(vx * vx + vy * vy, 1e-9), 0, 1)
+        dist = np.hypot(gx - (x0 + t * vx), gy - (y0 + t * vy))
+        p0 = np.maximum(p0, rng.uniform(0.5, 2) * np.clip(w + 0.5 - dist, 0, 1))
+    for _ in range(5):
+        cx, cy, r = rng.uniform(lo, hi), rng.uniform(lo, hi), rng.uniform(2, 6)
+        p0 = np.maximum(p0, rng.uniform(0.5, 2) * np.clip(r + 0.5 - np.hypot(gx - cx, gy - cy), 0, 1))
+    th = 2 * np.pi * np.arange(n_sensor) / n_sensor
+    sensor = np.stack([radius * np.cos(th), radius * np.sin(th)])
+    return dict(shape=(n, n), spacing=(dx, dx), dt=0.3 * dx / 1500.0, Nt=nt, sound_speed=1500.0, density=1000.0,
+                p0=p0, smooth_p0=False, sensor_mask=sensor, record=("p",), pml_size=(pml, pml),
+                pml_alpha=(2.0, 2.0), use_sg=True, use_kspace=True)
+
+
 def kwave_objects(prob):
     """The same problem as the objects the legacy kspaceFirstOrder3D call takes."""
     kgrid = SimpleNamespace(N=np.array(prob["shape"]), spacing=np.array(prob["spacing"]), Nt=prob["Nt"], dt=prob["dt"],
@@ -590,6 +617,49 @@ def run_transmit(args):
     return 0
 
 
+ADJOINT_WORKLOAD = ("p0 reconstruction: 512^2 incl. 20-pt PML, dx=0.05 mm, c=1500, lossless, vessel phantom "
+                    "(15 segments + 5 discs), 256-point Cartesian circle r=11 mm, 1500 steps, data + 1 % noise, "
+                    "steepest descent with exact line search from zero")
+
+
+def run_adjoint(args):
+    """p0 reconstruction by plain adjoint iterations: each iteration is one
+    GPU adjoint (transposed time loop) and one forward pass.  ``value`` =
+    cell-steps of all passes / wall time; the line also gives seconds per
+    iteration, the relative p0 error per iteration and the time to 1 %."""
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300.adjoint import adjoint_p0, forward_p0, steepest_descent_p0
+
+    prob = vessel_problem(nt=1500)
+    rng = np.random.default_rng(11)
+    d_clean = forward_p0(prob, prob["p0"])
+    d_obs = d_clean + 0.01 * np.std(d_clean) * rng.standard_normal(d_clean.shape)
+    fwd = lambda p: forward_p0(prob, p)  # noqa: E731
+    adj = lambda r: adjoint_p0(prob, r)  # noqa: E731
+    steepest_descent_p0(fwd, adj, d_obs, np.zeros(prob["shape"]), 1)  # warm-up (library, kernels)
+    torch.cuda.synchronize()
+    iters = max(1, args.steps if args.steps < 1000 else 20)
+    t0 = time.perf_counter()
+    p, hist = steepest_descent_p0(fwd, adj, d_obs, np.zeros(prob["shape"]), iters, p_true=prob["p0"])
+    secs = time.perf_counter() - t0
+    cells = int(np.prod(prob["shape"]))
+    passes = 1 + 2 * iters  # initial forward, then adjoint + forward per iteration
+    errs = [h[1] for h in hist]
+    to1 = next((i + 1 for i, e in enumerate(errs) if e <= 0.01), None)
+    line = {"metric": METRIC, "value": cells * prob["Nt"] * passes / secs / 1e6, "unit": UNIT, "n_gpus": 1,
+            "steps": iters, "warmup": 1, "ms_per_step": 1e3 * secs / iters, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic vessel phantom, 1 % noise",
+            "config": {"workload": ADJOINT_WORKLOAD, "iterations": iters},
+            "seconds_per_iteration": secs / iters, "p0_rel_error": errs,
+            "iterations_to_1pct": to1, "seconds_to_1pct": None if to1 is None else secs / iters * to1}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 import ctypes  # noqa: E402
 
 C_int64 = ctypes.c_int64
@@ -604,8 +674,9 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=256, help="grid edge (the headline workload is 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit"],
-                    help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events")
+    ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit", "adjoint"],
+                    help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events; "
+                         "adjoint: p0 reconstruction by adjoint iterations at 512^2")
     ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
     ap.add_argument("--grouped", action="store_true", help="transmit workload: grouped launches across members")
     ap.add_argument("--autotune", action="store_true", help="transmit workload: autotune each member's launch geometry")
@@ -616,6 +687,8 @@ def main(argv=None):
         return run_reference(args)
     if args.workload == "transmit":
         return run_transmit(args)
+    if args.workload == "adjoint":
+        return run_adjoint(args)
     return run_gb300(args)
 
 

@@ -77,6 +77,31 @@ def p0_gradient(prob, p0, d_obs):
     return 0.5 * float(np.sum(r * r)), adjoint_p0(prob, r)
 
 
+def steepest_descent_p0(forward, adjoint, d_obs, p_init, iterations, p_true=None):
+    """Steepest descent on the quadratic misfit 1/2 ||F p - d_obs||^2 with the
+    exact line search of a linear F: g = F^T r, alpha = |g|^2 / |F g|^2,
+    p <- p - alpha g, r <- r - alpha F g.  Two passes per iteration (one
+    adjoint, one forward).  ``forward``/``adjoint`` map p0 -> recorded data
+    and residual -> gradient (``forward_p0`` / ``adjoint_p0`` bound to a
+    problem on the GPU).  Returns p and the history of (misfit, relative p
+    error or None)."""
+    p = np.array(p_init, np.float64)
+    r = np.asarray(forward(p), np.float64) - np.asarray(d_obs, np.float64)
+    hist = []
+    for _ in range(int(iterations)):
+        g = np.asarray(adjoint(r), np.float64)
+        fg = np.asarray(forward(g), np.float64)
+        den = float(np.sum(fg * fg))
+        if den == 0.0:
+            break
+        alpha = float(np.sum(g * g)) / den
+        p -= alpha * g
+        r -= alpha * fg
+        err = None if p_true is None else float(np.linalg.norm(p - p_true) / np.linalg.norm(p_true))
+        hist.append((0.5 * float(np.sum(r * r)), err))
+    return p, hist
+
+
 try:
     import torch
 

@@ -162,3 +162,29 @@ def test_cartesian_residual_to_slots():
     B = AdjointOracle(dict(prob, sensor_mask=binary))
     r = np.random.default_rng(8).standard_normal((A.S.shape[0], A.Nt - A.rs))
     assert rel(B.adjoint(slot_residual(S, r)), A.adjoint(r)) < 1e-12
+
+
+def test_steepest_descent_driver():
+    """The reconstruction loop on the FP64 oracle's forward and adjoint: the
+    misfit falls every iteration and the p0 error shrinks."""
+    from kwave_gb300.adjoint import steepest_descent_p0
+
+    prob = problem(cartesian=True)
+    A = AdjointOracle(prob)
+    d_obs = A.forward(prob["p0"])
+    p, hist = steepest_descent_p0(A.forward, A.adjoint, d_obs, np.zeros(prob["shape"]), 8, p_true=prob["p0"])
+    misfits = [h[0] for h in hist]
+    assert all(b < a for a, b in zip(misfits, misfits[1:])), misfits
+    assert hist[-1][1] < 0.9 * hist[0][1], hist
+
+
+def test_vessel_problem_runs_on_the_oracle():
+    """The reconstruction workload's generator, at a reduced size, gives a
+    problem the adjoint oracle accepts (lossless, smoothing off, Cartesian
+    circle inside the grid)."""
+    import bench
+
+    prob = bench.vessel_problem(n=64, nt=20, pml=8, n_sensor=32, radius=1.2e-3)
+    A = AdjointOracle(prob)
+    d = A.forward(prob["p0"])
+    assert d.shape == (32, 20) and np.all(np.isfinite(d)) and np.abs(d).max() > 0
