@@ -329,14 +329,17 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_baseline_sample(n=256, steps=1):
+def cpu_baseline_sample(n=256, steps=1, warm=1):
     """Oracle (the reference's CPU implementation, restated) on the same
-    workload: set-up and the t=0 step untimed, then ``steps`` timed steps."""
+    workload: set-up and ``warm`` untimed steps (the first is the t=0 step),
+    then ``steps`` timed steps."""
     from oracle.kspace_oracle import OracleSimulation
 
-    prob = ivp3d_problem(n=n, nt=1 + steps)
+    warm = max(1, int(warm))
+    prob = ivp3d_problem(n=n, nt=warm + steps)
     sim = OracleSimulation(prob, dtype=np.float32).setup()
-    sim.step()
+    for _ in range(warm):
+        sim.step()
     t0 = time.perf_counter()
     for _ in range(steps):
         sim.step()
@@ -349,13 +352,15 @@ def run_reference(args):
     if rank != 0:
         return 0
     steps = max(1, min(args.steps, 3))
-    value, secs = cpu_baseline_sample(args.n, steps)
+    warm = min(args.warmup, 3)
+    value, secs = cpu_baseline_sample(args.n, steps, warm)
     cpu = {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-           "sample": f"{steps} time step(s) of the 256^3 workload after set-up and the t=0 step ({secs:.1f} s); "
+           "sample": f"{steps} time step(s) of the 256^3 workload after set-up and {warm} untimed steps "
+                     f"({secs:.1f} s); "
                      "NumPy pocketfft is single-threaded, so the reference path uses one core "
                      f"(host has {os.cpu_count()})"}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
-            "warmup": 1, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, shapes of the named workload)",
             "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "l2": "inputs larger than L2"},
             "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
