@@ -1740,6 +1740,7 @@ int32_t kw_batch_launch_count(const kw_batch* b, int64_t* count) {
 
 int32_t kw_batch_destroy(kw_batch* b) {
   if (!b) return KW_OK;
+  cudaDeviceSynchronize();  // replays and side-stream work may still be in flight
   for (auto& g : b->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
   if (b->cap) cudaStreamDestroy(b->cap);
@@ -1908,6 +1909,7 @@ int32_t kw_plan_launch_count(const kw_plan* p, int64_t* count) {
 
 int32_t kw_plan_destroy(kw_plan* p) {
   if (!p) return KW_OK;
+  cudaDeviceSynchronize();  // graph replays may still read the plan's buffers
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   drop_graphs(p);
   if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
