@@ -88,44 +88,21 @@ def test_gradients_against_finite_differences():
     assert abs(fd - np.sum(g_c * w)) <= 1e-6 * abs(fd), (fd, np.sum(g_c * w))
 
 
-def test_gradients_against_torch_autograd():
-    torch = pytest.importorskip("torch")
-    prob = problem(shape=(36, 40), nt=40)
+@pytest.mark.parametrize("shape,nt,record_start", [((36, 40), 40, 1), ((30, 32), 30, 5)])
+def test_gradients_against_torch_autograd(shape, nt, record_start):
+    pytest.importorskip("torch")
+    from oracle.torch_reference import misfit_and_grads
+
+    prob = problem(shape=shape, nt=nt, record_start=record_start)
     A = AdjointOracle(prob)
     rng = np.random.default_rng(3)
     d_obs = A.forward(prob["p0"]) + 0.01 * rng.standard_normal((A.S.shape[0], A.Nt - A.rs))
     p0_np = 0.5 * prob["p0"]
     L, g_p0, g_c = A.misfit_gradient(p0_np, d_obs)
-
-    T = lambda a: torch.as_tensor(np.asarray(a), dtype=torch.float64)  # noqa: E731
-    Tc = lambda a: torch.as_tensor(np.asarray(a), dtype=torch.complex128)  # noqa: E731
-    og, od = [Tc(o) for o in A.og], [Tc(o) for o in A.od]
-    m, sg, a = [T(x) for x in A.m], [T(x) for x in A.sg], [T(x) for x in A.a]
-    b, S = T(A.b), T(A.S)
-    p0 = T(p0_np).requires_grad_(True)
-    c = T(A.c).requires_grad_(True)
-    c2 = c * c
-    D = A.ndim
-    G = lambda i, f: torch.fft.ifftn(og[i] * torch.fft.fftn(f)).real  # noqa: E731
-    Dv = lambda i, f: torch.fft.ifftn(od[i] * torch.fft.fftn(f)).real  # noqa: E731
-    p = p0
-    rho = [p0 / (c2 * D) for _ in range(D)]
-    u = [(a[i] / 2) * G(i, p0) for i in range(D)]
-    rec = [S @ p.reshape(-1)]
-    for _ in range(1, A.Nt):
-        u = [sg[i] * (sg[i] * u[i] - a[i] * G(i, p)) for i in range(D)]
-        rho = [m[i] * (m[i] * rho[i] - b * Dv(i, u[i])) for i in range(D)]
-        s = rho[0]
-        for r in rho[1:]:
-            s = s + r
-        p = c2 * s
-        rec.append(S @ p.reshape(-1))
-    d = torch.stack(rec, dim=1)
-    loss = 0.5 * ((d - T(d_obs)) ** 2).sum()
-    loss.backward()
-    assert abs(loss.item() - L) <= 1e-12 * L
-    assert rel(g_p0, p0.grad.numpy()) < 1e-10
-    assert rel(g_c, c.grad.numpy()) < 1e-10
+    Lt, gt_p0, gt_c = misfit_and_grads(prob, p0_np, d_obs)
+    assert abs(Lt - L) <= 1e-12 * L
+    assert rel(g_p0, gt_p0) < 1e-10
+    assert rel(g_c, gt_c) < 1e-10
 
 
 def test_rejects_what_it_does_not_cover():
@@ -188,3 +165,19 @@ def test_vessel_problem_runs_on_the_oracle():
     A = AdjointOracle(prob)
     d = A.forward(prob["p0"])
     assert d.shape == (32, 20) and np.all(np.isfinite(d)) and np.abs(d).max() > 0
+
+
+def test_adjoint_oracle_against_autograd_at_128():
+    """The 128 x 128 check of the reconstruction workload's gradients: the
+    adjoint oracle against FP64 torch autograd (p0 and c)."""
+    pytest.importorskip("torch")
+    from oracle.torch_reference import misfit_and_grads
+
+    prob = problem(shape=(128, 128), nt=60, cartesian=False)
+    A = AdjointOracle(prob)
+    d_obs = A.forward(prob["p0"]) * 1.01
+    p0 = 0.5 * prob["p0"]
+    L, g_p0, g_c = A.misfit_gradient(p0, d_obs)
+    Lt, gt_p0, gt_c = misfit_and_grads(prob, p0, d_obs)
+    assert abs(Lt - L) <= 1e-12 * L
+    assert rel(g_p0, gt_p0) < 1e-10 and rel(g_c, gt_c) < 1e-10
