@@ -278,7 +278,7 @@ def measured_peaks():
 
 # DRAM bytes (read + write) per launch of each kernel class, measured with ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) on the 256^3 headline
-# workload; profiles/timeloop_256cubed_kernels.md has the capture and command.
+# workload.
 NCU_TRAFFIC_256 = {"rows_rho": 909.6e6, "rows_u": 956.3e6, "rows_eos": 530.1e6, "axis_ops": 269.2e6,
                    "axis_plain": 262.7e6}
 
@@ -291,8 +291,7 @@ def launch_bytes(S):
     ntot = int(np.prod(S.shape))
     L = S.shape[-1]
     H = L // 2 + 1
-    Hp = H + (H & 1)
-    spec = (ntot // L) * Hp * 8
+    spec = (ntot // L) * H * 8  # half spectrum, without the row padding to an even length
     real = ntot * 4
     grid = lambda name: isinstance(S.fields.get(name), np.ndarray)  # noqa: E731
     powerlaw = S.absorb_mode == 1
@@ -345,6 +344,32 @@ def cpu_baseline_sample(n=256, steps=1, warm=1):
         sim.step()
     dt = time.perf_counter() - t0
     return n ** 3 * steps / dt / 1e6, dt
+
+
+def headline_parity(e2e_result=None):
+    """Relative L2 errors of the headline result against the unmodified
+    reference's float32 and float64 runs of the same seeded problem
+    (tests/golden/ivp3d_256, made by tests/golden/make_golden_256.py): the
+    1000-step result of the e2e run when that golden exists, otherwise a
+    fresh run of the longest problem that has one."""
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    import ivp3d_256
+    from kwave_gb300.solver import run_problem
+
+    cps = ivp3d_256.checkpoints()
+    if not cps:
+        return None
+    t = cps[-1]
+    if e2e_result is not None and t == 1000:
+        got = e2e_result
+    else:
+        prob = ivp3d_problem(n=256, nt=t, seed=0)
+        ivp3d_256.check_inputs(prob, ivp3d_256.load(t)["ref32"])
+        prob["record"] = ("p", "p_max", "p_final")
+        got = run_problem(prob)
+    return {"steps_compared": t, "tolerance_vs_f32": 1e-5, "rel_l2": ivp3d_256.parity(got, t),
+            "what": "p_max on all 65,536 plane points, the p series of 256 plane points, every 8th cell of the "
+                    "final interior p (when recorded); against the reference solver in float32 and float64"}
 
 
 def run_reference(args):
@@ -451,6 +476,9 @@ def run_gb300(args):
                           "gbs": (by.get(names[i], 0.0) / (kms[i] / max(kcnt[i], 1) / 1e3) / 1e9) if kcnt[i] else None}
                for i in range(6) if kcnt[i]}
     step_gbs = A_MODEL_BYTES_PER_CELL_STEP * cells * K_steps / (ms / 1e3) / 1e9
+    # measured DRAM bytes of one step: ncu bytes per launch x launches per step
+    ncu_step = (sum(NCU_TRAFFIC_256[names[i]] * kcnt[i] for i in range(6) if kcnt[i] and names[i] in NCU_TRAFFIC_256)
+                / K_steps) if n == 256 else None
     plan.close()
     del plan
 
@@ -475,6 +503,7 @@ def run_gb300(args):
 
     if rank != 0:
         return 0
+    parity = None if (args.no_parity or n != 256) else headline_parity(res if e2e else None)
     cpu = None
     if not args.no_cpu_baseline:
         cv, secs = cpu_baseline_sample(256, 1)
@@ -491,14 +520,18 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_256.get(names[dom]) if n == 256 else None,
-                     "traffic_source": "ncu dram bytes per launch, profiles/timeloop_256cubed_kernels.md",
+                     "traffic_source": "ncu dram bytes per launch, 256^3 headline",
                      "peak_source": peak_kind},
         "step_roofline": {"model_bytes_per_cell_step": A_MODEL_BYTES_PER_CELL_STEP, "achieved": step_gbs,
-                          "peak": peak, "frac": step_gbs / peak, "unit": "GB/s"},
+                          "peak": peak, "frac": step_gbs / peak, "unit": "GB/s",
+                          "ncu_dram_bytes_per_step": ncu_step,
+                          "ncu_dram_over_model": None if ncu_step is None else
+                          ncu_step / (A_MODEL_BYTES_PER_CELL_STEP * cells)},
         "kernels": kernels,
         "instrumented_pass": {"ms_per_step": ms_instr / K_steps,
                               "note": "the same K steps as plain launches, each bracketed by CUDA events: source of "
                                       "the per-kernel durations in roofline and kernels"},
+        "parity": parity,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk.summary(),
@@ -679,6 +712,7 @@ def main(argv=None):
     ap.add_argument("--n", type=int, default=256, help="grid edge (the headline workload is 256)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the comparison with the 256^3 golden")
     ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit", "adjoint"],
                     help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events; "
                          "adjoint: p0 reconstruction by adjoint iterations at 512^2")

@@ -236,7 +236,9 @@ int32_t kw_plan_launch_count(const kw_plan* plan, int64_t* count);
  * operators of frameworks that own all device memory (PyTorch, JAX/XLA,
  * TensorRT plugins) and real-time pipelines that forbid allocation once
  * running.  The half-spectrum scratch is a static 16 MiB device array
- * (2,097,152 complex values; about 2040^2 in 2-D or 128^3 in 3-D), held by every
+ * (2,097,152 complex values: the grid must satisfy N0*N1*Hp (3-D) or N0*Hp
+ * (2-D) <= 2,097,152 with Hp = N_last/2 + 1 rounded up to even, e.g. square
+ * grids up to 2040^2 and cubes up to 159^3), held by every
  * GPU that loads the library until exit; larger grids return
  * KW_ERR_UNSUPPORTED.  The first call on a device resolves the array's address
  * and sets kernel attributes (make it before any stream capture).  All calls

@@ -13,7 +13,8 @@
 // Limits and sharing rules:
 //   * the scratch holds KW_NOALLOC_MAX_SPECTRUM complex values (16 MiB); a
 //     grid needs (N_total / N_last) * Hp of them, Hp = (N_last/2 + 1) rounded
-//     up to even -- about 2040^2 in 2-D or 128^3 in 3-D.  Larger grids are
+//     up to even, so N0*N1*Hp (3-D) or N0*Hp (2-D) must not exceed 2,097,152:
+//     square grids up to 2040^2 in 2-D and cubes up to 159^3 in 3-D.  Larger grids are
 //     rejected with KW_ERR_UNSUPPORTED.  Every GPU that loads the library holds
 //     these arrays until the process exits.
 //   * all calls share the arrays, and each call leaves its own values behind.

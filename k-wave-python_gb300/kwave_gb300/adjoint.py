@@ -22,6 +22,14 @@ import numpy as np
 from .solver import Simulation
 
 
+def _require_unsmoothed(prob, who):
+    """The adjoint is the transpose of the linear map p0 -> recorded p; the
+    restore-max smoothing of p0 (kwave/utils/filters.py:549-615) is not
+    linear, and an unset ``smooth_p0`` means True (kspace_solver.py:145)."""
+    if prob.get("smooth_p0", True):
+        raise ValueError(f"{who} needs smooth_p0=False (restore-max smoothing is not linear)")
+
+
 def _plan_for(prob):
     q = dict(prob)
     q["p0"] = None
@@ -61,6 +69,7 @@ def slot_residual(S, residual):
 
 def adjoint_p0(prob, residual):
     """Gradient with respect to p0 of sum(residual * recorded p)."""
+    _require_unsmoothed(prob, "adjoint_p0")
     sim = _plan_for(prob)
     try:
         return sim._plan.adjoint_p0(slot_residual(sim.S, residual))
@@ -70,8 +79,7 @@ def adjoint_p0(prob, residual):
 
 def p0_gradient(prob, p0, d_obs):
     """(misfit, gradient) of 1/2 ||d(p0) - d_obs||^2 with respect to p0."""
-    if prob.get("smooth_p0", True):
-        raise ValueError("p0_gradient needs smooth_p0=False (restore-max smoothing is not linear)")
+    _require_unsmoothed(prob, "p0_gradient")
     d = forward_p0(prob, p0)
     r = d.astype(np.float64) - np.asarray(d_obs, np.float64)
     return 0.5 * float(np.sum(r * r)), adjoint_p0(prob, r)
@@ -112,6 +120,7 @@ try:
 
         @staticmethod
         def forward(ctx, p0, prob):
+            _require_unsmoothed(prob, "SensorData")
             ctx.prob = prob
             ctx.device = p0.device
             d = forward_p0(prob, p0.detach().cpu().double().numpy())

@@ -21,7 +21,10 @@ import types
 import typing
 from pathlib import Path
 
-REFERENCE_ROOT = Path(os.environ.get("KWAVE_REFERENCE_ROOT", "/root/reference"))
+# The checkout is named by KWAVE_REFERENCE_ROOT; without it, a ``reference``
+# directory beside the repository is used (the layout of the build host).
+_BESIDE_REPO = Path(__file__).resolve().parents[3] / "reference"
+REFERENCE_ROOT = Path(os.environ.get("KWAVE_REFERENCE_ROOT", str(_BESIDE_REPO)))
 
 
 def reference_available() -> bool:

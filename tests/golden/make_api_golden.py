@@ -1,8 +1,8 @@
 """Golden cases for the entry points built on the solver: the unified
 ``kspaceFirstOrder`` (kwave/kspaceFirstOrder.py) and ``TimeReversal``
 (kwave/reconstruction/time_reversal.py), produced by the unmodified reference
-in a container that holds its checkout (default ``/root/reference``, override
-with ``KWAVE_REFERENCE_ROOT``):
+on a host that holds its checkout (``KWAVE_REFERENCE_ROOT``, or a ``reference``
+directory beside this repository):
 
     python tests/golden/make_api_golden.py
 

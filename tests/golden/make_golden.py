@@ -1,7 +1,7 @@
 """Generate the golden cases under tests/golden/ from the unmodified reference.
 
-Run in a container that holds the k-wave-python checkout (default
-``/root/reference``, override with ``KWAVE_REFERENCE_ROOT``):
+Run on a host that holds the k-wave-python checkout (``KWAVE_REFERENCE_ROOT``,
+or a ``reference`` directory beside this repository):
 
     python tests/golden/make_golden.py
 

@@ -123,6 +123,23 @@ def test_gpu_wrapper_host_checks():
         p0_gradient(dict(prob, smooth_p0=True), prob["p0"], np.zeros((1, 1)))
 
 
+def test_gpu_wrapper_rejects_smoothing_everywhere():
+    """Every entry of the GPU adjoint refuses a problem whose p0 would be
+    smoothed -- smooth_p0 True or left unset, which means True in the
+    reference -- before any device call: the forward would smooth, the
+    transposed loop would not."""
+    torch = pytest.importorskip("torch")
+    from kwave_gb300.adjoint import SensorData, adjoint_p0
+
+    prob = problem(cartesian=False)
+    unset = {k: v for k, v in prob.items() if k != "smooth_p0"}
+    for bad in (unset, dict(prob, smooth_p0=True)):
+        with pytest.raises(ValueError, match="smooth_p0"):
+            SensorData.apply(torch.zeros(prob["shape"], dtype=torch.float64), bad)
+        with pytest.raises(ValueError, match="smooth_p0"):
+            adjoint_p0(bad, np.zeros((1, 1)))
+
+
 def test_cartesian_residual_to_slots():
     """A Cartesian sensor's residual taken back to its recorded grid points
     (the device adjoint's input) gives the same p0 gradient as the adjoint

@@ -77,3 +77,27 @@ def test_dot_product_and_autograd():
     loss = 0.5 * ((SensorData.apply(t, prob) - torch.as_tensor(d_obs, dtype=torch.float64)) ** 2).sum()
     loss.backward()
     assert rel(t.grad.numpy(), g) <= 1e-6
+
+
+def test_cartesian_circle_adjoint_128():
+    """The route of the reconstruction workload: a Cartesian circle of sensor
+    points, whose residual goes back to the recorded grid corners through the
+    transposed interpolation weights (adjoint.slot_residual) and then through
+    the device adjoint, at 128^2 over 300 steps, against the FP64 adjoint
+    oracle (which takes the residual back through the interpolation itself)."""
+    from kwave_gb300.adjoint import adjoint_p0, forward_p0
+    from oracle.adjoint_oracle import AdjointOracle
+    from test_adjoint_cpu import circle
+
+    prob = problem(shape=(128, 128), nt=300, cartesian=True)
+    prob["sensor_mask"] = circle(64, 4.5e-3)
+    A = AdjointOracle(prob)
+    d = forward_p0(prob, prob["p0"])
+    d64 = A.forward(prob["p0"])
+    ef = rel(d, d64)
+    r = np.random.default_rng(8).standard_normal((64, A.Nt - A.rs))
+    g = adjoint_p0(prob, r)
+    e = rel(g, A.adjoint(r))
+    print(f"128^2 x 300 Cartesian circle: forward vs FP64 {ef:.2e}, adjoint vs FP64 {e:.2e}")
+    assert ef <= TOL, ef
+    assert e <= TOL, e

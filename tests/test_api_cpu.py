@@ -304,3 +304,78 @@ def test_batch_host_checks():
         assert n_src == 32 * 3 and p["p"].shape[0] == n_src
         assert p["dt"] <= 0.3 * 5e-5 / p["sound_speed"].max() * (1 + 1e-12)
         assert np.array_equal(p["sensor_mask"], p["p_mask"])
+
+
+def test_drop_in_switch_through_the_reference_call(monkeypatch):
+    """The reference's own legacy call, kwave.kspaceFirstOrder2D.kspaceFirstOrder2D
+    (kwave/kspaceFirstOrder2D.py:215-218), reaches the GB300 time loop after
+    ``install()`` when the execution options select ``backend="gb300"``, with
+    the options the reference bridge derives (kwave/solvers/native.py:6-30);
+    ``backend="python"`` still reaches the reference's own solver, and
+    ``uninstall()`` restores the original bridge.  The two solver classes are
+    replaced by recorders, so no GPU is needed."""
+    import kwave_shim
+
+    if not kwave_shim.reference_available():
+        pytest.skip("reference checkout not available")
+    kwave_shim.install()
+    import kwave.kspaceFirstOrder2D as K2
+    import kwave.solvers.native as native
+    from kwave.data import Vector
+    from kwave.kgrid import kWaveGrid
+    from kwave.kmedium import kWaveMedium
+    from kwave.ksensor import kSensor
+    from kwave.ksource import kSource
+    from kwave.options.simulation_execution_options import SimulationExecutionOptions
+    from kwave.options.simulation_options import SimulationOptions
+
+    from kwave_gb300 import backend
+
+    calls = []
+
+    def recorder(tag):
+        class Rec:
+            def __init__(self, kgrid, medium, source, sensor, **kw):
+                calls.append((tag, (kgrid, medium, source, sensor), kw))
+
+            def run(self):
+                return {"p": np.array([tag])}
+
+            def close(self):
+                pass
+
+        return Rec
+
+    monkeypatch.setattr(backend, "Simulation", recorder("gb300"))
+    monkeypatch.setattr(native, "Simulation", recorder("python"))
+    original = native.run_python_backend
+    kg = kWaveGrid(Vector([32, 32]), Vector([1e-4, 1e-4]))
+    kg.makeTime(1500.0, 0.3)
+    med = kWaveMedium(sound_speed=1500.0, density=1000.0)
+    src = kSource()
+    src.p0 = np.zeros((32, 32))
+    src.p0[16, 16] = 1.0
+    mask = np.zeros((32, 32), bool)
+    mask[8, :] = True
+    sen = kSensor(mask)
+    backend.install()
+    try:
+        assert native.run_python_backend is not original
+        with pytest.warns(FutureWarning):
+            out = K2.kspaceFirstOrder2D(kg, src, sen, med, SimulationOptions(), backend.execution_options())
+        assert out["p"][0] == "gb300"
+        with pytest.warns(FutureWarning):
+            out = K2.kspaceFirstOrder2D(kg, src, sen, med, SimulationOptions(),
+                                        SimulationExecutionOptions(backend="python", is_gpu_simulation=False))
+        assert out["p"][0] == "python"
+    finally:
+        backend.uninstall()
+    assert native.run_python_backend is original
+    (t1, a1, kw1), (t2, a2, kw2) = calls
+    assert (t1, t2) == ("gb300", "python")
+    assert all(x is y for x, y in zip(a1, (kg, med, src, sen))) and all(x is y for x, y in zip(a2, a1))
+    keys = ("use_sg", "use_kspace", "smooth_p0", "pml_size", "pml_alpha")
+    assert {k: kw1[k] for k in keys} == {k: kw2[k] for k in keys}
+    assert kw1["pml_size"] == (20, 20) and kw1["pml_alpha"] == (2.0, 2.0)
+    assert kw1["use_sg"] and kw1["use_kspace"] and kw1["smooth_p0"]
+    assert kw1["device"] == "gpu"

@@ -36,13 +36,13 @@ def lib():
     return _lib.lib()
 
 
-def plan_gradient(f, spacing, axis):
+def plan_gradient(f, spacing, axis, use_sg=True, use_kspace=True):
     from kwave_gb300.solver import Simulation
 
     nd = f.ndim
     prob = dict(shape=f.shape, spacing=spacing, dt=2.0, Nt=1, sound_speed=KAPPA_COEF, density=1.0, p0=f,
                 smooth_p0=False, sensor_mask=None, record=("p",), pml_size=(0,) * nd, pml_alpha=(0.0,) * nd,
-                use_sg=True, use_kspace=True)
+                use_sg=use_sg, use_kspace=use_kspace)
     sim = Simulation.from_problem(prob).setup()
     try:
         sim.step()
@@ -51,7 +51,7 @@ def plan_gradient(f, spacing, axis):
         sim.close()
 
 
-def noalloc_gradient(lib, f, spacing, axis):
+def noalloc_gradient(lib, f, spacing, axis, use_sg=True, kappa_coef=KAPPA_COEF):
     import torch
 
     fd = torch.from_numpy(np.ascontiguousarray(f, np.float32)).cuda()
@@ -60,7 +60,7 @@ def noalloc_gradient(lib, f, spacing, axis):
     d = (C.c_double * 3)(*spacing, *([1.0] * (3 - f.ndim)))
     stream = torch.cuda.current_stream().cuda_stream
     rc = lib.kw_gradient_noalloc(C.c_void_p(fd.data_ptr()), C.c_void_p(out.data_ptr()), f.ndim, shape, d, axis,
-                                 KAPPA_COEF, 1, C.c_void_p(stream))
+                                 kappa_coef, int(use_sg), C.c_void_p(stream))
     assert rc == 0, lib.kw_last_error()
     torch.cuda.synchronize()
     return out.cpu().numpy()
@@ -76,6 +76,25 @@ def test_noalloc_gradient_matches_plan_on_two_calls_in_a_row(lib):
         assert np.all(np.isfinite(got))
         err = rel_l2(got, ref)
         assert err <= TOL, (f.shape, axis, err)
+
+
+@pytest.mark.parametrize("shape,spacing,axis,use_sg,use_kspace", [
+    ((21, 15), (1e-4, 1.1e-4), 1, True, True),          # odd last axis: full complex row FFT
+    ((14, 12, 9), (1e-4, 0.9e-4, 1.2e-4), 2, True, True),  # 3-D, odd last axis, derivative along it
+    ((20, 18, 10), (1e-4, 1e-4, 1e-4), 2, True, True),   # 3-D, even last axis, axis 2
+    ((30, 25), (1e-4, 1e-4), 0, False, True),            # no staggered-grid shift
+    ((16, 12, 14), (1e-4, 1e-4, 1e-4), 1, True, False),  # kappa_coef = 0 (no k-space correction)
+])
+def test_noalloc_gradient_options_match_plan(lib, shape, spacing, axis, use_sg, use_kspace):
+    """Odd and even last axes, each axis in 3-D, use_sg off and kappa off,
+    each against the plan built with the same options."""
+    rng = np.random.default_rng(sum(shape) + axis)
+    f = np.float32(rng.standard_normal(shape))
+    got = noalloc_gradient(lib, f, spacing, axis, use_sg=use_sg, kappa_coef=KAPPA_COEF if use_kspace else 0.0)
+    ref = plan_gradient(f.astype(np.float64), spacing, axis, use_sg=use_sg, use_kspace=use_kspace)
+    assert np.all(np.isfinite(got))
+    err = rel_l2(got, ref)
+    assert err <= TOL, (shape, axis, use_sg, use_kspace, err)
 
 
 def test_noalloc_rejects_grids_beyond_the_static_scratch(lib):
