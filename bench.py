@@ -179,22 +179,10 @@ def vessel_problem(n=512, nt=1500, seed=0, pml=20, n_sensor=256, radius=11e-3, d
     p0 of 15 smoothed line segments (width 1-4 px) and 5 discs with amplitudes
     U(0.5, 2); ``n_sensor`` Cartesian points on a circle of ``radius``; p0
     smoothing off (the reconstruction variable is p0 itself)."""
-    rng = np.random.default_rng(seed)
-    gx, gy = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
-    p0 = np.zeros((n, n))
-    lo, hi = pml + 0.25 * (n - 2 * pml), n - pml - 0.25 * (n - 2 * pml)
-    for _ in range(15):
-        x0, y0, x1, y1 = rng.uniform(lo, hi, 4)
-        w = rng.uniform(1, 4) / 2
-        vx, vy = x1 - x0, y1 - y0
-        t = np.clip(((gx - x0) * vx + (gy - y0) * vy) / max(vx * vx + vy * vy, 1e-9), 0, 1)
-        dist = np.hypot(gx - (x0 + t * vx), gy - (y0 + t * vy))
-        p0 = np.maximum(p0, rng.uniform(0.5, 2) * np.clip(w + 0.5 - dist, 0, 1))
-    for _ in range(5):
-        cx, cy, r = rng.uniform(lo, hi), rng.uniform(lo, hi), rng.uniform(2, 6)
-        p0 = np.maximum(p0, rng.uniform(0.5, 2) * np.clip(r + 0.5 - np.hypot(gx - cx, gy - cy), 0, 1))
-    th = 2 * np.pi * np.arange(n_sensor) / n_sensor
-    sensor = np.stack([radius * np.cos(th), radius * np.sin(th)])
+    from kwave_gb300.phantoms import circle_points, vessel_phantom
+
+    p0 = vessel_phantom(n, np.random.default_rng(seed), pml)
+    sensor = circle_points(n_sensor, radius)
     return dict(shape=(n, n), spacing=(dx, dx), dt=0.3 * dx / 1500.0, Nt=nt, sound_speed=1500.0, density=1000.0,
                 p0=p0, smooth_p0=False, sensor_mask=sensor, record=("p",), pml_size=(pml, pml),
                 pml_alpha=(2.0, 2.0), use_sg=True, use_kspace=True)
@@ -657,43 +645,70 @@ def run_transmit(args):
 
 ADJOINT_WORKLOAD = ("p0 reconstruction: 512^2 incl. 20-pt PML, dx=0.05 mm, c=1500, lossless, vessel phantom "
                     "(15 segments + 5 discs), 256-point Cartesian circle r=11 mm, 1500 steps, data + 1 % noise, "
-                    "steepest descent with exact line search from zero")
+                    "CGLS (conjugate gradients on the normal equations) from zero")
 
 
 def run_adjoint(args):
-    """p0 reconstruction by plain adjoint iterations: each iteration is one
-    GPU adjoint (transposed time loop) and one forward pass.  ``value`` =
-    cell-steps of all passes / wall time; the line also gives seconds per
-    iteration, the relative p0 error per iteration and the time to 1 %."""
+    """p0 reconstruction by plain adjoint iterations (CGLS): each iteration is
+    one GPU adjoint (transposed time loop) and one forward pass on one device
+    plan (``adjoint.LinearP0``).  ``value`` = cell-steps of all passes / wall
+    time of the iterations, host inputs and outputs of every pass included
+    (what ``e2e`` also reports); the line gives seconds per iteration, the
+    relative p0 error per iteration, the time to 1 % and, under
+    ``gradient_p0_c``, one checkpointed misfit gradient with respect to p0
+    and c (the sound-speed gradient of the same problem)."""
     import torch
 
     import __graft_entry__ as g
 
     g.build()
-    from kwave_gb300.adjoint import adjoint_p0, forward_p0, steepest_descent_p0
+    from kwave_gb300.adjoint import LinearP0, cgls_p0, default_checkpoint_interval, misfit_gradients
 
     prob = vessel_problem(nt=1500)
     rng = np.random.default_rng(11)
-    d_clean = forward_p0(prob, prob["p0"])
+    op = LinearP0(prob)
+    d_clean = op.forward(prob["p0"])
     d_obs = d_clean + 0.01 * np.std(d_clean) * rng.standard_normal(d_clean.shape)
-    fwd = lambda p: forward_p0(prob, p)  # noqa: E731
-    adj = lambda r: adjoint_p0(prob, r)  # noqa: E731
-    steepest_descent_p0(fwd, adj, d_obs, np.zeros(prob["shape"]), 1)  # warm-up (library, kernels)
+    cgls_p0(op.forward, op.adjoint, d_obs, np.zeros(prob["shape"]), 1)  # warm-up (library, kernels, graphs)
     torch.cuda.synchronize()
     iters = max(1, args.steps if args.steps < 1000 else 20)
-    t0 = time.perf_counter()
-    p, hist = steepest_descent_p0(fwd, adj, d_obs, np.zeros(prob["shape"]), iters, p_true=prob["p0"])
-    secs = time.perf_counter() - t0
+    p0 = op.passes
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        p, hist = cgls_p0(op.forward, op.adjoint, d_obs, np.zeros(prob["shape"]), iters, p_true=prob["p0"])
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+    passes = op.passes - p0
+    op.close()
     cells = int(np.prod(prob["shape"]))
-    passes = 1 + 2 * iters  # initial forward, then adjoint + forward per iteration
     errs = [h[1] for h in hist]
     to1 = next((i + 1 for i, e in enumerate(errs) if e <= 0.01), None)
-    line = {"metric": METRIC, "value": cells * prob["Nt"] * passes / secs / 1e6, "unit": UNIT, "n_gpus": 1,
+    nslots = 256 * 4  # bilinear corners of the Cartesian points
+    h2d = (cells * 4 + nslots * prob["Nt"] * 4) / 2  # p0 of a forward or residual of an adjoint, per pass
+    d2h = (256 * prob["Nt"] * 4 + cells * 4) / 2     # series of a forward or gradient of an adjoint, per pass
+    value = cells * prob["Nt"] * passes / secs / 1e6
+    # one gradient with respect to p0 and c (checkpointed forward + adjoint)
+    K = default_checkpoint_interval(prob["Nt"], 2)
+    misfit_gradients(prob, 0.5 * prob["p0"], d_obs, checkpoint_interval=K)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    misfit_gradients(prob, 0.5 * prob["p0"], d_obs, checkpoint_interval=K)
+    torch.cuda.synchronize()
+    gsecs = time.perf_counter() - t0
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
             "steps": iters, "warmup": 1, "ms_per_step": 1e3 * secs / iters, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic vessel phantom, 1 % noise",
-            "config": {"workload": ADJOINT_WORKLOAD, "iterations": iters},
+            "config": {"workload": ADJOINT_WORKLOAD, "iterations": iters, "passes": passes,
+                       "l2": "each pass streams the 512^2 state 1500 times; no flush between passes"},
             "seconds_per_iteration": secs / iters, "p0_rel_error": errs,
-            "iterations_to_1pct": to1, "seconds_to_1pct": None if to1 is None else secs / iters * to1}
+            "iterations_to_1pct": to1, "seconds_to_1pct": None if to1 is None else secs / iters * to1,
+            "gradient_p0_c": {"seconds": gsecs, "checkpoint_interval": K,
+                              "note": "forward with checkpoints every K steps, then the transposed loop regenerating "
+                                      "each segment's forward density sums"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d / prob["Nt"],
+                    "d2h_bytes_per_step": d2h / prob["Nt"],
+                    "note": "every pass takes host inputs and returns host outputs; a step is one time step"},
+            "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0
 

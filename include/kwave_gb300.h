@@ -139,6 +139,12 @@ int32_t kw_plan_set_p0_smoothing(kw_plan* plan, const float* window, int32_t n, 
  * not also be set with kw_plan_set_field. */
 int32_t kw_plan_derive_medium(kw_plan* plan, int32_t what, const float* alpha, int64_t n, double alpha_s,
                               double alpha_power, int32_t absorb_mode);
+/* Replaces the initial pressure of a finalized plan that was given a p0 grid
+ * (n = N_total values) and rewinds it to t = 0 as kw_plan_reset does, keeping
+ * everything else uploaded.  No counterpart in the reference, where a new p0
+ * means a new Simulation; iterative reconstructions run many forward passes
+ * that differ only in p0. */
+int32_t kw_plan_update_p0(kw_plan* plan, const float* host, int64_t n);
 /* Allocates device memory, uploads all inputs and resets the state to t = 0. */
 int32_t kw_plan_finalize(kw_plan* plan);
 /* Advances min(nsteps, Nt - t) steps of Simulation.step (kspace_solver.py:691-747)
@@ -170,6 +176,25 @@ int32_t kw_plan_autotune(kw_plan* plan, int32_t nsteps, void* stream, int32_t* T
  * 1/2 ||recorded p - observed||^2.  The plan is reset (t = 0, zero state)
  * before and after; its uploaded medium, PML and sensor are used. */
 int32_t kw_plan_adjoint_p0(kw_plan* plan, const float* residual, int64_t n, float* grad, void* stream);
+/* Checkpoints of the forward run for kw_plan_adjoint's sound-speed gradient
+ * (no counterpart in the reference): with interval K > 0, kw_plan_run keeps
+ * the state carried between steps (u_i, rho_i and the spectrum of p) after
+ * every step t with t % K == 0, in ceil(Nt / K) device slots of
+ * (2 D N_total + 2 spectrum) floats each; K = 1 keeps every step (no
+ * recomputation), larger K trades memory for rerunning up to K - 1 steps per
+ * segment.  0 frees them.  The plan must be at t = 0. */
+int32_t kw_plan_set_checkpoints(kw_plan* plan, int32_t interval);
+/* Adjoint of the time loop with both gradients (no counterpart in the
+ * reference): as kw_plan_adjoint_p0 for grad_p0; when grad_c is not NULL it
+ * also receives the gradient with respect to the sound speed c0 (N_total
+ * float32) of sum(residual * recorded p), with c_ref (PML, kappa) held at the
+ * plan's value.  That needs the forward run of this plan from t = 0 to Nt
+ * with p0 set, smoothing off and checkpoints on (kw_plan_set_checkpoints):
+ * the forward density sum of every step is regenerated segment by segment
+ * from the checkpoints while the transposed steps run backwards.  The result
+ * does not depend on the interval: the regenerated steps are the forward's
+ * own steps, bit for bit.  The plan is reset (t = 0) afterwards. */
+int32_t kw_plan_adjoint(kw_plan* plan, const float* residual, int64_t n, float* grad_p0, float* grad_c, void* stream);
 /* enable == 0: every step as plain launches (default 1; the environment
  * variable KWAVE_GB300_GRAPHS=0 sets 0 at kw_plan_finalize). */
 int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);
@@ -246,6 +271,59 @@ int32_t kw_plan_launch_count(const kw_plan* plan, int64_t* count);
  * by the caller.  Work is enqueued on `stream` (NULL = default stream). */
 int32_t kw_gradient_noalloc(const float* f, float* out, int32_t ndim, const int32_t* shape, const double* spacing,
                             int32_t axis, double kappa_coef, int32_t use_sg, void* stream);
+/* ---- learned warm start (no counterpart in the reference) ----------------
+ * Kernels of a BF16 U-Net with FP32 accumulation on the 5th-generation tensor
+ * cores (tcgen05.mma with the accumulator in tensor memory), trained and run
+ * by kwave_gb300.warmstart.  Its input is a time-reversal image
+ * (kwave/reconstruction/time_reversal.py:129-150), its output an initial
+ * pressure estimate that adjoint iterations refine.  All pointers are device
+ * pointers owned by the caller; activations are bf16 NHWC, parameters and
+ * gradients f32; every call enqueues on `stream` (NULL = default stream). */
+/* C[M][N] (f32) = sum_k A[m][k] B[n][k], A and B row-major bf16, K % 8 == 0. */
+int32_t kw_umma_gemm(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, void* stream);
+/* 3x3 convolution, stride 1, zero padding: y[p][co] = act(bias[co] + sum over
+ * taps and input channels of w[co][tap][ci] x[p + tap][ci]), where the input is
+ * x1 (nb, H, W, c1) followed along channels by x2 (nb, H/2, W/2, c2) read with
+ * nearest-neighbour upsampling (c2 = 0: x1 alone).  c1, c2 multiples of 8,
+ * cout a multiple of 16; act = ReLU when relu != 0.  Output to y (bf16) and/or
+ * yf (f32), (nb, H, W, cout).  With the output gradient as x1 and the weights
+ * from kw_unet_flip_weights it is the data gradient. */
+int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
+                   const void* w, const float* bias, int32_t cout, int32_t relu, void* y, float* yf, void* stream);
+/* Weight gradient of kw_conv3x3: dw[co][tap][ci] += sum over pixels of
+ * dz[p][co] x[p + tap][ci] (x as in kw_conv3x3), cout a multiple of 8. */
+int32_t kw_conv3x3_wgrad(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
+                         const void* dz, int32_t cout, float* dw, void* stream);
+/* 2x2 average pooling (nb, H, W, C) -> (nb, H/2, W/2, C), and its gradient
+ * (dx = dy/4 on each child, plus `add` when not NULL). */
+int32_t kw_unet_avgpool2(const void* x, void* y, int32_t nb, int32_t H, int32_t W, int32_t C, void* stream);
+int32_t kw_unet_avgpool2_bwd(const void* dy, void* dx, int32_t nb, int32_t H, int32_t W, int32_t C, const void* add,
+                             void* stream);
+/* dz = dy where y > 0, else 0 (ReLU gradient), n bf16 values. */
+int32_t kw_unet_relu_grad(const void* dy, const void* y, void* dz, int64_t n, void* stream);
+/* Gradient of a concatenated input (nb, H, W, C1 + C2): channels < C1 to d1
+ * (plus add1 when not NULL), the rest summed over each 2x2 block to d2
+ * (nb, H/2, W/2, C2), the gradient of the nearest-neighbour upsampling. */
+int32_t kw_unet_split_concat_grad(const void* dcat, int32_t nb, int32_t H, int32_t W, int32_t C1, int32_t C2, void* d1,
+                                  const void* add1, void* d2, void* stream);
+/* wt[ci][8 - tap][co] = w[co][tap][ci] (bf16): the data-gradient weights. */
+int32_t kw_unet_flip_weights(const void* w, void* wt, int32_t cout, int32_t cin, void* stream);
+/* db[c] += sum over npix pixels of dz[p][c]. */
+int32_t kw_unet_bias_grad(const void* dz, float* db, int64_t npix, int32_t C, void* stream);
+/* Residual-form estimate e[p] = out[p][0] + s img[p] (out (npix, cout) f32,
+ * img (npix) f32): kw_unet_residual_out writes e; kw_unet_mse_grad adds
+ * sum (e - target)^2 to *loss and writes dout[p][0] = scale (e - target),
+ * the other channels 0 (bf16). */
+int32_t kw_unet_mse_grad(const float* out, int32_t cout, const float* img, float s, const float* target, void* dout,
+                         int64_t npix, float scale, float* loss, void* stream);
+int32_t kw_unet_residual_out(const float* out, int32_t cout, const float* img, float s, float* e, int64_t npix,
+                             void* stream);
+/* Adam step (bias-corrected, step >= 1) on f32 parameters w with moments m, v
+ * and gradient g; wb (may be NULL) receives the bf16 copy. */
+int32_t kw_unet_adam(float* w, float* m, float* v, const float* g, void* wb, int64_t n, float lr, float b1, float b2,
+                     float eps, int32_t step, void* stream);
+/* f32 image (npix) -> bf16 NHWC with C channels: channel 0 = scale * image, others 0. */
+int32_t kw_unet_image_to_nhwc(const float* img, void* x, int64_t npix, int32_t C, float scale, void* stream);
 /* Frees all device memory of the plan. */
 int32_t kw_plan_destroy(kw_plan* plan);
 

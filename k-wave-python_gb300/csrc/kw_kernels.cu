@@ -350,6 +350,10 @@ struct GenericRowFFT {
 // u_i = (a_i / 2) G_i p0 gives the gradient with respect to p0:
 //   ADJ_D: lp += S^T r_0; S_i <- F[(a_i / 2) lu_i]   (passes: op_div)
 //   ADJ_E: g = lp + sum_i lr_i / (c^2 D) - sum_i F^-1 S_i   (into p)
+// With the sound-speed gradient on (gacc set), ADJ_A also accumulates
+// gacc += fsum_t lp' (fsum_t = forward sum_i rho_i after step t, so that
+// p_t = c^2 fsum_t), and ADJ_E turns the c^2 gradient into the c gradient:
+//   gacc <- 2 c (gacc - p0 sum_i lr_i / (c^4 D)).
 template <class RF>
 __device__ __forceinline__ void adjoint_body(const RowsParams& P, const RF& rf, float* const* rb, int r0, int nr) {
   const int L = P.L, R = P.R;
@@ -370,6 +374,7 @@ __device__ __forceinline__ void adjoint_body(const RowsParams& P, const RF& rf, 
       const long long g = (long long)(r0 + row) * L + z;
       const float lp = lpb[i];
       if (P.stage == ST_ADJ_A) {
+        if (P.gacc) P.gacc[g] = __fmaf_rn(P.fsum[g], lp, P.gacc[g]);
         const float c = fld(P.c0, P.c0_s, g);
         const float c2 = __fmul_rn(c, c);
         const float b = __fmul_rn(P.dt, fld(P.rho0, P.rho0_s, g));
@@ -423,6 +428,12 @@ __device__ __forceinline__ void adjoint_body(const RowsParams& P, const RF& rf, 
       float acc = P.p[g];
       for (int a = 0; a < D; ++a) acc = __fadd_rn(acc, __fdiv_rn(P.rho[a][g], den));
       P.p[g] = __fsub_rn(acc, s);
+      if (P.gacc) {
+        float lr = P.rho[0][g];
+        for (int a = 1; a < D; ++a) lr = __fadd_rn(lr, P.rho[a][g]);
+        const float ov = __fdiv_rn(__fmul_rn(P.p0[g], lr), __fmul_rn(den, __fmul_rn(c, c)));
+        P.gacc[g] = __fmul_rn(__fmul_rn(2.f, c), __fsub_rn(P.gacc[g], ov));
+      }
     }
   }
 }
@@ -859,6 +870,15 @@ cudaError_t kw_axis_reg_launch(int n, dim3 grid, size_t smem, cudaStream_t st, c
 // ---------------------------------------------------------------------------
 // device step counter of replayed step graphs
 // ---------------------------------------------------------------------------
+__global__ void k_density_sum(float* __restrict__ out, const float* __restrict__ r0, const float* __restrict__ r1,
+                              const float* __restrict__ r2, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float s = __fadd_rn(r0[i], r1[i]);
+    if (r2) s = __fadd_rn(s, r2[i]);
+    out[i] = s;
+  }
+}
+
 __global__ void k_step_set(int* tdev, int t) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *tdev = t;
 }

@@ -95,6 +95,11 @@ struct RowsParams {
   // inside a replayed step graph: the plan's device step counter; t and
   // rec_row are then offsets added to it (nullptr: t and rec_row as given)
   const int* tdev;
+  // adjoint with the sound-speed gradient: fsum = forward density sum
+  // sum_i rho_i of the step being transposed (ST_ADJ_A), gacc = accumulator of
+  // the c^2 gradient, turned into the c gradient by ST_ADJ_E (nullptr: off)
+  const float* fsum;
+  float* gacc;
 };
 
 // step index and record column of a row-stage launch
@@ -199,6 +204,9 @@ __global__ void k_ratio(const unsigned int* a, const unsigned int* b, float* out
 // device step counter of a plan: set before a run of graph steps, advanced by
 // the last node of each step graph
 __global__ void k_step_set(int* tdev, int t);
+// out = rho_0 + rho_1 (+ rho_2): the forward density sum, in the step's order
+__global__ void k_density_sum(float* __restrict__ out, const float* __restrict__ r0, const float* __restrict__ r1,
+                              const float* __restrict__ r2, long long n);
 __global__ void k_step_tick(int* tdev);
 __global__ void k_step_tick_group(int* const* tdev, int n);
 // grouped generic passes over several plans (blk: per member first block and grid shape)

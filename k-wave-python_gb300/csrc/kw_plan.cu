@@ -147,6 +147,14 @@ struct kw_plan {
   int* d_tstep = nullptr;
   int tstep_val = -1;  // value d_tstep holds once the stream reaches the last enqueued work
   cudaStream_t cap_stream = nullptr;
+  // checkpoints of the carried state for the sound-speed gradient: slot s
+  // holds u_i, rho_i and the spectrum of p after step s * ckpt_K
+  int ckpt_K = 0;
+  std::vector<float*> ckpt;
+  std::vector<char> ckpt_ok;
+  // set by kw_plan_adjoint around its ST_ADJ_A / ST_ADJ_E launches
+  const float* adj_fsum = nullptr;
+  float* adj_gacc = nullptr;
   // launch accounting / timing
   long long launches = 0;
   bool timing = false;
@@ -306,6 +314,19 @@ int32_t kw_plan_set_field(kw_plan* p, int32_t field, const float* host, int64_t 
   }
   p->hscalar[field] = scalar;
   return KW_OK;
+}
+
+int32_t kw_plan_update_p0(kw_plan* p, const float* host, int64_t n) {
+  if (!p || !host) return fail(KW_ERR_INVALID, "kw_plan_update_p0: null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_update_p0 before kw_plan_finalize");
+  if (p->hfield[KW_F_P0].empty() || !p->d_field[KW_F_P0])
+    return fail(KW_ERR_STATE, "kw_plan_update_p0: the plan was finalized without a p0 grid");
+  if (n != p->ntot) return fail(KW_ERR_INVALID, "p0 has %lld values, grid has %lld", (long long)n, p->ntot);
+  CK(cudaDeviceSynchronize());
+  p->hfield[KW_F_P0].assign(host, host + n);
+  CK(cudaMemcpy(p->d_field[KW_F_P0], host, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+  p->p0s_ready = false;  // smoothing (if on) runs again on the new p0
+  return kw_plan_reset(p);
 }
 
 int32_t kw_plan_derive_medium(kw_plan* p, int32_t what, const float* alpha, int64_t n, double alpha_s, double alpha_power,
@@ -741,6 +762,8 @@ static void fill_rows(const kw_plan* p, RowsParams& P) {
   P.sens_ent = p->d_sens_ent;
   P.nslots = p->nslots;
   for (int s = 0; s < 7; ++s) P.rec[s] = p->d_rec[s];
+  P.fsum = p->adj_fsum;
+  P.gacc = p->adj_gacc;
 }
 
 // Host-side checks that every buffer a launch will touch exists: an internal
@@ -1189,6 +1212,25 @@ static int run_step(kw_plan* p, int t, int end, cudaStream_t st) {
 
 // plain_last == false (autotuning only): the last step is a graph step too and
 // leaves p in spectral form only.
+static size_t ckpt_floats(const kw_plan* p) { return 2 * (size_t)p->D * p->ntot + 2 * (size_t)p->spec_elems; }
+
+// Copy the state carried into step t + 1 (u_i, rho_i, spectrum of p) to or
+// from checkpoint slot s.
+static int ckpt_copy(kw_plan* p, int s, bool save, cudaStream_t st) {
+  float* base = p->ckpt[s];
+  const size_t nf = (size_t)p->ntot * sizeof(float);
+  for (int a = 0; a < p->D; ++a) {
+    float* cu = base + (size_t)a * p->ntot;
+    float* cr = base + (size_t)(p->D + a) * p->ntot;
+    CK(cudaMemcpyAsync(save ? cu : p->d_u[a], save ? p->d_u[a] : cu, nf, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(save ? cr : p->d_rho[a], save ? p->d_rho[a] : cr, nf, cudaMemcpyDeviceToDevice, st));
+  }
+  float* cs = base + 2 * (size_t)p->D * p->ntot;
+  CK(cudaMemcpyAsync(save ? (void*)cs : (void*)p->d_S[B_P], save ? (void*)p->d_S[B_P] : (void*)cs,
+                     (size_t)p->spec_elems * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+  return KW_OK;
+}
+
 static int plan_run(kw_plan* p, int nsteps, cudaStream_t st, bool plain_last) {
   const int end = std::min(p->g.Nt, p->t + nsteps);
   const int eend = plain_last ? end : end + 1;
@@ -1196,6 +1238,11 @@ static int plan_run(kw_plan* p, int nsteps, cudaStream_t st, bool plain_last) {
     int rc = run_step(p, t, eend, st);
     if (rc) return rc;
     p->t = t + 1;
+    if (p->ckpt_K > 0 && t % p->ckpt_K == 0) {
+      const int s = t / p->ckpt_K;
+      if ((rc = ckpt_copy(p, s, true, st))) return rc;
+      p->ckpt_ok[s] = 1;
+    }
   }
   return KW_OK;
 }
@@ -1274,13 +1321,74 @@ int32_t kw_plan_autotune(kw_plan* p, int32_t nsteps, void* stream, int32_t* T_ou
 
 static int check_device_error();
 
-// Gradient with respect to p0 of <residual, recorded p> for the lossless,
-// source-free loop with a binary sensor: the transposed steps t = Nt-1 .. 1
-// and the transposed t = 0 override (adjoint_body in kw_kernels.cu), on the
-// run-time-length row kernels.  The plan is reset before and after.
-int32_t kw_plan_adjoint_p0(kw_plan* p, const float* residual, int64_t n, float* grad, void* stream) {
-  if (!p || !residual || !grad) return fail(KW_ERR_INVALID, "kw_plan_adjoint_p0: null argument");
-  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_adjoint_p0 before kw_plan_finalize");
+int32_t kw_plan_set_checkpoints(kw_plan* p, int32_t interval) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_set_checkpoints before kw_plan_finalize");
+  if (interval < 0) return fail(KW_ERR_INVALID, "checkpoint interval < 0");
+  if (p->t != 0) return fail(KW_ERR_STATE, "kw_plan_set_checkpoints needs the plan at t = 0");
+  CK(cudaDeviceSynchronize());
+  for (float* c : p->ckpt) dfree_last(p, c);
+  p->ckpt.clear();
+  p->ckpt_ok.clear();
+  p->ckpt_K = 0;
+  if (interval == 0) return KW_OK;
+  const int nslot = (p->g.Nt - 1) / interval + 1;
+  p->ckpt.assign(nslot, nullptr);
+  for (int s = 0; s < nslot; ++s) {
+    int rc = dalloc(p, &p->ckpt[s], ckpt_floats(p));
+    if (rc) {
+      p->ckpt.resize(s);
+      for (float* c : p->ckpt) dfree_last(p, c);
+      p->ckpt.clear();
+      return rc;
+    }
+  }
+  p->ckpt_ok.assign(nslot, 0);
+  p->ckpt_K = interval;
+  return KW_OK;
+}
+
+namespace {
+// Adjoint state and work buffers of one kw_plan_adjoint call (freed on return).
+struct AdjBufs {
+  std::vector<void*> mem;
+  ~AdjBufs() {
+    for (void* m : mem) cudaFree(m);
+  }
+  int get(float** out, size_t count) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaMalloc(&ptr, count * sizeof(float));
+    if (e != cudaSuccess)
+      return fail(e == cudaErrorMemoryAllocation ? KW_ERR_OOM : KW_ERR_CUDA, "cudaMalloc(%zu): %s",
+                  count * sizeof(float), cudaGetErrorString(e));
+    mem.push_back(ptr);
+    *out = static_cast<float*>(ptr);
+    return KW_OK;
+  }
+};
+}  // namespace
+
+// Exchanges the plan's state and p series with the adjoint's buffers, so that
+// the row stages (which read the plan) see the adjoint state.
+static void adj_swap(kw_plan* p, float*& lp, float** lu, float** lr, float*& res) {
+  std::swap(p->d_p, lp);
+  for (int a = 0; a < p->D; ++a) {
+    std::swap(p->d_u[a], lu[a]);
+    std::swap(p->d_rho[a], lr[a]);
+  }
+  std::swap(p->d_rec[KW_R_P], res);
+}
+
+// The gradient of <residual, recorded p> for the lossless, source-free loop:
+// the transposed steps t = Nt-1 .. 1 and the transposed t = 0 override
+// (adjoint_body in kw_kernels.cu) on the run-time-length row kernels, with the
+// adjoint state in buffers of its own.  With grad_c, the forward density sum
+// of every step is regenerated from the checkpoints, segment by segment from
+// the last (restore slot s, rerun its steps, keep sum_i rho_i of each), and
+// the segment's adjoint steps accumulate the sound-speed gradient.
+int32_t kw_plan_adjoint(kw_plan* p, const float* residual, int64_t n, float* grad_p0, float* grad_c, void* stream) {
+  if (!p || !residual || !grad_p0) return fail(KW_ERR_INVALID, "kw_plan_adjoint: null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_adjoint before kw_plan_finalize");
   if (p->g.absorb_mode != 0 || p->g.nonlinear)
     return fail(KW_ERR_UNSUPPORTED, "the adjoint covers the lossless loop (no absorption, no B/A)");
   for (int s = 0; s < 6; ++s)
@@ -1289,48 +1397,122 @@ int32_t kw_plan_adjoint_p0(kw_plan* p, const float* residual, int64_t n, float* 
     return fail(KW_ERR_UNSUPPORTED, "the adjoint needs a sensor recording p");
   if (n != (int64_t)p->nrec * p->nslots)
     return fail(KW_ERR_INVALID, "residual has %lld values, expected %lld", (long long)n, (long long)p->nrec * p->nslots);
+  const int K = p->ckpt_K;
+  if (grad_c) {
+    if (p->smooth) return fail(KW_ERR_UNSUPPORTED, "the sound-speed gradient needs p0 smoothing off");
+    if (p->hfield[KW_F_P0].empty()) return fail(KW_ERR_STATE, "the sound-speed gradient needs the forward's p0");
+    if (K <= 0) return fail(KW_ERR_STATE, "the sound-speed gradient needs checkpoints (kw_plan_set_checkpoints)");
+    if (p->t != p->g.Nt) return fail(KW_ERR_STATE, "the sound-speed gradient needs the forward run to t = Nt");
+    for (char ok : p->ckpt_ok)
+      if (!ok) return fail(KW_ERR_STATE, "a checkpoint of the forward run is missing (run from t = 0 after setting them)");
+  }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  int rc = kw_plan_reset(p);
+  const int D = p->D;
+  const bool three = D == 3;
+  const size_t nt = (size_t)p->ntot;
+  AdjBufs B;
+  float *lp, *lu[3] = {nullptr, nullptr, nullptr}, *lr[3] = {nullptr, nullptr, nullptr}, *res, *gacc = nullptr;
+  float* seg = nullptr;
+  int rc = B.get(&lp, nt);
+  for (int a = 0; a < D && !rc; ++a)
+    if (!(rc = B.get(&lu[a], nt))) rc = B.get(&lr[a], nt);
+  if (!rc) rc = B.get(&res, (size_t)n);
+  if (!rc && grad_c && !(rc = B.get(&gacc, nt))) rc = B.get(&seg, (size_t)K * nt);
   if (rc) return rc;
+  CK(cudaMemsetAsync(lp, 0, nt * sizeof(float), st));
+  for (int a = 0; a < D; ++a) {
+    CK(cudaMemsetAsync(lu[a], 0, nt * sizeof(float), st));
+    CK(cudaMemsetAsync(lr[a], 0, nt * sizeof(float), st));
+  }
+  if (gacc) CK(cudaMemsetAsync(gacc, 0, nt * sizeof(float), st));
   {
     // sensor-major (n_points, n_rec) -> the time-major series layout
     std::vector<float> tm((size_t)n);
     for (int s = 0; s < p->nslots; ++s)
       for (int t = 0; t < p->nrec; ++t) tm[(size_t)t * p->nslots + s] = residual[(size_t)s * p->nrec + t];
-    CK(cudaMemcpy(p->d_rec[KW_R_P], tm.data(), tm.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(res, tm.data(), tm.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
   }
   const bool timing = p->timing;
   p->timing = false;
-  const int D = p->D;
-  const bool three = D == 3;
   const int SB[3] = {0, 1, 2};
   AxisJob gj[3], dj[3];
   for (int a = 0; a < D; ++a) {
     gj[a] = AxisJob{a, a, OP_GRAD, a};
     dj[a] = AxisJob{a, a, OP_DIV, a};
   }
-  for (int t = p->g.Nt - 1; t >= 1 && !rc; --t) {
-    if ((rc = launch_rows(p, ST_ADJ_A, 0, t, 0, st))) break;
-    if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) break;
-    if ((rc = launch_axis_ops(p, gj, D, st))) break;
-    if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) break;
-    if ((rc = launch_rows(p, ST_ADJ_B, 0, t, 0, st))) break;
-    if (three && (rc = launch_axis_plain(p, 1, 0, SB, D, st))) break;
-    if ((rc = launch_axis_ops(p, dj, D, st))) break;
-    if (three && (rc = launch_axis_plain(p, 1, 1, SB, D, st))) break;
-    rc = launch_rows(p, ST_ADJ_C, 0, t, 0, st);
+  const long long grid = std::min<long long>(((long long)nt + 255) / 256, 8LL * p->nsm);
+  auto dsum = [&](float* out) -> int {
+    k_density_sum<<<(int)grid, 256, 0, st>>>(out, p->d_rho[0], p->d_rho[1], D == 3 ? p->d_rho[2] : nullptr,
+                                             (long long)nt);
+    CK(cudaGetLastError());
+    p->launches++;
+    return KW_OK;
+  };
+  // adjoint steps t = hi .. lo (descending), the plan's buffers swapped for the adjoint's
+  auto adj_steps = [&](int hi, int lo, int t_base) -> int {
+    adj_swap(p, lp, lu, lr, res);
+    int r = KW_OK;
+    for (int t = hi; t >= lo && !r; --t) {
+      p->adj_fsum = seg ? seg + (size_t)(t - t_base) * nt : nullptr;
+      p->adj_gacc = gacc;
+      if ((r = launch_rows(p, ST_ADJ_A, 0, t, 0, st))) break;
+      p->adj_fsum = nullptr;
+      p->adj_gacc = nullptr;
+      if (three && (r = launch_axis_plain(p, 1, 0, SB, D, st))) break;
+      if ((r = launch_axis_ops(p, gj, D, st))) break;
+      if (three && (r = launch_axis_plain(p, 1, 1, SB, D, st))) break;
+      if ((r = launch_rows(p, ST_ADJ_B, 0, t, 0, st))) break;
+      if (three && (r = launch_axis_plain(p, 1, 0, SB, D, st))) break;
+      if ((r = launch_axis_ops(p, dj, D, st))) break;
+      if (three && (r = launch_axis_plain(p, 1, 1, SB, D, st))) break;
+      r = launch_rows(p, ST_ADJ_C, 0, t, 0, st);
+    }
+    p->adj_fsum = nullptr;
+    p->adj_gacc = nullptr;
+    adj_swap(p, lp, lu, lr, res);
+    return r;
+  };
+  const int Nt = p->g.Nt;
+  if (!grad_c) {
+    rc = adj_steps(Nt - 1, 1, 0);
+  } else {
+    // forward recomputation runs as plain launches and records nothing
+    float* rec_p = p->d_rec[KW_R_P];
+    p->d_rec[KW_R_P] = nullptr;
+    const int nseg = (Nt - 1) / K + 1;
+    for (int s = nseg - 1; s >= 0 && !rc; --s) {
+      const int t0 = s * K, t1 = std::min(t0 + K - 1, Nt - 1);
+      if ((rc = ckpt_copy(p, s, false, st))) break;
+      if ((rc = dsum(seg))) break;
+      for (int t = t0 + 1; t <= t1 && !rc; ++t)
+        if (!(rc = enqueue_step(p, t, t == Nt - 1, st))) rc = dsum(seg + (size_t)(t - t0) * nt);
+      if (!rc) rc = adj_steps(t1, std::max(t0, 1), t0);
+    }
+    p->d_rec[KW_R_P] = rec_p;
   }
-  if (!rc) rc = launch_rows(p, ST_ADJ_D, 0, 0, 0, st);
-  if (!rc && three) rc = launch_axis_plain(p, 1, 0, SB, D, st);
-  if (!rc) rc = launch_axis_ops(p, dj, D, st);
-  if (!rc && three) rc = launch_axis_plain(p, 1, 1, SB, D, st);
-  if (!rc) rc = launch_rows(p, ST_ADJ_E, 0, 0, 0, st);
+  if (!rc) {
+    adj_swap(p, lp, lu, lr, res);
+    rc = launch_rows(p, ST_ADJ_D, 0, 0, 0, st);
+    if (!rc && three) rc = launch_axis_plain(p, 1, 0, SB, D, st);
+    if (!rc) rc = launch_axis_ops(p, dj, D, st);
+    if (!rc && three) rc = launch_axis_plain(p, 1, 1, SB, D, st);
+    p->adj_gacc = gacc;
+    if (!rc) rc = launch_rows(p, ST_ADJ_E, 0, 0, 0, st);
+    p->adj_gacc = nullptr;
+    adj_swap(p, lp, lu, lr, res);
+  }
   p->timing = timing;
   if (rc) return rc;
   CK(cudaStreamSynchronize(st));
   if ((rc = check_device_error())) return rc;
-  CK(cudaMemcpy(grad, p->d_p, (size_t)p->ntot * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad_p0, lp, nt * sizeof(float), cudaMemcpyDeviceToHost));
+  if (grad_c) CK(cudaMemcpy(grad_c, gacc, nt * sizeof(float), cudaMemcpyDeviceToHost));
   return kw_plan_reset(p);
+}
+
+int32_t kw_plan_adjoint_p0(kw_plan* p, const float* residual, int64_t n, float* grad, void* stream) {
+  return kw_plan_adjoint(p, residual, n, grad, nullptr, stream);
 }
 
 int32_t kw_plan_set_graphs(kw_plan* p, int32_t enable) {
@@ -1873,6 +2055,7 @@ int32_t kw_plan_reset(kw_plan* p) {
   if (rc) return rc;
   CK(cudaDeviceSynchronize());
   p->t = 0;
+  std::fill(p->ckpt_ok.begin(), p->ckpt_ok.end(), 0);
   return KW_OK;
 }
 

@@ -1,0 +1,738 @@
+// Kernels of the learned warm start: a BF16 U-Net (FP32 accumulation) that
+// maps a time-reversal image to an initial-pressure estimate, trained and run
+// with this file's kernels only.  The reference has no counterpart; its input
+// is the image of kwave/reconstruction/time_reversal.py:129-150.
+//
+// Tensor-core core (k_umma): one CTA of 128 threads computes a 128 x NT tile
+// D[m][n] = sum_k A(m, k) B(n, k) on the 5th-generation tensor cores:
+//   * the 128 threads gather 64-wide K chunks of A and B (bf16) into a
+//     two-stage shared-memory ring, in the canonical K-major layout without
+//     swizzle (core matrices of 8 rows x 16 bytes, 128 contiguous bytes each;
+//     LBO = 128 bytes between core matrices along K, SBO = 1024 bytes between
+//     8-row groups);
+//   * one thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> f32, M = 128,
+//     N = NT, K = 16 per instruction) into an accumulator in tensor memory
+//     (TMEM, allocated by warp 0) and tcgen05.commit's each stage to an
+//     mbarrier, which the gatherers wait on before refilling that stage;
+//   * the epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM
+//     lanes 32w..32w+31, one D row per thread).
+// Every mbarrier wait is bounded (2 s of global time); a timeout sets the
+// device error word, skips the epilogue and still frees the TMEM.
+//
+// Gathers:
+//   GEMM   A = row-major [M][K], B = row-major [N][K] (tests of the core)
+//   CONV   3x3 convolution, stride 1, zero padding, NHWC bf16: m = output
+//          pixel, n = output channel, k = (tap, input channel); the input is
+//          one tensor or the concatenation of a full-resolution tensor and a
+//          half-resolution one read through nearest-neighbour upsampling (the
+//          decoder's skip + upsampled input).  The data gradient of a 3x3
+//          convolution is the same gather with the flipped, transposed
+//          weights and the output gradient as input.
+//   WGRAD  weight gradient: m = output channel, n = (tap, input channel),
+//          k = pixel (split over CTAs, partial tiles added with red.add);
+//          8 x 8 blocks are loaded along channels and transposed in registers.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/kwave_gb300.h"
+#include "kw_tma.cuh"
+
+int kw_internal_fail(int code, const char* msg);
+int* kw_device_error_ptr();
+
+namespace {
+
+using kwtma::mbar_init;
+using kwtma::mbar_wait;
+using kwtma::smem_u32;
+
+constexpr int kThreads = 128;
+constexpr int kBM = 128;            // tile rows (TMEM lanes)
+constexpr int kBK = 64;             // K chunk per stage (bf16: 128 bytes per row)
+constexpr int kMaxNT = 256;         // tile columns (TMEM columns)
+constexpr uint32_t kSBO = 1024;     // 8-row group stride in a stage tile
+constexpr uint32_t kLBO = 128;      // K-adjacent core matrix stride
+constexpr int kATile = kBM * kBK * 2;         // 16 KB
+constexpr int kBTileMax = kMaxNT * kBK * 2;   // 32 KB
+constexpr uint64_t kWaitNs = 2000000000ull;
+constexpr int kErrUmmaTimeout = 0x55;
+
+// tcgen05 shared-memory matrix descriptor: K-major, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((kLBO >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((kSBO >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of the 5th-generation tensor cores
+  return d;                // base offset 0, swizzle mode 0 (none)
+}
+
+// Instruction descriptor of kind::f16: D f32, A and B bf16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void umma_bf16(uint32_t taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(taddr),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive f32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Byte offset of the 16-byte chunk (row r, 8-wide K group kc) in a stage tile.
+__device__ __forceinline__ uint32_t chunk_off(int r, int kc) {
+  return (uint32_t)((r >> 3) * kSBO + kc * kLBO + (r & 7) * 16);
+}
+
+__device__ __forceinline__ uint4 ldg16(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+
+// 8 x 8 bf16 transpose: in[j] holds 8 values of row j; out[i] gets element i of every row.
+__device__ __forceinline__ void transpose8(const uint4 (&in)[8], uint4 (&out)[8]) {
+  uint16_t e[8][8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint32_t w[4] = {in[j].x, in[j].y, in[j].z, in[j].w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      e[j][2 * q] = (uint16_t)(w[q] & 0xFFFFu);
+      e[j][2 * q + 1] = (uint16_t)(w[q] >> 16);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q] = (uint32_t)e[2 * q][i] | ((uint32_t)e[2 * q + 1][i] << 16);
+    out[i] = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// gather policies
+// ---------------------------------------------------------------------------
+struct UmmaArgs {
+  int mode;  // 0 GEMM, 1 CONV, 2 WGRAD
+  int M, N, K;
+  int NT;    // tile columns (multiple of 16, <= 256)
+  // GEMM
+  const __nv_bfloat16* A;
+  const __nv_bfloat16* B;
+  float* C;
+  // CONV / WGRAD geometry
+  int nb, H, W;       // batch, output height and width (= input height and width)
+  int C1, C2;         // channels of the full-resolution input and of the half-resolution one (0: none)
+  const __nv_bfloat16* X1;
+  const __nv_bfloat16* X2;
+  const __nv_bfloat16* Wt;   // CONV weights [N][9][C1 + C2]
+  const float* bias;         // CONV: per output channel (may be null)
+  int relu;                  // CONV: apply ReLU
+  __nv_bfloat16* Y;          // CONV output [pixels][N] bf16 (may be null)
+  float* Yf;                 // CONV output [pixels][N] f32 (may be null)
+  const __nv_bfloat16* dZ;   // WGRAD: output gradient [pixels][M]
+  float* dW;                 // WGRAD: [M][N] f32, accumulated
+  int ksplit;                // WGRAD: pixels per CTA (multiple of 64)
+};
+
+// 16-byte chunk of the convolution input for output pixel m and K position k
+// (8 channels of one tap); zero outside the image (padding) and beyond the batch.
+__device__ __forceinline__ uint4 conv_in_chunk(const UmmaArgs& a, int m, int k) {
+  const int cin = a.C1 + a.C2;
+  const int tap = k / cin, ci = k - tap * cin;
+  const int hw = a.H * a.W;
+  const int b = m / hw, rem = m - b * hw;
+  const int y = rem / a.W + tap / 3 - 1, x = rem % a.W + tap % 3 - 1;
+  if (b >= a.nb || tap >= 9 || y < 0 || y >= a.H || x < 0 || x >= a.W) return make_uint4(0, 0, 0, 0);
+  if (ci < a.C1) return ldg16(a.X1 + (((long long)b * a.H + y) * a.W + x) * a.C1 + ci);
+  const int h2 = a.H >> 1, w2 = a.W >> 1;
+  return ldg16(a.X2 + (((long long)b * h2 + (y >> 1)) * w2 + (x >> 1)) * a.C2 + (ci - a.C1));
+}
+
+// Fill stage tiles for K chunk k0 (all 128 threads).
+__device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA, unsigned char* sB, int m0, int n0,
+                                           int k0) {
+  const int tid = threadIdx.x;
+  if (a.mode == 2) {
+    // WGRAD: A(co, p) = dZ[p][co], B((tap, ci), p) = input[p + tap][ci]; 8 x 8 blocks transposed
+    {
+      const int cb = tid >> 3, pb = tid & 7;  // 16 channel blocks x 8 pixel blocks
+      uint4 in[8], out[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int p = k0 + pb * 8 + j;
+        const int co = m0 + cb * 8;
+        in[j] = (p < a.K && co < a.M) ? ldg16(a.dZ + (long long)p * a.M + co) : make_uint4(0, 0, 0, 0);
+      }
+      transpose8(in, out);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) *reinterpret_cast<uint4*>(sA + chunk_off(cb * 8 + i, pb)) = out[i];
+    }
+    const int nblk = (a.NT >> 3) * 8;
+    for (int q = tid; q < nblk; q += kThreads) {
+      const int nb8 = q >> 3, pb = q & 7;
+      const int n = n0 + nb8 * 8;
+      uint4 in[8], out[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int p = k0 + pb * 8 + j;
+        in[j] = (p < a.K && n < a.N) ? conv_in_chunk(a, p, n) : make_uint4(0, 0, 0, 0);
+      }
+      transpose8(in, out);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) *reinterpret_cast<uint4*>(sB + chunk_off(nb8 * 8 + i, pb)) = out[i];
+    }
+    return;
+  }
+  // GEMM / CONV: A rows are output rows (pixels), 8 K groups of 8 per row
+#pragma unroll
+  for (int it = 0; it < (kBM * 8) / kThreads; ++it) {
+    const int c = it * kThreads + tid;
+    const int r = (c >> 6) * 8 + (c & 7), kc = (c >> 3) & 7;
+    const int m = m0 + r, k = k0 + kc * 8;
+    uint4 v;
+    if (a.mode == 0)
+      v = (m < a.M && k < a.K) ? ldg16(a.A + (long long)m * a.K + k) : make_uint4(0, 0, 0, 0);
+    else
+      v = conv_in_chunk(a, m, k);
+    *reinterpret_cast<uint4*>(sA + chunk_off(r, kc)) = v;
+  }
+  const __nv_bfloat16* Bm = a.mode == 0 ? a.B : a.Wt;
+  for (int c = tid; c < a.NT * 8; c += kThreads) {
+    const int r = (c >> 6) * 8 + (c & 7), kc = (c >> 3) & 7;
+    const int n = n0 + r, k = k0 + kc * 8;
+    const uint4 v = (n < a.N && k < a.K) ? ldg16(Bm + (long long)n * a.K + k) : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(sB + chunk_off(r, kc)) = v;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* sA[2] = {base, base + kATile};
+  unsigned char* sB[2] = {base + 2 * kATile, base + 2 * kATile + kBTileMax};
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * kATile + 2 * kBTileMax);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+  __shared__ int s_fail;
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * a.NT;
+  const uint32_t ncols = a.NT <= 32 ? 32 : a.NT <= 64 ? 64 : a.NT <= 128 ? 128 : 256;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    s_fail = 0;
+    kwtma::fence_barrier_init();
+  }
+  if (warp == 0) tmem_alloc(tslot, ncols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  int kbeg = 0, kend = a.K;
+  if (a.mode == 2) {
+    kbeg = blockIdx.z * a.ksplit;
+    kend = min(a.K, kbeg + a.ksplit);
+  }
+  const int nchunks = (kend - kbeg + kBK - 1) / kBK;
+  const uint32_t idesc = idesc_bf16(kBM, a.NT);
+  bool ok = true;
+  for (int c = 0; c < nchunks && ok; ++c) {
+    const int s = c & 1;
+    if (c >= 2) {
+      if (!mbar_wait(&bar[s], ((c - 2) >> 1) & 1, kWaitNs)) ok = false;
+      if (__syncthreads_or(!ok)) {
+        ok = false;
+        break;
+      }
+    }
+    fill_stage(a, sA[s], sB[s], m0, n0, kbeg + c * kBK);
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t ab = smem_u32(sA[s]), bb = smem_u32(sB[s]);
+#pragma unroll
+      for (int kk = 0; kk < kBK / 16; ++kk)
+        umma_bf16(tmem, smem_desc(ab + kk * 2 * kLBO), smem_desc(bb + kk * 2 * kLBO), idesc, (c | kk) != 0);
+      umma_commit(&bar[s]);
+    }
+  }
+  if (ok && nchunks > 0) {
+    const int L = nchunks - 1;
+    if (!mbar_wait(&bar[L & 1], (L >> 1) & 1, kWaitNs)) ok = false;
+  }
+  if (!ok) s_fail = 1;
+  __syncthreads();
+  tc_fence_after();
+  if (!s_fail && nchunks > 0) {
+    const int r = warp * 32 + (tid & 31);
+    const int m = m0 + r;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int j0 = 0; j0 < a.NT; j0 += 16) {
+      float v[16];
+      tmem_ld16(trow + (uint32_t)j0, v);
+      if (m >= a.M) continue;
+      if (a.mode == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (n0 + j0 + j < a.N) a.C[(long long)m * a.N + n0 + j0 + j] = v[j];
+      } else if (a.mode == 1) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + j0 + j;
+          float y = v[j] + ((a.bias && n < a.N) ? a.bias[n] : 0.f);
+          if (a.relu) y = fmaxf(y, 0.f);
+          v[j] = y;
+        }
+        const long long o = (long long)m * a.N + n0 + j0;
+        if (n0 + j0 + 16 <= a.N) {
+          if (a.Y) {
+            uint32_t w[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+              w[q] = *reinterpret_cast<const uint32_t*>(&h);
+            }
+            *reinterpret_cast<uint4*>(a.Y + o) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4*>(a.Y + o + 8) = make_uint4(w[4], w[5], w[6], w[7]);
+          }
+          if (a.Yf) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              *reinterpret_cast<float4*>(a.Yf + o + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+          }
+        } else {
+          for (int j = 0; j < 16 && n0 + j0 + j < a.N; ++j) {
+            if (a.Y) a.Y[o + j] = __float2bfloat16_rn(v[j]);
+            if (a.Yf) a.Yf[o + j] = v[j];
+          }
+        }
+      } else {
+        // WGRAD: add this pixel range's partial tile
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + j0 + j;
+          if (n < a.N) atomicAdd(a.dW + (long long)m * a.N + n, v[j]);
+        }
+      }
+    }
+  }
+  if (s_fail && tid == 0 && err) atomicCAS(err, 0, kErrUmmaTimeout);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
+// elementwise kernels of the network (bf16 NHWC activations, f32 parameters)
+// ---------------------------------------------------------------------------
+// 2 x 2 average pooling, NHWC.
+__global__ void k_avgpool2(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int nb, int H, int W,
+                           int C) {
+  const int h2 = H / 2, w2 = W / 2;
+  const long long n = (long long)nb * h2 * w2 * C;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    long long q = i / C;
+    const int xo = (int)(q % w2);
+    q /= w2;
+    const int yo = (int)(q % h2);
+    const int b = (int)(q / h2);
+    const long long r0 = (((long long)b * H + 2 * yo) * W + 2 * xo) * C + c;
+    const float s = __bfloat162float(x[r0]) + __bfloat162float(x[r0 + C]) + __bfloat162float(x[r0 + (long long)W * C]) +
+                    __bfloat162float(x[r0 + (long long)W * C + C]);
+    y[i] = __float2bfloat16_rn(0.25f * s);
+  }
+}
+
+// Gradient of 2 x 2 average pooling, added into dx (f32 accumulation buffer or
+// bf16 with add = 0 meaning overwrite).
+__global__ void k_avgpool2_bwd(const __nv_bfloat16* __restrict__ dy, __nv_bfloat16* __restrict__ dx, int nb, int H,
+                               int W, int C, const __nv_bfloat16* __restrict__ add) {
+  const long long n = (long long)nb * H * W * C;
+  const int h2 = H / 2, w2 = W / 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    long long q = i / C;
+    const int x = (int)(q % W);
+    q /= W;
+    const int yy = (int)(q % H);
+    const int b = (int)(q / H);
+    float g = 0.25f * __bfloat162float(dy[(((long long)b * h2 + yy / 2) * w2 + x / 2) * C + c]);
+    if (add) g += __bfloat162float(add[i]);
+    dx[i] = __float2bfloat16_rn(g);
+  }
+}
+
+// dz = dy * (y > 0) (ReLU gradient), all [n] bf16.
+__global__ void k_relu_grad(const __nv_bfloat16* __restrict__ dy, const __nv_bfloat16* __restrict__ y,
+                            __nv_bfloat16* __restrict__ dz, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dz[i] = __bfloat162float(y[i]) > 0.f ? dy[i] : __float2bfloat16_rn(0.f);
+}
+
+// Split the data gradient of a concatenated input [pixels][C1 + C2] into the
+// full-resolution part (added to d1, [pixels][C1]; add1 may be null) and the
+// half-resolution part summed over its 2 x 2 nearest-neighbour children (d2,
+// [pixels/4][C2]).
+__global__ void k_split_concat_grad(const __nv_bfloat16* __restrict__ dcat, int nb, int H, int W, int C1, int C2,
+                                    __nv_bfloat16* __restrict__ d1, const __nv_bfloat16* __restrict__ add1,
+                                    __nv_bfloat16* __restrict__ d2) {
+  const int C = C1 + C2;
+  const long long n1 = (long long)nb * H * W * C1;
+  const int h2 = H / 2, w2 = W / 2;
+  const long long n2 = (long long)nb * h2 * w2 * C2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n1 + n2;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (i < n1) {
+      const long long p = i / C1;
+      const int c = (int)(i % C1);
+      float g = __bfloat162float(dcat[p * C + c]);
+      if (add1) g += __bfloat162float(add1[i]);
+      d1[i] = __float2bfloat16_rn(g);
+    } else {
+      const long long j = i - n1;
+      const int c = (int)(j % C2);
+      long long q = j / C2;
+      const int xo = (int)(q % w2);
+      q /= w2;
+      const int yo = (int)(q % h2);
+      const int b = (int)(q / h2);
+      float g = 0.f;
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+          const long long p = ((long long)b * H + 2 * yo + dy) * W + 2 * xo + dx;
+          g += __bfloat162float(dcat[p * C + C1 + c]);
+        }
+      d2[j] = __float2bfloat16_rn(g);
+    }
+  }
+}
+
+// Flipped, transposed weights for the data gradient: wt[ci][8 - tap][co] = w[co][tap][ci].
+__global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __restrict__ wt, int cout, int cin) {
+  const long long n = (long long)cout * 9 * cin;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int ci = (int)(i % cin);
+    const int tap = (int)((i / cin) % 9);
+    const int co = (int)(i / (9LL * cin));
+    wt[((long long)ci * 9 + (8 - tap)) * cout + co] = w[i];
+  }
+}
+
+// Bias gradient: db[c] += sum over pixels of dz[p][c] (one block per 256 pixels, red.add).
+__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dz, float* __restrict__ db, long long npix, int C) {
+  const long long p0 = (long long)blockIdx.x * 256;
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    float s = 0.f;
+    for (long long p = p0; p < min(npix, p0 + 256); ++p) s += __bfloat162float(dz[p * C + c]);
+    atomicAdd(db + c, s);
+  }
+}
+
+// Loss of the network output in residual form: the estimate is
+// e = out[p][0] + s img[p] (out [pixels][cout] f32, img and target [pixels]
+// f32); *loss += sum (e - target)^2 and dout[p][0] = scale (e - target), the
+// other channels 0 (bf16).
+__global__ void k_mse_grad(const float* __restrict__ out, int cout, const float* __restrict__ img, float s,
+                           const float* __restrict__ target, __nv_bfloat16* __restrict__ dout, long long npix,
+                           float scale, float* loss) {
+  float acc = 0.f;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+    const float d = __fmaf_rn(s, img[p], out[p * cout]) - target[p];
+    acc += d * d;
+    dout[p * cout] = __float2bfloat16_rn(d * scale);
+    for (int c = 1; c < cout; ++c) dout[p * cout + c] = __float2bfloat16_rn(0.f);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc);
+}
+
+// The estimate of the residual form: e[p] = out[p][0] + s img[p].
+__global__ void k_residual_out(const float* __restrict__ out, int cout, const float* __restrict__ img, float s,
+                               float* __restrict__ e, long long npix) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x)
+    e[p] = __fmaf_rn(s, img[p], out[p * cout]);
+}
+
+// Adam step on f32 master parameters, with the bf16 copy the kernels read.
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v, const float* __restrict__ g,
+                       __nv_bfloat16* __restrict__ wb, long long n, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+// f32 image [pixels] -> bf16 NHWC with C channels, the image in channel 0 (scaled).
+__global__ void k_image_to_nhwc(const float* __restrict__ img, __nv_bfloat16* __restrict__ x, long long npix, int C,
+                                float scale) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x)
+    for (int c = 0; c < C; ++c) x[p * C + c] = __float2bfloat16_rn(c == 0 ? img[p] * scale : 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+namespace {
+
+int g_umma_attr_dev = -1;
+
+int umma_fail(int code, const char* msg) { return kw_internal_fail(code, msg); }
+
+int umma_launch(UmmaArgs& a, dim3 grid, cudaStream_t st) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return umma_fail(KW_ERR_CUDA, "cudaGetDevice failed");
+  const int smem = 2 * kATile + 2 * kBTileMax + 64 + 1024;
+  if (g_umma_attr_dev != dev) {
+    if (cudaFuncSetAttribute(k_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return umma_fail(KW_ERR_CUDA, "k_umma: cannot set the shared-memory size");
+    g_umma_attr_dev = dev;
+  }
+  k_umma<<<grid, kThreads, smem, st>>>(a, kw_device_error_ptr());
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "k_umma launch: %s", cudaGetErrorString(e));
+    return umma_fail(KW_ERR_CUDA, buf);
+  }
+  return KW_OK;
+}
+
+int tile_cols(int n) {
+  const int r = (n + 15) / 16 * 16;
+  return r > kMaxNT ? kMaxNT : r;
+}
+
+inline int grid1(long long n) {
+  long long g = (n + 255) / 256;
+  return (int)(g < 1 ? 1 : g > 4096 ? 4096 : g);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t kw_umma_gemm(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, void* stream) {
+  if (!A || !B || !C) return umma_fail(KW_ERR_INVALID, "kw_umma_gemm: null argument");
+  if (M <= 0 || N <= 0 || K <= 0 || K % 8) return umma_fail(KW_ERR_INVALID, "kw_umma_gemm: M, N, K > 0 and K % 8 == 0");
+  UmmaArgs a;
+  memset(&a, 0, sizeof a);
+  a.mode = 0;
+  a.M = M;
+  a.N = N;
+  a.K = K;
+  a.NT = tile_cols(N);
+  a.A = static_cast<const __nv_bfloat16*>(A);
+  a.B = static_cast<const __nv_bfloat16*>(B);
+  a.C = C;
+  return umma_launch(a, dim3((N + a.NT - 1) / a.NT, (M + kBM - 1) / kBM), static_cast<cudaStream_t>(stream));
+}
+
+int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
+                   const void* w, const float* bias, int32_t cout, int32_t relu, void* y, float* yf, void* stream) {
+  if (!x1 || !w || (!y && !yf)) return umma_fail(KW_ERR_INVALID, "kw_conv3x3: null argument");
+  if (c1 <= 0 || c1 % 8 || c2 < 0 || c2 % 8 || (c2 && !x2) || cout <= 0 || cout % 16)
+    return umma_fail(KW_ERR_INVALID, "kw_conv3x3: channels must be multiples of 8 (inputs) and 16 (output)");
+  if (nb <= 0 || H <= 0 || W <= 0 || (c2 && (H % 2 || W % 2)))
+    return umma_fail(KW_ERR_INVALID, "kw_conv3x3: bad geometry");
+  UmmaArgs a;
+  memset(&a, 0, sizeof a);
+  a.mode = 1;
+  a.nb = nb;
+  a.H = H;
+  a.W = W;
+  a.C1 = c1;
+  a.C2 = c2;
+  a.M = nb * H * W;
+  a.N = cout;
+  a.K = 9 * (c1 + c2);
+  a.NT = tile_cols(cout);
+  a.X1 = static_cast<const __nv_bfloat16*>(x1);
+  a.X2 = static_cast<const __nv_bfloat16*>(x2);
+  a.Wt = static_cast<const __nv_bfloat16*>(w);
+  a.bias = bias;
+  a.relu = relu;
+  a.Y = static_cast<__nv_bfloat16*>(y);
+  a.Yf = yf;
+  return umma_launch(a, dim3((cout + a.NT - 1) / a.NT, (a.M + kBM - 1) / kBM), static_cast<cudaStream_t>(stream));
+}
+
+int32_t kw_conv3x3_wgrad(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
+                         const void* dz, int32_t cout, float* dw, void* stream) {
+  if (!x1 || !dz || !dw) return umma_fail(KW_ERR_INVALID, "kw_conv3x3_wgrad: null argument");
+  if (c1 <= 0 || c1 % 8 || c2 < 0 || c2 % 8 || (c2 && !x2) || cout <= 0 || cout % 8)
+    return umma_fail(KW_ERR_INVALID, "kw_conv3x3_wgrad: channels must be multiples of 8");
+  UmmaArgs a;
+  memset(&a, 0, sizeof a);
+  a.mode = 2;
+  a.nb = nb;
+  a.H = H;
+  a.W = W;
+  a.C1 = c1;
+  a.C2 = c2;
+  a.M = cout;
+  a.N = 9 * (c1 + c2);
+  a.K = nb * H * W;
+  a.NT = tile_cols(a.N);
+  a.X1 = static_cast<const __nv_bfloat16*>(x1);
+  a.X2 = static_cast<const __nv_bfloat16*>(x2);
+  a.dZ = static_cast<const __nv_bfloat16*>(dz);
+  a.dW = dw;
+  const int ntile = (a.N + a.NT - 1) / a.NT, mtile = (cout + kBM - 1) / kBM;
+  // split the pixels so that the grid covers the GPU a few times over
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  long long want = 4LL * nsm / (ntile * mtile);
+  if (want < 1) want = 1;
+  long long per = ((long long)a.K + want - 1) / want;
+  per = (per + kBK - 1) / kBK * kBK;
+  if (per < 4 * kBK) per = 4 * kBK;
+  a.ksplit = (int)per;
+  const int nsplit = (int)((a.K + per - 1) / per);
+  return umma_launch(a, dim3(ntile, mtile, nsplit), static_cast<cudaStream_t>(stream));
+}
+
+#define KW_UNET_CK()                                                                 \
+  do {                                                                              \
+    const cudaError_t e_ = cudaGetLastError();                                      \
+    if (e_ != cudaSuccess) return umma_fail(KW_ERR_CUDA, cudaGetErrorString(e_));   \
+  } while (0)
+
+int32_t kw_unet_avgpool2(const void* x, void* y, int32_t nb, int32_t H, int32_t W, int32_t C, void* stream) {
+  if (!x || !y || H % 2 || W % 2) return umma_fail(KW_ERR_INVALID, "kw_unet_avgpool2: bad argument");
+  k_avgpool2<<<grid1((long long)nb * H * W * C / 4), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(x), static_cast<__nv_bfloat16*>(y), nb, H, W, C);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_avgpool2_bwd(const void* dy, void* dx, int32_t nb, int32_t H, int32_t W, int32_t C, const void* add,
+                             void* stream) {
+  if (!dy || !dx || H % 2 || W % 2) return umma_fail(KW_ERR_INVALID, "kw_unet_avgpool2_bwd: bad argument");
+  k_avgpool2_bwd<<<grid1((long long)nb * H * W * C), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(dy), static_cast<__nv_bfloat16*>(dx), nb, H, W, C,
+      static_cast<const __nv_bfloat16*>(add));
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_relu_grad(const void* dy, const void* y, void* dz, int64_t n, void* stream) {
+  if (!dy || !y || !dz) return umma_fail(KW_ERR_INVALID, "kw_unet_relu_grad: null argument");
+  k_relu_grad<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(dy), static_cast<const __nv_bfloat16*>(y), static_cast<__nv_bfloat16*>(dz), n);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_split_concat_grad(const void* dcat, int32_t nb, int32_t H, int32_t W, int32_t C1, int32_t C2, void* d1,
+                                  const void* add1, void* d2, void* stream) {
+  if (!dcat || !d1 || !d2 || H % 2 || W % 2) return umma_fail(KW_ERR_INVALID, "kw_unet_split_concat_grad: bad argument");
+  k_split_concat_grad<<<grid1((long long)nb * H * W * C1 + (long long)nb * H * W * C2 / 4), 256, 0,
+                        static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(dcat), nb, H, W, C1, C2, static_cast<__nv_bfloat16*>(d1),
+      static_cast<const __nv_bfloat16*>(add1), static_cast<__nv_bfloat16*>(d2));
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_flip_weights(const void* w, void* wt, int32_t cout, int32_t cin, void* stream) {
+  if (!w || !wt) return umma_fail(KW_ERR_INVALID, "kw_unet_flip_weights: null argument");
+  k_flip_weights<<<grid1((long long)cout * 9 * cin), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(w), static_cast<__nv_bfloat16*>(wt), cout, cin);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_bias_grad(const void* dz, float* db, int64_t npix, int32_t C, void* stream) {
+  if (!dz || !db) return umma_fail(KW_ERR_INVALID, "kw_unet_bias_grad: null argument");
+  k_bias_grad<<<(int)((npix + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(dz), db, npix, C);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_mse_grad(const float* out, int32_t cout, const float* img, float s, const float* target, void* dout,
+                         int64_t npix, float scale, float* loss, void* stream) {
+  if (!out || !img || !target || !dout || !loss) return umma_fail(KW_ERR_INVALID, "kw_unet_mse_grad: null argument");
+  k_mse_grad<<<grid1(npix), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      out, cout, img, s, target, static_cast<__nv_bfloat16*>(dout), npix, scale, loss);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_residual_out(const float* out, int32_t cout, const float* img, float s, float* e, int64_t npix,
+                             void* stream) {
+  if (!out || !img || !e) return umma_fail(KW_ERR_INVALID, "kw_unet_residual_out: null argument");
+  k_residual_out<<<grid1(npix), 256, 0, static_cast<cudaStream_t>(stream)>>>(out, cout, img, s, e, npix);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_adam(float* w, float* m, float* v, const float* g, void* wb, int64_t n, float lr, float b1, float b2,
+                     float eps, int32_t step, void* stream) {
+  if (!w || !m || !v || !g || step < 1) return umma_fail(KW_ERR_INVALID, "kw_unet_adam: bad argument");
+  const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  k_adam<<<grid1(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(w, m, v, g, static_cast<__nv_bfloat16*>(wb), n, lr, b1,
+                                                                   b2, eps, c1, c2);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+int32_t kw_unet_image_to_nhwc(const float* img, void* x, int64_t npix, int32_t C, float scale, void* stream) {
+  if (!img || !x || C < 1) return umma_fail(KW_ERR_INVALID, "kw_unet_image_to_nhwc: bad argument");
+  k_image_to_nhwc<<<grid1(npix), 256, 0, static_cast<cudaStream_t>(stream)>>>(img, static_cast<__nv_bfloat16*>(x),
+                                                                              npix, C, scale);
+  KW_UNET_CK();
+  return KW_OK;
+}
+
+}  // extern "C"

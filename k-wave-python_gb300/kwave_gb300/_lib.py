@@ -79,6 +79,27 @@ _PROTOS = {
     "kw_plan_run": (C.c_int32, [_P, C.c_int32, _P]),
     "kw_plan_set_graphs": (C.c_int32, [_P, C.c_int32]),
     "kw_plan_adjoint_p0": (C.c_int32, [_P, _P, C.c_int64, _P, _P]),
+    "kw_plan_adjoint": (C.c_int32, [_P, _P, C.c_int64, _P, _P, _P]),
+    "kw_plan_set_checkpoints": (C.c_int32, [_P, C.c_int32]),
+    "kw_plan_update_p0": (C.c_int32, [_P, _P, C.c_int64]),
+    # learned warm start (kw_unet.cu)
+    "kw_umma_gemm": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "kw_conv3x3": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, C.c_int32,
+                               C.c_int32, _P, _P, _P]),
+    "kw_conv3x3_wgrad": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, C.c_int32,
+                                     _P, _P]),
+    "kw_unet_avgpool2": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "kw_unet_avgpool2_bwd": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P]),
+    "kw_unet_relu_grad": (C.c_int32, [_P, _P, _P, C.c_int64, _P]),
+    "kw_unet_split_concat_grad": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P,
+                                              _P]),
+    "kw_unet_flip_weights": (C.c_int32, [_P, _P, C.c_int32, C.c_int32, _P]),
+    "kw_unet_bias_grad": (C.c_int32, [_P, _P, C.c_int64, C.c_int32, _P]),
+    "kw_unet_mse_grad": (C.c_int32, [_P, C.c_int32, _P, C.c_float, _P, _P, C.c_int64, C.c_float, _P, _P]),
+    "kw_unet_residual_out": (C.c_int32, [_P, C.c_int32, _P, C.c_float, _P, C.c_int64, _P]),
+    "kw_unet_adam": (C.c_int32, [_P, _P, _P, _P, _P, C.c_int64, C.c_float, C.c_float, C.c_float, C.c_float,
+                                 C.c_int32, _P]),
+    "kw_unet_image_to_nhwc": (C.c_int32, [_P, _P, C.c_int64, C.c_int32, C.c_float, _P]),
     "kw_plan_autotune": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "kw_batch_create": (C.c_int32, [_P, C.c_int32, C.POINTER(_P)]),
     "kw_batch_run": (C.c_int32, [_P, C.c_int32, _P]),

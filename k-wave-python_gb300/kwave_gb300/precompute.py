@@ -379,6 +379,10 @@ def build_setup(prob, derive_on_device=False) -> Setup:
     c0_32 = f32(c0)
     # c_ref = max(c0) of the FP32-cast medium (kspace_solver.py:228-231)
     c_ref = float(np.float32(c0_32)) if isinstance(c0_32, float) else float(np.max(c0_32))
+    if prob.get("c_ref") is not None:
+        # held fixed by the sound-speed gradient (the reference has no such
+        # input: c_ref is always max(c0)), so that PML and kappa do not move with c0
+        c_ref = float(np.float32(prob["c_ref"]))
     S = Setup(shape=shape, spacing=spacing, dt=dt, Nt=Nt, ndim=ndim, c_ref=c_ref,
               use_sg=bool(prob.get("use_sg", True)), use_kspace=bool(prob.get("use_kspace", True)))
     S.fields["c0"] = c0_32

@@ -162,6 +162,28 @@ class DevicePlan:
         K.check(self.lib.kw_plan_adjoint_p0(self._h, K.ptr(r), r.size, K.ptr(g), st))
         return g
 
+    def update_p0(self, p0):
+        """New initial pressure for this plan (kw_plan_update_p0); rewinds to t = 0."""
+        a = np.ascontiguousarray(p0, dtype=np.float32).ravel()
+        K.check(self.lib.kw_plan_update_p0(self._h, K.ptr(a), a.size))
+        STATS["h2d_bytes"] += a.nbytes
+
+    def set_checkpoints(self, interval):
+        """Keep the carried state every ``interval`` steps of the coming
+        forward run (kw_plan_set_checkpoints); 0 turns them off."""
+        K.check(self.lib.kw_plan_set_checkpoints(self._h, int(interval)))
+
+    def adjoint(self, residual, grad_c=False):
+        """kw_plan_adjoint: (gradient w.r.t. p0, gradient w.r.t. c0 or None) of
+        sum(residual * recorded slot values).  ``grad_c`` needs this plan's
+        forward run to Nt with p0 set and checkpoints on.  The plan is reset."""
+        r = np.ascontiguousarray(residual, dtype=np.float32)
+        g = np.empty(self.S.shape, np.float32)
+        gc = np.empty(self.S.shape, np.float32) if grad_c else None
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        K.check(self.lib.kw_plan_adjoint(self._h, K.ptr(r), r.size, K.ptr(g), K.ptr(gc) if grad_c else None, st))
+        return g, gc
+
     def set_graphs(self, enable):
         """Run repeated steps as replayed CUDA graphs (default) or as plain launches."""
         K.check(self.lib.kw_plan_set_graphs(self._h, int(bool(enable))))

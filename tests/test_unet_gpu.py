@@ -1,0 +1,146 @@
+"""The learned warm start's network as a whole: forward and parameter
+gradients against the same network in plain PyTorch FP32 on the CPU, a
+training run that lowers the loss, and the trained network beating the
+time-reversal image it starts from on held-out pairs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300 import _lib
+
+    _lib.require_device()
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def torch_reference(net, images, targets):
+    """The network of kwave_gb300.warmstart in torch.nn.functional (NCHW,
+    FP32, weights rounded to bf16 as the kernels read them); returns the
+    estimate, the loss and the gradients of every parameter."""
+    import torch
+    import torch.nn.functional as F
+
+    from kwave_gb300.warmstart import LAYERS
+
+    W, B = {}, {}
+    for name, c1, c2, co, _ in LAYERS:
+        w = net.p[name]["w"].detach().cpu().to(torch.bfloat16).float()
+        W[name] = w.reshape(co, 3, 3, c1 + c2).permute(0, 3, 1, 2).contiguous().requires_grad_(True)
+        B[name] = net.p[name]["b"].detach().cpu().clone().requires_grad_(True)
+    img = torch.as_tensor(images).float()
+    x = torch.zeros((img.shape[0], 8, img.shape[1], img.shape[2]))
+    x[:, 0] = (img * net.in_scale).to(torch.bfloat16).float()
+
+    def conv(name, a, b=None, relu=True):
+        if b is not None:
+            a = torch.cat([a, F.interpolate(b, scale_factor=2, mode="nearest")], 1)
+        y = F.conv2d(a, W[name], B[name], padding=1)
+        return torch.relu(y) if relu else y
+
+    e1 = conv("e1b", conv("e1a", x))
+    e2 = conv("e2b", conv("e2a", F.avg_pool2d(e1, 2)))
+    e3 = conv("e3b", conv("e3a", F.avg_pool2d(e2, 2)))
+    b = conv("bb", conv("ba", F.avg_pool2d(e3, 2)))
+    d3 = conv("d3b", conv("d3a", e3, b))
+    d2 = conv("d2b", conv("d2a", e2, d3))
+    d1 = conv("d1b", conv("d1a", e1, d2))
+    out = conv("out", d1, relu=False)
+    est = out[:, 0] + net.in_scale * img
+    loss = ((est - torch.as_tensor(targets).float()) ** 2).mean()
+    loss.backward()
+    grads = {}
+    for name, c1, c2, co, _ in LAYERS:
+        grads[name] = (W[name].grad.permute(0, 2, 3, 1).reshape(co, 9, c1 + c2).numpy(), B[name].grad.numpy())
+    return est.detach().numpy(), float(loss), grads
+
+
+def smooth_images(nb, n, seed):
+    rng = np.random.default_rng(seed)
+    g = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    out = np.zeros((nb, n, n))
+    for i in range(nb):
+        for _ in range(4):
+            cx, cy, s = rng.uniform(4, n - 4), rng.uniform(4, n - 4), rng.uniform(1.5, 4)
+            out[i] += rng.uniform(0.5, 2) * np.exp(-((g[0] - cx) ** 2 + (g[1] - cy) ** 2) / (2 * s * s))
+    return out.astype(np.float32)
+
+
+def test_network_forward_and_gradients_match_torch():
+    """Whole-network estimate and every parameter gradient against torch
+    autograd.  The kernels store activations and gradients in bf16 between
+    layers (the reference keeps FP32), which sets the tolerances: 1e-2 for
+    the estimate, 5e-2 for the gradients; the per-operation tests pin each
+    kernel at 1e-5."""
+    import torch
+
+    from kwave_gb300.warmstart import LAYERS, UNet
+
+    net = UNet(seed=3, in_scale=0.8)
+    for name, *_ in LAYERS:  # a non-trivial output layer, so that every gradient is exercised
+        net.p[name]["w"].mul_(1.0 if name != "out" else 30.0)
+        net.p[name]["b"].normal_(0.0, 0.05)
+        net.wb[name] = net.p[name]["w"].to(torch.bfloat16).contiguous()
+    imgs = smooth_images(2, 32, 1)
+    tgts = 1.5 * smooth_images(2, 32, 2)
+    est_ref, loss_ref, g_ref = torch_reference(net, imgs, tgts)
+    x = torch.as_tensor(imgs, device="cuda")
+    y = torch.as_tensor(tgts, device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    net.loss_and_grad(x, y, loss)
+    est = net.forward(x).cpu().numpy()
+    torch.cuda.synchronize()
+    e_est = rel(est, est_ref)
+    e_loss = abs(float(loss) / imgs.size - loss_ref) / loss_ref
+    print(f"estimate {e_est:.2e}, loss {e_loss:.2e}")
+    assert e_est <= 1e-2 and e_loss <= 1e-2
+    worst = 0.0
+    for name, *_ in LAYERS:
+        gw = net.state[name]["w"]["g"].cpu().numpy()
+        gb = net.state[name]["b"]["g"].cpu().numpy()
+        ew, eb = rel(gw, g_ref[name][0]), rel(gb, g_ref[name][1])
+        print(f"{name}: weight grad {ew:.2e}, bias grad {eb:.2e}")
+        worst = max(worst, ew, eb)
+    assert worst <= 5e-2, worst
+
+
+def test_training_lowers_the_loss():
+    """Adam steps on a fixed smooth-image-to-target map bring the loss down."""
+    from kwave_gb300.warmstart import UNet
+
+    imgs = smooth_images(64, 32, 5)
+    tgts = np.maximum(1.3 * imgs - 0.3, 0).astype(np.float32)
+    net = UNet(seed=1, in_scale=1.0)
+    hist = net.train(imgs, tgts, epochs=6, batch=8, lr=2e-3)
+    print("loss per epoch", hist)
+    assert hist[-1] < 0.5 * hist[0], hist
+
+
+def test_trained_network_beats_time_reversal():
+    """Training pairs from the device forward solver and time reversal
+    (vessel phantoms, 128^2, 64-point circle, 400 steps, 1 % noise): after
+    training on 384 pairs, the network's estimate is closer to the held-out
+    phantoms than the time-reversal image scaled by its least-squares factor."""
+    from kwave_gb300.warmstart import UNet, fit_input_scale, generate_pairs
+
+    kw = dict(n=128, nt=400, n_sensor=64, radius=2.4e-3)
+    imgs, p0s = generate_pairs(384, seed0=10, batch=128, **kw)
+    timgs, tp0s = generate_pairs(16, seed0=5000, batch=16, **kw)
+    s = fit_input_scale(imgs, p0s)
+    net = UNet(seed=0, in_scale=s)
+    hist = net.train(imgs, p0s, epochs=12, batch=16, lr=1e-3)
+    est = net.predict(timgs)
+    e_net = np.mean([rel(e, t) for e, t in zip(est, tp0s)])
+    e_tr = np.mean([rel(s * i, t) for i, t in zip(timgs, tp0s)])
+    print(f"held-out relative p0 error: network {e_net:.3f}, scaled time reversal {e_tr:.3f}; losses {hist}")
+    assert e_net < e_tr
