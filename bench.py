@@ -713,6 +713,176 @@ def run_adjoint(args):
     return 0
 
 
+WARMSTART_WORKLOAD = ("learned warm start: 4-level U-Net, 32 base channels, BF16 on tcgen05, trained on pairs (time-"
+                      "reversal image, p0) from the device forward solver at 256^2 (vessel phantoms, 128-point circle "
+                      "r=5 mm on the grid, 800 steps, 1 % noise); held-out problems refined by CGLS from the network's "
+                      "estimate vs CGLS from zero")
+
+
+def run_warmstart(args):
+    """Learned warm start against plain adjoint iterations.  Generates the
+    training pairs with the device solver (batched forward runs and batched
+    time-reversal runs), trains the U-Net with the library's tcgen05 kernels,
+    then on held-out problems runs CGLS from zero and CGLS from the network's
+    estimate (inference time included) and reports the relative p0 error
+    after each iteration, the time to 1 % and the time to reach the error
+    that plain CGLS ends at."""
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300.warmstart import UNet, fit_input_scale, generate_pairs, noisy, pair_problem, refine, time_to
+
+    npairs, epochs, iters, ntest = args.pairs, args.epochs, args.iterations, args.test_problems
+    t0 = time.perf_counter()
+    imgs, p0s = generate_pairs(npairs, seed0=1000, batch=256)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    s = fit_input_scale(imgs[: min(npairs, 512)], p0s[: min(npairs, 512)])
+    net = UNet(seed=0, in_scale=s)
+    t0 = time.perf_counter()
+    hist = net.train(imgs, p0s, epochs=epochs, batch=16, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del imgs, p0s
+    cells = 256 * 256
+    results = []
+    for j in range(ntest):
+        prob = pair_problem(90000 + j)
+        from kwave_gb300.adjoint import forward_p0
+
+        d_obs = noisy(forward_p0(prob, prob["p0"]).astype(np.float64), np.random.default_rng(90000 + j))
+        # plain: CGLS from zero
+        _, h0, st0 = refine(prob, d_obs, np.zeros(prob["shape"]), iters, p_true=prob["p0"])
+        # learned: time reversal + network + CGLS from its estimate
+        torch.cuda.synchronize()
+        tl = time.perf_counter()
+        from kwave_gb300.warmstart import time_reversal_images
+
+        img = time_reversal_images([prob], [d_obs])[0].astype(np.float32)
+        est = net.predict(img[None])[0]
+        torch.cuda.synchronize()
+        t_net = time.perf_counter() - tl
+        e_net = float(np.linalg.norm(est - prob["p0"]) / np.linalg.norm(prob["p0"]))
+        _, h1, st1 = refine(prob, d_obs, est.astype(np.float64), iters, p_true=prob["p0"])
+        e0 = [h[1] for h in h0]
+        e1 = [h[1] for h in h1]
+        target = min(e0)
+        results.append({"plain_errors": e0, "learned_errors": e1, "network_error": e_net,
+                        "tr_plus_network_seconds": t_net, "plain_seconds": st0[-1], "learned_seconds": t_net + st1[-1],
+                        "plain_to_1pct": time_to(e0, st0, 0.01), "learned_to_1pct": time_to(e1, st1, 0.01, t_net),
+                        "plain_to_plain_best": time_to(e0, st0, target),
+                        "learned_to_plain_best": (t_net if e_net <= target else time_to(e1, st1, target, t_net))})
+    ratios = [r["plain_to_plain_best"] / r["learned_to_plain_best"] for r in results
+              if r["learned_to_plain_best"] is not None and r["plain_to_plain_best"] is not None]
+    line = {"metric": METRIC, "impl": "gb300", "workload": "warmstart", "value": float(np.median(ratios)) if ratios else None,
+            "unit": "x (time for plain CGLS to reach its own best p0 error / time for learned+CGLS to reach it)",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 network, f32 solver",
+            "data": "synthetic vessel phantoms", "config": {"workload": WARMSTART_WORKLOAD, "pairs": npairs,
+                                                            "epochs": epochs, "cgls_iterations": iters,
+                                                            "test_problems": ntest},
+            "generation_seconds": t_gen, "training_seconds": t_train, "train_loss_per_epoch": hist,
+            "median_network_error": float(np.median([r["network_error"] for r in results])),
+            "median_plain_final_error": float(np.median([r["plain_errors"][-1] for r in results])),
+            "median_learned_final_error": float(np.median([r["learned_errors"][-1] for r in results])),
+            "time_to_1pct": {"plain": [r["plain_to_1pct"] for r in results],
+                             "learned": [r["learned_to_1pct"] for r in results]},
+            "per_problem": results, "cell_steps_per_pass": cells * 800}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+UNET_WORKLOAD = ("U-Net training step of the learned warm start: batch 16 of 256^2 images, 4 levels, 32 base "
+                 "channels, BF16 activations and weights, FP32 accumulation on tcgen05; forward, data and weight "
+                 "gradients, Adam")
+
+
+def unet_step_flops(nb=16, n=256):
+    """Algorithmic flops of one training step: 2 M N K per convolution for the
+    forward pass, the data gradient (all layers but the first) and the weight
+    gradient, M = pixels, N = output channels, K = 9 x input channels."""
+    from kwave_gb300.warmstart import LAYERS
+
+    res = {"e1": n, "e2": n // 2, "e3": n // 4, "ba": n // 8, "bb": n // 8, "d3": n // 4, "d2": n // 2, "d1": n,
+           "ou": n}
+    tot = 0.0
+    for name, c1, c2, co, _ in LAYERS:
+        h = res[name[:2]]
+        f = 2.0 * nb * h * h * co * 9 * (c1 + c2)
+        tot += f * (3 if name != "e1a" else 2)
+    return tot
+
+
+def run_unet(args):
+    """Throughput of the U-Net training step on the tensor cores: ``value`` =
+    images per second; the roofline is the convolution flops of a step over
+    its device time against the measured bf16 tensor peak, and the dominant
+    kernel (the tcgen05 convolution, ``k_umma``) is timed alone on the
+    largest layer for its own fraction."""
+    import torch
+
+    import __graft_entry__ as g
+
+    g.build()
+    from kwave_gb300 import unet_ops as U
+    from kwave_gb300.warmstart import UNet
+
+    nb, n = 16, 256
+    rng = np.random.default_rng(0)
+    imgs = torch.as_tensor(rng.random((nb, n, n), dtype=np.float32), device="cuda")
+    tgts = torch.as_tensor(rng.random((nb, n, n), dtype=np.float32), device="cuda")
+    net = UNet(seed=0, in_scale=1.0)
+    loss = torch.zeros(1, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, args.warmup)):
+        net.loss_and_grad(imgs, tgts, loss)
+        net.adam_step(1e-4)
+    torch.cuda.synchronize()
+    K_steps = args.steps if args.steps < 1000 else 20
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record(stream)
+        for _ in range(K_steps):
+            net.loss_and_grad(imgs, tgts, loss)
+            net.adam_step(1e-4)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / K_steps
+    flops = unet_step_flops(nb, n)
+    # the dominant kernel alone: the 32 -> 32 convolution at 256^2 (batch 16)
+    x = torch.randn((nb, n, n, 32), device="cuda").to(torch.bfloat16)
+    w = (0.1 * torch.randn((32, 9, 32), device="cuda")).to(torch.bfloat16)
+    y = torch.empty((nb, n, n, 32), dtype=torch.bfloat16, device="cuda")
+    for _ in range(3):
+        U.conv3x3(x, w, None, relu=True, y=y)
+    torch.cuda.synchronize()
+    reps = 20
+    ev0.record(stream)
+    for _ in range(reps):
+        U.conv3x3(x, w, None, relu=True, y=y)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    kms = ev0.elapsed_time(ev1) / reps
+    kflops = 2.0 * nb * n * n * 32 * 9 * 32
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    step_tf = flops / (ms / 1e3) / 1e12
+    k_tf = kflops / (kms / 1e3) / 1e12
+    line = {"metric": METRIC, "impl": "gb300", "workload": "unet", "value": nb / (ms / 1e3), "unit": "images/s",
+            "n_gpus": 1, "steps": K_steps, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (f32 accumulation)", "data": "random images",
+            "config": {"workload": UNET_WORKLOAD, "batch": nb, "image": n},
+            "step_roofline": {"bound": "tensor", "flops_per_step": flops, "achieved": step_tf, "peak": peak,
+                              "unit": "TFLOP/s", "frac": step_tf / peak, "peak_source": "measured" if peaks else "fallback"},
+            "roofline": {"bound": "tensor", "kernel": "k_umma (conv3x3 32->32, 16 x 256^2)", "achieved": k_tf,
+                         "peak": peak, "unit": "TFLOP/s", "frac": k_tf / peak, "traffic": None,
+                         "kernel_ms": kms},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 import ctypes  # noqa: E402
 
 C_int64 = ctypes.c_int64
@@ -728,7 +898,11 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the comparison with the 256^3 golden")
-    ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit", "adjoint"],
+    ap.add_argument("--pairs", type=int, default=10000, help="warmstart workload: training pairs")
+    ap.add_argument("--epochs", type=int, default=6, help="warmstart workload: training epochs")
+    ap.add_argument("--iterations", type=int, default=20, help="warmstart workload: CGLS iterations per problem")
+    ap.add_argument("--test-problems", type=int, default=4, help="warmstart workload: held-out problems")
+    ap.add_argument("--workload", default="ivp3d", choices=["ivp3d", "transmit", "adjoint", "warmstart", "unet"],
                     help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events; "
                          "adjoint: p0 reconstruction by adjoint iterations at 512^2")
     ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
@@ -743,6 +917,10 @@ def main(argv=None):
         return run_transmit(args)
     if args.workload == "adjoint":
         return run_adjoint(args)
+    if args.workload == "warmstart":
+        return run_warmstart(args)
+    if args.workload == "unet":
+        return run_unet(args)
     return run_gb300(args)
 
 

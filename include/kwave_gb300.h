@@ -195,6 +195,15 @@ int32_t kw_plan_set_checkpoints(kw_plan* plan, int32_t interval);
  * does not depend on the interval: the regenerated steps are the forward's
  * own steps, bit for bit.  The plan is reset (t = 0) afterwards. */
 int32_t kw_plan_adjoint(kw_plan* plan, const float* residual, int64_t n, float* grad_p0, float* grad_c, void* stream);
+/* Failure-detection test of the bounded device waits (off by default; no
+ * counterpart in the reference).  While enabled, the velocity stage's bulk-fed
+ * row kernel withholds, in its first CTA, the first copy its consumers wait
+ * for, and its waits give up after 20 ms instead of 2 s: the consumers time
+ * out, leave together, and the next kw_plan_sync returns KW_ERR_CUDA with the
+ * timeout message.  Nothing faults and no wait is unbounded; the plan's
+ * results are invalid until it is reset.  Needs a power-of-two last axis of
+ * 128 to 2048 points (the bulk-fed row stages). */
+int32_t kw_plan_set_wait_test(kw_plan* plan, int32_t enable);
 /* enable == 0: every step as plain launches (default 1; the environment
  * variable KWAVE_GB300_GRAPHS=0 sets 0 at kw_plan_finalize). */
 int32_t kw_plan_set_graphs(kw_plan* plan, int32_t enable);
@@ -284,8 +293,8 @@ int32_t kw_umma_gemm(const void* A, const void* B, float* C, int32_t M, int32_t 
 /* 3x3 convolution, stride 1, zero padding: y[p][co] = act(bias[co] + sum over
  * taps and input channels of w[co][tap][ci] x[p + tap][ci]), where the input is
  * x1 (nb, H, W, c1) followed along channels by x2 (nb, H/2, W/2, c2) read with
- * nearest-neighbour upsampling (c2 = 0: x1 alone).  c1, c2 multiples of 8,
- * cout a multiple of 16; act = ReLU when relu != 0.  Output to y (bf16) and/or
+ * nearest-neighbour upsampling (c2 = 0: x1 alone).  c1, c2 and cout
+ * multiples of 8; act = ReLU when relu != 0.  Output to y (bf16) and/or
  * yf (f32), (nb, H, W, cout).  With the output gradient as x1 and the weights
  * from kw_unet_flip_weights it is the data gradient. */
 int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,

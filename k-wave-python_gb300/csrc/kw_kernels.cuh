@@ -100,6 +100,11 @@ struct RowsParams {
   // the c^2 gradient, turned into the c gradient by ST_ADJ_E (nullptr: off)
   const float* fsum;
   float* gacc;
+  // failure-detection test (kw_plan_set_wait_test): the bulk-fed row stage's
+  // CTA 0 withholds its first copy, and its bounded waits give up after
+  // wait_ns (0: the normal limit), so that the timeout path runs
+  int withhold;
+  unsigned long long wait_ns;
 };
 
 // step index and record column of a row-stage launch

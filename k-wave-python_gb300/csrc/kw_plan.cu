@@ -152,6 +152,8 @@ struct kw_plan {
   int ckpt_K = 0;
   std::vector<float*> ckpt;
   std::vector<char> ckpt_ok;
+  // failure-detection test of the bounded waits (kw_plan_set_wait_test)
+  int wait_test = 0;
   // set by kw_plan_adjoint around its ST_ADJ_A / ST_ADJ_E launches
   const float* adj_fsum = nullptr;
   float* adj_gacc = nullptr;
@@ -860,8 +862,13 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
                                           (dsm ? (size_t)128 * p->rows_regE : 0));
     const int grid = (p->nrows + p->rows_R - 1) / p->rows_R;
     const bool extra = P.srcp_on || P.srcu_on[0] || P.srcu_on[1] || P.srcu_on[2] || P.rec_us;
-    if (stage == ST_U && !init && !extra && p->rows_tma)
+    if (stage == ST_U && !init && !extra && p->rows_tma) {
+      if (p->wait_test) {
+        P.withhold = 1;
+        P.wait_ns = 20000000ull;  // 20 ms
+      }
       CK(kw_rows_tma_launch(p->Mfft, ST_U, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
+    }
     else if (stage == ST_RHO && dsm && !extra && p->rows_tma)
       CK(kw_rows_tma_launch(p->Mfft, ST_RHO_PL, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
     else if (stage == ST_EOS && p->rows_tma)
@@ -1513,6 +1520,17 @@ int32_t kw_plan_adjoint(kw_plan* p, const float* residual, int64_t n, float* gra
 
 int32_t kw_plan_adjoint_p0(kw_plan* p, const float* residual, int64_t n, float* grad, void* stream) {
   return kw_plan_adjoint(p, residual, n, grad, nullptr, stream);
+}
+
+int32_t kw_plan_set_wait_test(kw_plan* p, int32_t enable) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_set_wait_test before kw_plan_finalize");
+  if (enable && !p->rows_tma)
+    return fail(KW_ERR_UNSUPPORTED, "the wait test needs the bulk-fed row stages (a power-of-two last axis)");
+  CK(cudaDeviceSynchronize());
+  p->wait_test = enable != 0;
+  drop_graphs(p);  // captured steps hold the launch parameters
+  return KW_OK;
 }
 
 int32_t kw_plan_set_graphs(kw_plan* p, int32_t enable) {

@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
 
   const int nblk = (Q.nrows + R - 1) / R;
   const int nload = row_nloads<STAGE>(Q);
+  const uint64_t wait_ns = Q.wait_ns ? Q.wait_ns : kRowWaitNs;
 
   if (warp == CT / 32) {
     // ---------------- producer ----------------
@@ -154,7 +155,12 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
           const void* base = row_load<STAGE>(Q, idx, spec);
           if (!base) continue;
           const uint32_t s = it % NST, k = it / NST;
-          if (k > 0 && !kwtma::mbar_wait(&empty[s], (k - 1) & 1, kRowWaitNs)) {
+          if (Q.withhold && blockIdx.x == 0) {
+            // failure-detection test: no copy is issued, the consumers' wait for it runs out
+            ok = false;
+            break;
+          }
+          if (k > 0 && !kwtma::mbar_wait(&empty[s], (k - 1) & 1, wait_ns)) {
             atomicExch(err, 3);
             ok = false;
             break;
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
     // wait for item `i` (bounded; all consumers agree on a timeout)
     auto wait_item = [&](uint32_t i) -> const float2* {
       const uint32_t s = i % NST;
-      const bool got = kwtma::mbar_wait(&full[s], (i / NST) & 1, kRowWaitNs);
+      const bool got = kwtma::mbar_wait(&full[s], (i / NST) & 1, wait_ns);
       if (consumers_any_rows(!got, CT)) {
         if (tid == 0) atomicExch(err, 4);
         aborted = true;
@@ -406,7 +412,7 @@ __global__ void __launch_bounds__(160, row_ctas(STAGE)) k_rows_tma(const __grid_
   if (tid == 0) {
     for (int i = counters[1]; i < counters[0]; ++i) {
       const uint32_t s = (uint32_t)i % NST, k = (uint32_t)i / NST;
-      if (!kwtma::mbar_wait(&full[s], k & 1, kRowWaitNs)) break;
+      if (!kwtma::mbar_wait(&full[s], k & 1, wait_ns)) break;
     }
   }
 }

@@ -579,8 +579,8 @@ int32_t kw_umma_gemm(const void* A, const void* B, float* C, int32_t M, int32_t 
 int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
                    const void* w, const float* bias, int32_t cout, int32_t relu, void* y, float* yf, void* stream) {
   if (!x1 || !w || (!y && !yf)) return umma_fail(KW_ERR_INVALID, "kw_conv3x3: null argument");
-  if (c1 <= 0 || c1 % 8 || c2 < 0 || c2 % 8 || (c2 && !x2) || cout <= 0 || cout % 16)
-    return umma_fail(KW_ERR_INVALID, "kw_conv3x3: channels must be multiples of 8 (inputs) and 16 (output)");
+  if (c1 <= 0 || c1 % 8 || c2 < 0 || c2 % 8 || (c2 && !x2) || cout <= 0 || cout % 8)
+    return umma_fail(KW_ERR_INVALID, "kw_conv3x3: channel counts must be multiples of 8");
   if (nb <= 0 || H <= 0 || W <= 0 || (c2 && (H % 2 || W % 2)))
     return umma_fail(KW_ERR_INVALID, "kw_conv3x3: bad geometry");
   UmmaArgs a;

@@ -24,14 +24,46 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def _rounders():
+    """Autograd functions that round to bf16 where the kernels store bf16:
+    R rounds the values in both directions (an activation written in bf16 and
+    the gradient that arrives at it, also written in bf16), G only the
+    gradient (the f32 output layer, whose gradient is written in bf16)."""
+    import torch
+
+    class R(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x):
+            return x.to(torch.bfloat16).float()
+
+        @staticmethod
+        def backward(ctx, g):
+            return g.to(torch.bfloat16).float()
+
+    class G(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x):
+            return x.clone()
+
+        @staticmethod
+        def backward(ctx, g):
+            return g.to(torch.bfloat16).float()
+
+    return R.apply, G.apply
+
+
 def torch_reference(net, images, targets):
     """The network of kwave_gb300.warmstart in torch.nn.functional (NCHW,
-    FP32, weights rounded to bf16 as the kernels read them); returns the
-    estimate, the loss and the gradients of every parameter."""
+    FP32 arithmetic, weights rounded to bf16 as the kernels read them, and
+    activations and their gradients rounded to bf16 at the points where the
+    kernels store them); returns the estimate, the loss and the gradients of
+    every parameter."""
     import torch
     import torch.nn.functional as F
 
     from kwave_gb300.warmstart import LAYERS
+
+    R, G = _rounders()
 
     W, B = {}, {}
     for name, c1, c2, co, _ in LAYERS:
@@ -45,13 +77,16 @@ def torch_reference(net, images, targets):
     def conv(name, a, b=None, relu=True):
         if b is not None:
             a = torch.cat([a, F.interpolate(b, scale_factor=2, mode="nearest")], 1)
-        y = F.conv2d(a, W[name], B[name], padding=1)
-        return torch.relu(y) if relu else y
+        y = F.conv2d(R(a), W[name], B[name], padding=1)
+        return R(torch.relu(y)) if relu else G(y)
+
+    def pool(a):
+        return R(F.avg_pool2d(a, 2))
 
     e1 = conv("e1b", conv("e1a", x))
-    e2 = conv("e2b", conv("e2a", F.avg_pool2d(e1, 2)))
-    e3 = conv("e3b", conv("e3a", F.avg_pool2d(e2, 2)))
-    b = conv("bb", conv("ba", F.avg_pool2d(e3, 2)))
+    e2 = conv("e2b", conv("e2a", pool(e1)))
+    e3 = conv("e3b", conv("e3a", pool(e2)))
+    b = conv("bb", conv("ba", pool(e3)))
     d3 = conv("d3b", conv("d3a", e3, b))
     d2 = conv("d2b", conv("d2a", e2, d3))
     d1 = conv("d1b", conv("d1a", e1, d2))
@@ -62,7 +97,7 @@ def torch_reference(net, images, targets):
     grads = {}
     for name, c1, c2, co, _ in LAYERS:
         grads[name] = (W[name].grad.permute(0, 2, 3, 1).reshape(co, 9, c1 + c2).numpy(), B[name].grad.numpy())
-    return est.detach().numpy(), float(loss), grads
+    return est.detach().numpy(), float(loss.detach()), grads
 
 
 def smooth_images(nb, n, seed):
@@ -78,10 +113,11 @@ def smooth_images(nb, n, seed):
 
 def test_network_forward_and_gradients_match_torch():
     """Whole-network estimate and every parameter gradient against torch
-    autograd.  The kernels store activations and gradients in bf16 between
-    layers (the reference keeps FP32), which sets the tolerances: 1e-2 for
-    the estimate, 5e-2 for the gradients; the per-operation tests pin each
-    kernel at 1e-5."""
+    autograd, the reference rounding activations and gradients to bf16 where
+    the kernels store them; what remains is FP32 summation order and the odd
+    rounding-boundary flip it causes: 1e-2 relative L2 for the estimate, the
+    loss and every gradient (the per-operation tests pin each kernel at
+    1e-5)."""
     import torch
 
     from kwave_gb300.warmstart import LAYERS, UNet
@@ -111,7 +147,7 @@ def test_network_forward_and_gradients_match_torch():
         ew, eb = rel(gw, g_ref[name][0]), rel(gb, g_ref[name][1])
         print(f"{name}: weight grad {ew:.2e}, bias grad {eb:.2e}")
         worst = max(worst, ew, eb)
-    assert worst <= 5e-2, worst
+    assert worst <= 1e-2, worst
 
 
 def test_training_lowers_the_loss():
