@@ -145,6 +145,12 @@ int32_t kw_plan_derive_medium(kw_plan* plan, int32_t what, const float* alpha, i
  * means a new Simulation; iterative reconstructions run many forward passes
  * that differ only in p0. */
 int32_t kw_plan_update_p0(kw_plan* plan, const float* host, int64_t n);
+/* Replaces the signal of a source slot of a finalized plan (same shape as
+ * given to kw_plan_set_source, already scaled the same way); the mask and
+ * mode stay.  Call kw_plan_reset before running from t = 0 again.  No
+ * counterpart in the reference (a new Simulation per signal there); used to
+ * run many time-reversal passes on one plan. */
+int32_t kw_plan_update_source(kw_plan* plan, int32_t slot, const float* signal, int32_t n_rows, int32_t length);
 /* Allocates device memory, uploads all inputs and resets the state to t = 0. */
 int32_t kw_plan_finalize(kw_plan* plan);
 /* Advances min(nsteps, Nt - t) steps of Simulation.step (kspace_solver.py:691-747)

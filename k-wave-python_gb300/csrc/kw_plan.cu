@@ -331,6 +331,24 @@ int32_t kw_plan_update_p0(kw_plan* p, const float* host, int64_t n) {
   return kw_plan_reset(p);
 }
 
+int32_t kw_plan_update_source(kw_plan* p, int32_t slot, const float* signal, int32_t n_rows, int32_t length) {
+  if (!p || !signal) return fail(KW_ERR_INVALID, "kw_plan_update_source: null argument");
+  if (!p->finalized) return fail(KW_ERR_STATE, "kw_plan_update_source before kw_plan_finalize");
+  if (slot < 0 || slot > KW_S_U2 || !p->hsrc[slot].set || !p->src[slot].sig)
+    return fail(KW_ERR_STATE, "kw_plan_update_source: source slot %d was not set before kw_plan_finalize", slot);
+  HostSrc& h = p->hsrc[slot];
+  if (n_rows != h.nrows || length != h.len)
+    return fail(KW_ERR_INVALID, "kw_plan_update_source: signal is (%d, %d), the slot holds (%d, %d)", n_rows, length,
+                h.nrows, h.len);
+  CK(cudaDeviceSynchronize());
+  h.sig.assign(signal, signal + (size_t)n_rows * length);
+  std::vector<float> tm((size_t)length * n_rows);
+  for (int r = 0; r < n_rows; ++r)
+    for (int t = 0; t < length; ++t) tm[(size_t)t * n_rows + r] = signal[(size_t)r * length + t];
+  CK(cudaMemcpy(const_cast<float*>(p->src[slot].sig), tm.data(), tm.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return KW_OK;
+}
+
 int32_t kw_plan_derive_medium(kw_plan* p, int32_t what, const float* alpha, int64_t n, double alpha_s, double alpha_power,
                               int32_t absorb_mode) {
   if (!p) return fail(KW_ERR_INVALID, "null plan");

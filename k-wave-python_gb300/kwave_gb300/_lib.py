@@ -82,6 +82,7 @@ _PROTOS = {
     "kw_plan_adjoint": (C.c_int32, [_P, _P, C.c_int64, _P, _P, _P]),
     "kw_plan_set_checkpoints": (C.c_int32, [_P, C.c_int32]),
     "kw_plan_update_p0": (C.c_int32, [_P, _P, C.c_int64]),
+    "kw_plan_update_source": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, C.c_int32]),
     "kw_plan_set_wait_test": (C.c_int32, [_P, C.c_int32]),
     # learned warm start (kw_unet.cu)
     "kw_umma_gemm": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, _P]),

@@ -506,6 +506,7 @@ def build_setup(prob, derive_on_device=False) -> Setup:
 
     # --- sources (kspace_solver.py:552-645) ---
     S.sources = _build_sources(prob, shape, spacing, dt, c0, ndim)
+    S.source_c0 = c0  # the sound speed the source scalings use (for later signal updates)
 
     # --- p0 (kspace_solver.py:679-689) ---
     p0r = prob.get("p0", 0)

@@ -168,6 +168,19 @@ class DevicePlan:
         K.check(self.lib.kw_plan_update_p0(self._h, K.ptr(a), a.size))
         STATS["h2d_bytes"] += a.nbytes
 
+    def update_sources(self, prob):
+        """New source signals from problem dict ``prob`` (same masks and modes
+        as this plan's), scaled as at set-up (kw_plan_update_source); rewinds
+        the plan to t = 0."""
+        from .precompute import _build_sources
+
+        S = self.S
+        for src in _build_sources(prob, S.shape, S.spacing, S.dt, S.source_c0, S.ndim):
+            sig = np.ascontiguousarray(src.signal, dtype=np.float32)
+            K.check(self.lib.kw_plan_update_source(self._h, src.slot, K.ptr(sig), sig.shape[0], sig.shape[1]))
+            STATS["h2d_bytes"] += sig.nbytes
+        K.check(self.lib.kw_plan_reset(self._h))
+
     def set_checkpoints(self, interval):
         """Keep the carried state every ``interval`` steps of the coming
         forward run (kw_plan_set_checkpoints); 0 turns them off."""

@@ -87,6 +87,12 @@ def tr_problem(prob, data):
     return q
 
 
+def _tr_image(sim, compensation_factor):
+    img = compensation_factor * sim.p
+    img[img < 0] = 0
+    return img
+
+
 def time_reversal_images(probs, datas, stream=None, compensation_factor=2.0):
     """Time-reversal images of several recordings in one batch: the whole
     final pressure field of each reversed run times the compensation factor,
@@ -94,33 +100,65 @@ def time_reversal_images(probs, datas, stream=None, compensation_factor=2.0):
     b = SimulationBatch.from_problems([tr_problem(p, d) for p, d in zip(probs, datas)], stream=stream)
     try:
         b.run()
-        out = []
-        for s in b.sims:
-            img = compensation_factor * s.p
-            img[img < 0] = 0
-            out.append(img)
-        return out
+        return [_tr_image(s, compensation_factor) for s in b.sims]
     finally:
         b.close()
 
 
-def generate_pairs(n_pairs, seed0=1000, batch=128, noise=0.01, **kw):
+class PairGenerator:
+    """Forward and time-reversal runs of many pairs on two persistent batches
+    of ``batch`` plans each: the forward plans get each new phantom with
+    kw_plan_update_p0 and the time-reversal plans each new reversed recording
+    with kw_plan_update_source, so the host set-up and the plan creation are
+    paid once, not per pair.  All pairs share the grid, medium and sensor."""
+
+    def __init__(self, batch=256, noise=0.01, compensation_factor=2.0, **kw):
+        self.kw = kw
+        self.noise = noise
+        self.cf = compensation_factor
+        self.batch = batch
+        probs = [pair_problem(s, **kw) for s in range(batch)]
+        self.fwd = SimulationBatch.from_problems(probs)
+        ones = np.ones((int(probs[0]["sensor_mask"].sum()), probs[0]["Nt"]))
+        self.tr = SimulationBatch.from_problems([tr_problem(p, ones) for p in probs])
+
+    def run(self, seeds, rng):
+        """(images, phantoms) of the given phantom seeds (at most ``batch``)."""
+        probs = [pair_problem(s, **self.kw) for s in seeds]
+        sims = self.fwd.sims[: len(probs)]
+        for sim, pr in zip(sims, probs):
+            sim._plan.update_p0(pr["p0"])
+            sim.t = 0
+        self.fwd.run_steps(max(s.S.Nt for s in sims))
+        sims[0]._plan.sync()
+        datas = [noisy(s.results()["p"].astype(np.float64), rng, self.noise) for s in sims]
+        tsims = self.tr.sims[: len(probs)]
+        for sim, pr, d in zip(tsims, probs, datas):
+            sim._plan.update_sources(tr_problem(pr, d))
+            sim.t = 0
+        self.tr.run_steps(max(s.S.Nt for s in tsims))
+        tsims[0]._plan.sync()
+        return [_tr_image(s, self.cf) for s in tsims], [p["p0"] for p in probs]
+
+    def close(self):
+        self.fwd.close()
+        self.tr.close()
+
+
+def generate_pairs(n_pairs, seed0=1000, batch=256, noise=0.01, **kw):
     """(images, targets): time-reversal images of noisy recordings and the
-    phantoms that made them, float32 (n_pairs, n, n); the forward and the
-    reversed runs of each group of ``batch`` pairs run as one batch each."""
+    phantoms that made them, float32 (n_pairs, n, n), generated ``batch``
+    pairs at a time on persistent batches of plans (PairGenerator)."""
+    gen = PairGenerator(batch=min(batch, n_pairs), noise=noise, **kw)
     imgs, p0s = [], []
-    for g0 in range(0, n_pairs, batch):
-        seeds = list(range(seed0 + g0, seed0 + min(n_pairs, g0 + batch)))
-        probs = [pair_problem(s, **kw) for s in seeds]
-        fb = SimulationBatch.from_problems(probs)
-        try:
-            datas = [r["p"] for r in fb.run()]
-        finally:
-            fb.close()
-        rng = np.random.default_rng(seed0 + g0 + 7)
-        datas = [noisy(d.astype(np.float64), rng, noise) for d in datas]
-        imgs += time_reversal_images(probs, datas)
-        p0s += [p["p0"] for p in probs]
+    try:
+        for g0 in range(0, n_pairs, gen.batch):
+            seeds = list(range(seed0 + g0, seed0 + min(n_pairs, g0 + gen.batch)))
+            a, b = gen.run(seeds, np.random.default_rng(seed0 + g0 + 7))
+            imgs += a
+            p0s += b
+    finally:
+        gen.close()
     return np.asarray(imgs, np.float32), np.asarray(p0s, np.float32)
 
 
