@@ -557,9 +557,11 @@ def run_transmit(args):
     cells = sum(int(np.prod(p["shape"])) for p in probs)
     stream = torch.cuda.current_stream()
     t_setup = time.perf_counter()
-    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped, autotune=args.autotune)
+    b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped, autotune=args.autotune,
+                                      radix=args.radix)
     t_setup = time.perf_counter() - t_setup
     tuned = b.tuned
+    radix_order = b.radix_order
 
     def launches():
         return b.launch_count()
@@ -603,7 +605,7 @@ def run_transmit(args):
         cells_e2e = sum(int(np.prod(p["shape"])) for p in probs_e2e)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res = run_batch(probs_e2e, grouped=args.grouped, autotune=args.autotune)
+        res = run_batch(probs_e2e, grouped=args.grouped, autotune=args.autotune, radix=args.radix)
         t1 = time.perf_counter()
         assert len(res) == ninst and all(r["p"].shape[1] == 2000 for r in res)
         h2d = sum(sum(np.asarray(v).nbytes for v in (p["sound_speed"], p["density"], p["p"], p["p_mask"]))
@@ -632,7 +634,8 @@ def run_transmit(args):
         "data": "synthetic (seeded speckle media, discs, steering angles and grid sizes of the named ranges)",
         "config": {"workload": TRANSMIT_WORKLOAD, "instances": ninst, "cells_per_step": cells, "nt": nt,
                    "batch": "grouped launches" if args.grouped else "members as parallel graph branches",
-                   "autotune": bool(args.autotune), "tuned": tuned, "setup_seconds": t_setup,
+                   "autotune": bool(args.autotune), "tuned": tuned, "radix_autotune": bool(args.radix),
+                   "radix_order": radix_order, "setup_seconds": t_setup,
                    "l2": f"inputs larger than L2 ({cells * 4 * 12 / 1e9:.1f} GB of state, medium and spectra)"},
         "step_roofline": {"model_bytes_per_cell_step": TRANSMIT_A_MODEL, "achieved": step_gbs, "peak": peak,
                           "frac": step_gbs / peak, "unit": "GB/s", "peak_source": peak_kind},
@@ -908,6 +911,7 @@ def main(argv=None):
     ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
     ap.add_argument("--grouped", action="store_true", help="transmit workload: grouped launches across members")
     ap.add_argument("--autotune", action="store_true", help="transmit workload: autotune each member's launch geometry")
+    ap.add_argument("--radix", action="store_true", help="transmit workload: autotune the FFT radix schedule too")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #define KW_MAX_STAGES 16
+#define KW_RADIX_ORDERS 3  // radix schedules a plan can use (kw_plan.cu: kRadixOrders)
 
 // x / d for 0 <= x < 2^31 and 1 <= d < 2^31 as a multiply-high, an add and a
 // shift: m = floor(2^32 (2^l - d) / d) + 1 with l = ceil(log2 d) (the

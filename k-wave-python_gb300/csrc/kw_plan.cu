@@ -147,6 +147,7 @@ struct kw_plan {
   int* d_tstep = nullptr;
   int tstep_val = -1;  // value d_tstep holds once the stream reaches the last enqueued work
   cudaStream_t cap_stream = nullptr;
+  int radix_order = 0;  // schedule of the Stockham stages (kRadixOrders)
   // checkpoints of the carried state for the sound-speed gradient: slot s
   // holds u_i, rho_i and the spectrum of p after step s * ckpt_K
   int ckpt_K = 0;
@@ -193,12 +194,19 @@ static int ev_end(kw_plan* p, cudaStream_t st, int cls, size_t slot) {
   return KW_OK;
 }
 
-static bool factor_len(int n, KwFftLen& f) {
+// Radix schedules of the shared-memory Stockham FFTs: the order in which the
+// factors 4, 2, 3, 5, 7 of a length become stages.  Every schedule computes
+// the same DFT; they differ in shared-memory traffic, bank conflicts and
+// rounding (kw_batch_autotune_radix picks one by timing).
+static const int kRadixOrders[KW_RADIX_ORDERS][5] = {{4, 2, 3, 5, 7}, {5, 3, 7, 4, 2}, {3, 4, 5, 2, 7}};
+
+static bool factor_len(int n, KwFftLen& f, int order = 0) {
   f.n = n;
   f.nst = 0;
   int m = n;
-  const int rs[5] = {4, 2, 3, 5, 7};
-  for (int r : rs) {
+  const int* rs = kRadixOrders[order];
+  for (int i = 0; i < 5; ++i) {
+    const int r = rs[i];
     while (m % r == 0 && m > 1) {
       if (f.nst >= KW_MAX_STAGES) return false;
       f.radix[f.nst++] = r;
@@ -1945,6 +1953,68 @@ int32_t kw_batch_autotune(kw_batch* b, int32_t nsteps, void* stream, int32_t* T_
   if (T_out) *T_out = bestT;
   if (R_num) *R_num = bestN;
   if (R_den) *R_den = bestD;
+  return rc;
+}
+
+static int set_radix_order(kw_plan* p, int order) {
+  for (int a = 0; a < p->D - 1; ++a)
+    if (!factor_len(p->N[a], p->flen_axis[a], order)) return fail(KW_ERR_UNSUPPORTED, "radix schedule");
+  if (!factor_len(p->Mfft, p->flen_row, order)) return fail(KW_ERR_UNSUPPORTED, "radix schedule");
+  p->radix_order = order;
+  drop_graphs(p);
+  return KW_OK;
+}
+
+int32_t kw_plan_set_radix_order(kw_plan* p, int32_t order) {
+  if (!p) return fail(KW_ERR_INVALID, "null plan");
+  if (order < 0 || order >= KW_RADIX_ORDERS) return fail(KW_ERR_INVALID, "radix schedule %d outside [0, %d)", order,
+                                                          KW_RADIX_ORDERS);
+  if (p->finalized) CK(cudaDeviceSynchronize());
+  return set_radix_order(p, order);
+}
+
+int32_t kw_batch_autotune_radix(kw_batch* b, int32_t nsteps, void* stream, int32_t* order_out) {
+  if (!b) return fail(KW_ERR_INVALID, "null batch");
+  for (kw_plan* p : b->plans)
+    if (p->t != 0) return fail(KW_ERR_STATE, "kw_batch_autotune_radix needs every plan at t = 0");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int k = std::max(2, (int)nsteps);
+  for (kw_plan* p : b->plans) k = std::min(k, p->g.Nt - 1);
+  int best_order = b->plans.empty() ? 0 : b->plans[0]->radix_order;
+  int rc = KW_OK;
+  if (k >= 2) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int o = 0; o < KW_RADIX_ORDERS && !rc; ++o) {
+      for (kw_plan* p : b->plans)
+        if ((rc = set_radix_order(p, o))) break;
+      if (rc) break;
+      batch_clear(b);
+      if ((rc = batch_run(b, 1 + k, st, false)) || (rc = batch_reset(b)) || (rc = batch_run(b, 1, st, false))) break;
+      float ms = 0.f;
+      if (cudaEventRecord(e0, st) != cudaSuccess) rc = fail(KW_ERR_CUDA, "autotune event");
+      if (!rc) rc = batch_run(b, k, st, false);
+      if (!rc && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                  cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = fail(KW_ERR_CUDA, "autotune timing");
+      if (!rc) rc = batch_reset(b);
+      if (!rc && ms < best) {
+        best = ms;
+        best_order = o;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (kw_plan* p : b->plans) {
+      const int r2 = set_radix_order(p, best_order);
+      if (!rc) rc = r2;
+    }
+    batch_clear(b);
+    if (!rc) rc = batch_reset(b);
+  }
+  if (order_out) *order_out = best_order;
   return rc;
 }
 

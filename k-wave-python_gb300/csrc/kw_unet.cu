@@ -57,7 +57,6 @@ constexpr int kMaxNT = 256;         // tile columns (TMEM columns)
 constexpr uint32_t kSBO = 1024;     // 8-row group stride in a stage tile
 constexpr uint32_t kLBO = 128;      // K-adjacent core matrix stride
 constexpr int kATile = kBM * kBK * 2;         // 16 KB
-constexpr int kBTileMax = kMaxNT * kBK * 2;   // 32 KB
 constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr int kErrUmmaTimeout = 0x55;
 
@@ -122,23 +121,21 @@ __device__ __forceinline__ uint32_t chunk_off(int r, int kc) {
 
 __device__ __forceinline__ uint4 ldg16(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
 
-// 8 x 8 bf16 transpose: in[j] holds 8 values of row j; out[i] gets element i of every row.
+// Word w (0..3) of a uint4, w known at compile time after unrolling.
+__device__ __forceinline__ uint32_t word_of(const uint4& v, int w) {
+  return w == 0 ? v.x : w == 1 ? v.y : w == 2 ? v.z : v.w;
+}
+
+// 8 x 8 bf16 transpose: in[j] holds 8 values of row j; out[i] gets element i
+// of every row.  Word q of out[i] pairs element i of rows 2q and 2q + 1,
+// picked with byte permutes (low halves for even i, high halves for odd i).
 __device__ __forceinline__ void transpose8(const uint4 (&in)[8], uint4 (&out)[8]) {
-  uint16_t e[8][8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const uint32_t w[4] = {in[j].x, in[j].y, in[j].z, in[j].w};
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      e[j][2 * q] = (uint16_t)(w[q] & 0xFFFFu);
-      e[j][2 * q + 1] = (uint16_t)(w[q] >> 16);
-    }
-  }
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
+    const uint32_t sel = (i & 1) ? 0x7632u : 0x5410u;
     uint32_t w[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) w[q] = (uint32_t)e[2 * q][i] | ((uint32_t)e[2 * q + 1][i] << 16);
+    for (int q = 0; q < 4; ++q) w[q] = __byte_perm(word_of(in[2 * q], i >> 1), word_of(in[2 * q + 1], i >> 1), sel);
     out[i] = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
@@ -171,23 +168,57 @@ struct UmmaArgs {
   int ksplit;                // WGRAD: pixels per CTA (multiple of 64)
 };
 
-// 16-byte chunk of the convolution input for output pixel m and K position k
-// (8 channels of one tap); zero outside the image (padding) and beyond the batch.
-__device__ __forceinline__ uint4 conv_in_chunk(const UmmaArgs& a, int m, int k) {
-  const int cin = a.C1 + a.C2;
-  const int tap = k / cin, ci = k - tap * cin;
-  const int hw = a.H * a.W;
-  const int b = m / hw, rem = m - b * hw;
-  const int y = rem / a.W + tap / 3 - 1, x = rem % a.W + tap % 3 - 1;
-  if (b >= a.nb || tap >= 9 || y < 0 || y >= a.H || x < 0 || x >= a.W) return make_uint4(0, 0, 0, 0);
-  if (ci < a.C1) return ldg16(a.X1 + (((long long)b * a.H + y) * a.W + x) * a.C1 + ci);
-  const int h2 = a.H >> 1, w2 = a.W >> 1;
-  return ldg16(a.X2 + (((long long)b * h2 + (y >> 1)) * w2 + (x >> 1)) * a.C2 + (ci - a.C1));
+// 16-byte chunk of the convolution input at pixel (b, y, x) of the output
+// grid shifted by tap, channels ci..ci+7 (zero outside the image); bimg is the
+// index of the image's first pixel, b * H * W.
+__device__ __forceinline__ uint4 conv_chunk_at(const UmmaArgs& a, int bimg, int y, int x, int tap, int ci) {
+  y += tap / 3 - 1;
+  x += tap % 3 - 1;
+  if (tap >= 9 || y < 0 || y >= a.H || x < 0 || x >= a.W) return make_uint4(0, 0, 0, 0);
+  if (ci < a.C1) return ldg16(a.X1 + ((long long)bimg + y * a.W + x) * a.C1 + ci);
+  const int w2 = a.W >> 1;
+  return ldg16(a.X2 + ((long long)(bimg >> 2) + (y >> 1) * w2 + (x >> 1)) * a.C2 + (ci - a.C1));
 }
+
+// Per-thread state of the CONV operand gathers.  Thread tid fills the 8-wide
+// K group kc = (tid >> 3) & 7 of the tile rows r_i = (2 i + (tid >> 6)) * 8 +
+// (tid & 7), i < 8, in every chunk: their output pixels are decomposed once
+// per tile, and the group's (tap, channel) advances by 64 per chunk without
+// divisions.
+struct ConvRows {
+  int bimg[8];  // b * H * W of the row's pixel, -1 beyond the batch
+  int yx[8];    // y << 16 | x
+  int tap, ci;
+  __device__ __forceinline__ void init(const UmmaArgs& a, int m0, int kbeg) {
+    const int tid = threadIdx.x, hw = a.H * a.W;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int m = m0 + (2 * i + (tid >> 6)) * 8 + (tid & 7);
+      if (m < a.M) {
+        const int b = m / hw, rem = m - b * hw;
+        bimg[i] = b * hw;
+        yx[i] = ((rem / a.W) << 16) | (rem % a.W);
+      } else {
+        bimg[i] = -1;
+        yx[i] = 0;
+      }
+    }
+    const int cin = a.C1 + a.C2, k = kbeg + ((tid >> 3) & 7) * 8;
+    tap = k / cin;
+    ci = k - tap * cin;
+  }
+  __device__ __forceinline__ void advance(int cin) {
+    ci += kBK;
+    while (ci >= cin) {
+      ci -= cin;
+      ++tap;
+    }
+  }
+};
 
 // Fill stage tiles for K chunk k0 (all 128 threads).
 __device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA, unsigned char* sB, int m0, int n0,
-                                           int k0) {
+                                           int k0, ConvRows& cr) {
   const int tid = threadIdx.x;
   if (a.mode == 2) {
     // WGRAD: A(co, p) = dZ[p][co], B((tap, ci), p) = input[p + tap][ci]; 8 x 8 blocks transposed
@@ -205,14 +236,26 @@ __device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA,
       for (int i = 0; i < 8; ++i) *reinterpret_cast<uint4*>(sA + chunk_off(cb * 8 + i, pb)) = out[i];
     }
     const int nblk = (a.NT >> 3) * 8;
+    const int cin = a.C1 + a.C2, hw = a.H * a.W;
     for (int q = tid; q < nblk; q += kThreads) {
       const int nb8 = q >> 3, pb = q & 7;
       const int n = n0 + nb8 * 8;
+      const int tap = n / cin, ci = n - tap * cin;
+      // the block's 8 consecutive pixels, walked from the first without divisions
+      const int p0 = k0 + pb * 8;
+      int b = p0 / hw, rem = p0 - b * hw;
+      int y = rem / a.W, x = rem - y * a.W;
       uint4 in[8], out[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const int p = k0 + pb * 8 + j;
-        in[j] = (p < a.K && n < a.N) ? conv_in_chunk(a, p, n) : make_uint4(0, 0, 0, 0);
+        in[j] = (p0 + j < a.K && n < a.N) ? conv_chunk_at(a, b * hw, y, x, tap, ci) : make_uint4(0, 0, 0, 0);
+        if (++x == a.W) {
+          x = 0;
+          if (++y == a.H) {
+            y = 0;
+            ++b;
+          }
+        }
       }
       transpose8(in, out);
 #pragma unroll
@@ -220,18 +263,27 @@ __device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA,
     }
     return;
   }
-  // GEMM / CONV: A rows are output rows (pixels), 8 K groups of 8 per row
+  // GEMM / CONV: A rows are output rows (pixels), 8 K groups of 8 per row;
+  // this thread's group is kc, its rows those of ConvRows
+  const int kc = (tid >> 3) & 7;
+  if (a.mode == 0) {
 #pragma unroll
-  for (int it = 0; it < (kBM * 8) / kThreads; ++it) {
-    const int c = it * kThreads + tid;
-    const int r = (c >> 6) * 8 + (c & 7), kc = (c >> 3) & 7;
-    const int m = m0 + r, k = k0 + kc * 8;
-    uint4 v;
-    if (a.mode == 0)
-      v = (m < a.M && k < a.K) ? ldg16(a.A + (long long)m * a.K + k) : make_uint4(0, 0, 0, 0);
-    else
-      v = conv_in_chunk(a, m, k);
-    *reinterpret_cast<uint4*>(sA + chunk_off(r, kc)) = v;
+    for (int i = 0; i < 8; ++i) {
+      const int r = (2 * i + (tid >> 6)) * 8 + (tid & 7);
+      const int m = m0 + r, k = k0 + kc * 8;
+      const uint4 v = (m < a.M && k < a.K) ? ldg16(a.A + (long long)m * a.K + k) : make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(sA + chunk_off(r, kc)) = v;
+    }
+  } else {
+    uint4 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      v[i] = cr.bimg[i] < 0 ? make_uint4(0, 0, 0, 0)
+                            : conv_chunk_at(a, cr.bimg[i], cr.yx[i] >> 16, cr.yx[i] & 0xFFFF, cr.tap, cr.ci);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      *reinterpret_cast<uint4*>(sA + chunk_off((2 * i + (tid >> 6)) * 8 + (tid & 7), kc)) = v[i];
+    cr.advance(a.C1 + a.C2);
   }
   const __nv_bfloat16* Bm = a.mode == 0 ? a.B : a.Wt;
   for (int c = tid; c < a.NT * 8; c += kThreads) {
@@ -245,9 +297,9 @@ __device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA,
 __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* sA[2] = {base, base + kATile};
-  unsigned char* sB[2] = {base + 2 * kATile, base + 2 * kATile + kBTileMax};
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * kATile + 2 * kBTileMax);
+  // stage s: A at base + s kATile, B at base + 2 kATile + s bstage
+  const uint32_t bstage = (uint32_t)a.NT * (kBK * 2);  // NT rows of 128 bytes
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * kATile + 2 * bstage);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
   __shared__ int s_fail;
 
@@ -273,6 +325,8 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
   }
   const int nchunks = (kend - kbeg + kBK - 1) / kBK;
   const uint32_t idesc = idesc_bf16(kBM, a.NT);
+  ConvRows cr;
+  if (a.mode == 1) cr.init(a, m0, kbeg);
   bool ok = true;
   for (int c = 0; c < nchunks && ok; ++c) {
     const int s = c & 1;
@@ -283,12 +337,14 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
         break;
       }
     }
-    fill_stage(a, sA[s], sB[s], m0, n0, kbeg + c * kBK);
+    unsigned char* sAs = base + s * kATile;
+    unsigned char* sBs = base + 2 * kATile + s * bstage;
+    fill_stage(a, sAs, sBs, m0, n0, kbeg + c * kBK, cr);
     fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc_fence_after();
-      const uint32_t ab = smem_u32(sA[s]), bb = smem_u32(sB[s]);
+      const uint32_t ab = smem_u32(sAs), bb = smem_u32(sBs);
 #pragma unroll
       for (int kk = 0; kk < kBK / 16; ++kk)
         umma_bf16(tmem, smem_desc(ab + kk * 2 * kLBO), smem_desc(bb + kk * 2 * kLBO), idesc, (c | kk) != 0);
@@ -527,12 +583,23 @@ int g_umma_attr_dev = -1;
 
 int umma_fail(int code, const char* msg) { return kw_internal_fail(code, msg); }
 
+// Dynamic shared memory of a launch: the two A stages, two B stages of the
+// launch's tile width, barriers and alignment slack -- at least enough that no
+// more CTAs share an SM than its 512 TMEM columns hold (256-column tiles: 2
+// CTAs, 128-column tiles: 4), so that tcgen05.alloc never has to wait.
+int umma_smem(int NT) {
+  const int need = 2 * kATile + 2 * NT * kBK * 2 + 64 + 1024;
+  const int ncols = NT <= 32 ? 32 : NT <= 64 ? 64 : NT <= 128 ? 128 : 256;
+  const int floor_bytes = ncols == 256 ? 80 * 1024 : ncols == 128 ? 48 * 1024 : 0;
+  return need > floor_bytes ? need : floor_bytes;
+}
+
 int umma_launch(UmmaArgs& a, dim3 grid, cudaStream_t st) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return umma_fail(KW_ERR_CUDA, "cudaGetDevice failed");
-  const int smem = 2 * kATile + 2 * kBTileMax + 64 + 1024;
+  const int smem = umma_smem(a.NT);
   if (g_umma_attr_dev != dev) {
-    if (cudaFuncSetAttribute(k_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, umma_smem(kMaxNT)) != cudaSuccess)
       return umma_fail(KW_ERR_CUDA, "k_umma: cannot set the shared-memory size");
     g_umma_attr_dev = dev;
   }

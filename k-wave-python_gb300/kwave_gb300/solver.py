@@ -197,6 +197,10 @@ class DevicePlan:
         K.check(self.lib.kw_plan_adjoint(self._h, K.ptr(r), r.size, K.ptr(g), K.ptr(gc) if grad_c else None, st))
         return g, gc
 
+    def set_radix_order(self, order):
+        """Radix schedule of the run-time-length FFTs (kw_plan_set_radix_order)."""
+        K.check(self.lib.kw_plan_set_radix_order(self._h, int(order)))
+
     def set_graphs(self, enable):
         """Run repeated steps as replayed CUDA graphs (default) or as plain launches."""
         K.check(self.lib.kw_plan_set_graphs(self._h, int(bool(enable))))
@@ -389,7 +393,7 @@ class SimulationBatch:
     over members here gives the same results.
     """
 
-    def __init__(self, sims, stream=None, grouped=False, autotune=False):
+    def __init__(self, sims, stream=None, grouped=False, autotune=False, radix=False):
         self.sims = list(sims)
         if not self.sims:
             raise ValueError("SimulationBatch needs at least one simulation")
@@ -406,6 +410,9 @@ class SimulationBatch:
         self.tuned = None
         if autotune:
             self.tuned = self.autotune()
+        self.radix_order = 0
+        if radix:
+            self.radix_order = self.autotune_radix()
 
     def autotune(self, nsteps=8):
         """One launch geometry of the run-time-length kernels for all members,
@@ -418,10 +425,22 @@ class SimulationBatch:
             s.t = s._plan.time_index()
         return T.value, num.value / den.value
 
+    def autotune_radix(self, nsteps=8):
+        """One radix schedule of the run-time-length FFTs for all members,
+        timed on the batch itself (kw_batch_autotune_radix); every member must
+        be at t = 0 and is rewound there.  Schedules differ in rounding, within
+        the parity bar.  Returns the schedule index."""
+        st = C.c_void_p(self.stream) if self.stream is not None else None
+        o = C.c_int32()
+        K.check(self.lib.kw_batch_autotune_radix(self._h, int(nsteps), st, C.byref(o)))
+        for s in self.sims:
+            s.t = s._plan.time_index()
+        return o.value
+
     @classmethod
-    def from_problems(cls, problems, stream=None, grouped=False, autotune=False):
+    def from_problems(cls, problems, stream=None, grouped=False, autotune=False, radix=False):
         return cls([Simulation.from_problem(p, stream=stream) for p in problems], stream=stream, grouped=grouped,
-                   autotune=autotune)
+                   autotune=autotune, radix=radix)
 
     def launch_count(self):
         c = C.c_int64()
@@ -456,9 +475,9 @@ class SimulationBatch:
             pass
 
 
-def run_batch(problems, stream=None, grouped=False, autotune=False):
+def run_batch(problems, stream=None, grouped=False, autotune=False, radix=False):
     """Set up, run together and close the simulations described by plain problem dicts."""
-    b = SimulationBatch.from_problems(problems, stream=stream, grouped=grouped, autotune=autotune)
+    b = SimulationBatch.from_problems(problems, stream=stream, grouped=grouped, autotune=autotune, radix=radix)
     try:
         return b.run()
     finally:

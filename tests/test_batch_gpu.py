@@ -205,3 +205,46 @@ def test_transmit_events_batch_vs_oracle():
             print(f"transmit {shape} {mode}: p rel L2 {e:.2e}")
             assert r["p"].shape == ref["p"].shape
             assert e <= TOL, (shape, mode, e)
+
+
+def test_radix_schedules_vs_oracle():
+    """Every radix schedule of the run-time-length FFTs, set on a plan or
+    picked by the batch radix autotuner, keeps transmit events and the golden
+    cases within the parity bar of the oracle / the reference (the schedules
+    differ in rounding, so they are compared with the oracle, not bit for
+    bit)."""
+    import bench
+    from kwave_gb300.solver import Simulation, SimulationBatch
+    from oracle.kspace_oracle import OracleSimulation
+
+    probs = [bench.transmit_problem(shape, seed, nt=90, n_elem=6, pml=12) for shape, seed in TRANSMIT[:3]]
+    refs = [OracleSimulation(p, np.float32).run()["p"] for p in probs]
+    for order in range(3):
+        for prob, ref in zip(probs, refs):
+            sim = Simulation.from_problem(prob).setup(generic_fft=True)
+            try:
+                sim._plan.set_radix_order(order)
+                e = rel_l2(sim.run()["p"], ref)
+            finally:
+                sim.close()
+            print(f"radix schedule {order} {prob['shape']}: {e:.2e}")
+            assert e <= TOL, (order, prob["shape"], e)
+    b = SimulationBatch.from_problems(probs, grouped=True, autotune=True, radix=True)
+    try:
+        res = b.run()
+        print("tuned radix schedule", b.radix_order)
+        for r, ref in zip(res, refs):
+            assert rel_l2(r["p"], ref) <= TOL
+    finally:
+        b.close()
+    name = "het2d_abs_nl"
+    prob, r32, _, _ = load_case(name)
+    for order in (1, 2):
+        sim = Simulation.from_problem(prob).setup(generic_fft=True)
+        try:
+            sim._plan.set_radix_order(order)
+            res = sim.run()
+        finally:
+            sim.close()
+        for k in r32:
+            assert rel_l2(res[k], r32[k]) <= TOL, (name, order, k)
