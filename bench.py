@@ -739,7 +739,7 @@ def run_warmstart(args):
 
     npairs, epochs, iters, ntest = args.pairs, args.epochs, args.iterations, args.test_problems
     t0 = time.perf_counter()
-    imgs, p0s = generate_pairs(npairs, seed0=1000, batch=256)
+    imgs, p0s = generate_pairs(npairs, seed0=1000, batch=256, grouped=args.grouped)
     torch.cuda.synchronize()
     t_gen = time.perf_counter() - t0
     s = fit_input_scale(imgs[: min(npairs, 512)], p0s[: min(npairs, 512)])
@@ -783,6 +783,7 @@ def run_warmstart(args):
             "unit": "x (time for plain CGLS to reach its own best p0 error / time for learned+CGLS to reach it)",
             "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 network, f32 solver",
             "data": "synthetic vessel phantoms", "config": {"workload": WARMSTART_WORKLOAD, "pairs": npairs,
+                                                            "grouped_generation": bool(args.grouped),
                                                             "epochs": epochs, "cgls_iterations": iters,
                                                             "test_problems": ntest},
             "generation_seconds": t_gen, "training_seconds": t_train, "train_loss_per_epoch": hist,
@@ -909,7 +910,8 @@ def main(argv=None):
                     help="ivp3d: the 256^3 headline; transmit: 128 batched 2-D transmit events; "
                          "adjoint: p0 reconstruction by adjoint iterations at 512^2")
     ap.add_argument("--instances", type=int, default=128, help="transmit workload: simulations per batch")
-    ap.add_argument("--grouped", action="store_true", help="transmit workload: grouped launches across members")
+    ap.add_argument("--grouped", action="store_true",
+                    help="transmit / warmstart workloads: grouped launches across the batch members")
     ap.add_argument("--autotune", action="store_true", help="transmit workload: autotune each member's launch geometry")
     ap.add_argument("--radix", action="store_true", help="transmit workload: autotune the FFT radix schedule too")
     args = ap.parse_args(argv)

@@ -112,15 +112,15 @@ class PairGenerator:
     with kw_plan_update_source, so the host set-up and the plan creation are
     paid once, not per pair.  All pairs share the grid, medium and sensor."""
 
-    def __init__(self, batch=256, noise=0.01, compensation_factor=2.0, **kw):
+    def __init__(self, batch=256, noise=0.01, compensation_factor=2.0, grouped=False, **kw):
         self.kw = kw
         self.noise = noise
         self.cf = compensation_factor
         self.batch = batch
         probs = [pair_problem(s, **kw) for s in range(batch)]
-        self.fwd = SimulationBatch.from_problems(probs)
+        self.fwd = SimulationBatch.from_problems(probs, grouped=grouped)
         ones = np.ones((int(probs[0]["sensor_mask"].sum()), probs[0]["Nt"]))
-        self.tr = SimulationBatch.from_problems([tr_problem(p, ones) for p in probs])
+        self.tr = SimulationBatch.from_problems([tr_problem(p, ones) for p in probs], grouped=grouped)
 
     def run(self, seeds, rng):
         """(images, phantoms) of the given phantom seeds (at most ``batch``)."""
@@ -145,11 +145,12 @@ class PairGenerator:
         self.tr.close()
 
 
-def generate_pairs(n_pairs, seed0=1000, batch=256, noise=0.01, **kw):
+def generate_pairs(n_pairs, seed0=1000, batch=256, noise=0.01, grouped=False, **kw):
     """(images, targets): time-reversal images of noisy recordings and the
     phantoms that made them, float32 (n_pairs, n, n), generated ``batch``
-    pairs at a time on persistent batches of plans (PairGenerator)."""
-    gen = PairGenerator(batch=min(batch, n_pairs), noise=noise, **kw)
+    pairs at a time on persistent batches of plans (PairGenerator);
+    ``grouped`` runs each pass of all members as one grouped launch."""
+    gen = PairGenerator(batch=min(batch, n_pairs), noise=noise, grouped=grouped, **kw)
     imgs, p0s = [], []
     try:
         for g0 in range(0, n_pairs, gen.batch):
