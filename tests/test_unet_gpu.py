@@ -194,7 +194,7 @@ def test_pair_generator_reuses_plans_exactly():
     from kwave_gb300.warmstart import generate_pairs, noisy, pair_problem, time_reversal_images
 
     kw = dict(n=64, nt=120, n_sensor=32, radius=5e-4)
-    imgs, p0s = generate_pairs(6, seed0=3, batch=4, **kw)
+    imgs, p0s = generate_pairs(6, seed0=3, batch=4, grouped=False, **kw)
     for g0, seeds in ((0, [3, 4, 5, 6]), (4, [7, 8])):
         probs = [pair_problem(s, **kw) for s in seeds]
         rng = np.random.default_rng(3 + g0 + 7)
@@ -203,3 +203,8 @@ def test_pair_generator_reuses_plans_exactly():
         for i, (r, pr) in enumerate(zip(ref, probs)):
             assert np.array_equal(imgs[g0 + i], r.astype(np.float32))
             assert np.array_equal(p0s[g0 + i], pr["p0"].astype(np.float32))
+    # grouped launches run the run-time-length kernels: the same pairs to rounding
+    gimgs, gp0s = generate_pairs(6, seed0=3, batch=4, grouped=True, **kw)
+    assert np.array_equal(gp0s, p0s)
+    for a, b in zip(gimgs, imgs):
+        assert rel(a, b) <= 1e-5
