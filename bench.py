@@ -334,6 +334,12 @@ def cpu_baseline_sample(n=256, steps=1, warm=1):
     return n ** 3 * steps / dt / 1e6, dt
 
 
+def headline_config(n, nt):
+    """The workload description both arms print (identical for the same grid and step count)."""
+    return {"workload": WORKLOAD, "grid": [n] * 3, "nt": nt,
+            "l2": "inputs larger than L2 (state + medium ~1.1 GB per step at 256^3)"}
+
+
 def headline_parity(e2e_result=None):
     """Relative L2 errors of the headline result against the unmodified
     reference's float32 and float64 runs of the same seeded problem
@@ -375,7 +381,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
             "warmup": warm, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, shapes of the named workload)",
-            "config": {"workload": WORKLOAD, "grid": [args.n] * 3, "l2": "inputs larger than L2"},
+            "config": headline_config(args.n, max(1000, args.steps + args.warmup)),
+            "timed_steps": f"{warm}..{warm + steps - 1} (a bounded sample of the GPU arm's steps)",
             "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -502,9 +509,9 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K_steps, "warmup": W,
         "ms_per_step": ms_max / K_steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded ellipsoids and Gaussian blobs with the named shapes and ranges)",
-        "config": {"workload": WORKLOAD, "grid": list(S.shape), "nt": nt, "timed_steps": f"{W}..{W + K_steps - 1}",
-                   "l2": "inputs larger than L2 (state + medium ~1.1 GB per step)",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "config": headline_config(n, nt),
+        "timed_steps": f"{W}..{W + K_steps - 1}",
+        "parallelism": "replicas" if ws > 1 else "single GPU",
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": NCU_TRAFFIC_256.get(names[dom]) if n == 256 else None,
