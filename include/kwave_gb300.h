@@ -244,6 +244,18 @@ int32_t kw_plan_set_radix_order(kw_plan* plan, int32_t order);
  * the fastest and rewinds every plan to t = 0; *order_out (may be NULL)
  * receives it.  Run after kw_batch_autotune when both are wanted. */
 int32_t kw_batch_autotune_radix(kw_batch* batch, int32_t nsteps, void* stream, int32_t* order_out);
+/* Runs of steps with an unchanged launch sequence (no source switching on or
+ * off, no record start, not the last step) run as ONE launch of a graph that
+ * loops over the batch's step graph on the device: a conditional while node
+ * whose body is the step graph followed by a one-thread kernel counting the
+ * passes (cudaGraphSetConditional).  Runs shorter than 4 steps, and every
+ * step when enable == 0 (or KWAVE_GB300_BATCH_LOOPS=0 at kw_batch_create),
+ * are one launch each.  Results are bit-identical either way.  No
+ * counterpart in the reference. */
+int32_t kw_batch_set_loops(kw_batch* batch, int32_t enable);
+/* Graph launches issued by kw_batch_run for the batch's steps since its
+ * creation (one per loop run or per single step). */
+int32_t kw_batch_graph_launches(const kw_batch* batch, int64_t* count);
 /* Kernels launched through the batch and its plans since their creation (a
  * grouped launch over several plans counts once). */
 int32_t kw_batch_launch_count(const kw_batch* batch, int64_t* count);

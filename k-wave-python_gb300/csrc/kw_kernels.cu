@@ -883,6 +883,15 @@ __global__ void k_step_set(int* tdev, int t) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *tdev = t;
 }
 
+__global__ void k_loop_set(int* left, int n) { *left = n; }
+
+// End of one pass through a loop graph's body: count the pass and keep the
+// while-condition set while passes remain.
+__global__ void k_loop_tick(cudaGraphConditionalHandle h, int* left) {
+  const int v = --(*left);
+  cudaGraphSetConditional(h, v > 0 ? 1u : 0u);
+}
+
 __global__ void k_step_tick(int* tdev) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *tdev += 1;
 }

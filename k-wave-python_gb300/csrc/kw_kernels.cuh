@@ -213,6 +213,8 @@ __global__ void k_step_set(int* tdev, int t);
 __global__ void k_density_sum(float* __restrict__ out, const float* __restrict__ r0, const float* __restrict__ r1,
                               const float* __restrict__ r2, long long n);
 __global__ void k_step_tick(int* tdev);
+__global__ void k_loop_set(int* left, int n);
+__global__ void k_loop_tick(cudaGraphConditionalHandle h, int* left);
 __global__ void k_step_tick_group(int* const* tdev, int n);
 // grouped generic passes over several plans (blk: per member first block and grid shape)
 __global__ void k_axis_group(const AxisParams* Ps, const int4* blk, int n);

@@ -1574,7 +1574,9 @@ struct kw_batch {
     std::vector<int> keys;     // per plan: step key, or -1 when the plan does not step
     std::vector<char> grouped; // per plan: its passes run inside the grouped launches
     std::vector<long long> nl; // per ungrouped plan: launches of its step graph
+    cudaGraph_t graph;         // the step graph (kept as the body of loop graphs)
     cudaGraphExec_t exec;
+    cudaGraphExec_t loop_exec; // the step graph in a device-side while loop, or null
     long long nlaunch;         // grouped launches per replay
   };
   std::vector<Graph> graphs;
@@ -1588,6 +1590,12 @@ struct kw_batch {
   cudaEvent_t fork_ev = nullptr;
   std::vector<int> last_keys;
   int repeat = 0;
+  // runs of steps with one key vector: one launch of a graph that loops over
+  // the step graph on the device (KWAVE_GB300_BATCH_LOOPS=0 or
+  // kw_batch_set_loops(b, 0): one launch per step)
+  bool loops = true;
+  int* d_loop = nullptr;      // passes left in the running loop graph
+  long long graph_launches = 0;
 };
 
 int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
@@ -1601,6 +1609,10 @@ int32_t kw_batch_create(kw_plan* const* plans, int32_t n, kw_batch** out) {
   }
   kw_batch* b = new kw_batch;
   b->plans.assign(plans, plans + n);
+  {
+    const char* env = getenv("KWAVE_GB300_BATCH_LOOPS");
+    b->loops = !(env && env[0] == '0');
+  }
   // step graphs of batch members become child graphs: capture them with plain
   // stream-order edges between their kernels
   for (kw_plan* p : b->plans)
@@ -1637,7 +1649,9 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
   G.keys = keys;
   G.grouped.assign(n, 0);
   G.nl.assign(n, 0);
+  G.graph = nullptr;
   G.exec = nullptr;
+  G.loop_exec = nullptr;
   G.nlaunch = 0;
   int rc;
   for (size_t i = 0; i < n; ++i) {
@@ -1742,10 +1756,52 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
     }
   }
   const cudaError_t ei = cudaGraphInstantiate(&G.exec, graph, 0);
-  cudaGraphDestroy(graph);
-  if (ei != cudaSuccess) return fail(KW_ERR_CUDA, "batch graph instantiation: %s", cudaGetErrorString(ei));
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(KW_ERR_CUDA, "batch graph instantiation: %s", cudaGetErrorString(ei));
+  }
+  G.graph = graph;
   b->graphs.push_back(G);
   *out = &b->graphs.back();
+  return KW_OK;
+}
+
+// The loop graph of a batch step graph: a conditional while node whose body
+// is the step graph followed by k_loop_tick, so that one launch runs as many
+// steps as k_loop_set put in d_loop.
+static int batch_loop_graph(kw_batch* b, kw_batch::Graph* g) {
+  if (g->loop_exec) return KW_OK;
+  if (!b->d_loop) CK(cudaMalloc(&b->d_loop, sizeof(int)));
+  cudaGraph_t lg = nullptr;
+  CK(cudaGraphCreate(&lg, 0));
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t cn, child, tick;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, lg, 1, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    e = cudaGraphAddNode(&cn, lg, nullptr, nullptr, 0, &cp);
+  }
+  if (e == cudaSuccess) e = cudaGraphAddChildGraphNode(&child, cp.conditional.phGraph_out[0], nullptr, 0, g->graph);
+  if (e == cudaSuccess) {
+    cudaKernelNodeParams kp = {};
+    int* left = b->d_loop;
+    void* args[2] = {&h, &left};
+    kp.func = reinterpret_cast<void*>(k_loop_tick);
+    kp.gridDim = dim3(1);
+    kp.blockDim = dim3(1);
+    kp.kernelParams = args;
+    e = cudaGraphAddKernelNode(&tick, cp.conditional.phGraph_out[0], &child, 1, &kp);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->loop_exec, lg, 0);
+  cudaGraphDestroy(lg);
+  if (e != cudaSuccess) {
+    g->loop_exec = nullptr;
+    return fail(KW_ERR_CUDA, "batch loop graph: %s", cudaGetErrorString(e));
+  }
   return KW_OK;
 }
 
@@ -1845,17 +1901,46 @@ static int batch_run(kw_batch* b, int nsteps, cudaStream_t st, bool plain_last) 
       if ((rc = batch_step_streams(b, keys, st))) return rc;
       continue;
     }
+    // how many steps from here keep this key vector (all of them graph steps)
+    int m = 1;
+    if (b->loops) {
+      while (s + m < span) {
+        bool same = true;
+        for (size_t i = 0; i < n && same; ++i) {
+          kw_plan* p = b->plans[i];
+          const int t = p->t + m;
+          if (keys[i] < 0) {
+            same = t >= end[i];
+          } else {
+            same = t < end[i] && !step_eager(p, t, eend[i]) && step_key(p, t) == keys[i];
+          }
+        }
+        if (!same) break;
+        ++m;
+      }
+      if (m >= 4 && (rc = batch_loop_graph(b, g))) return rc;
+    }
     for (size_t i = 0; i < n; ++i)
       if (keys[i] >= 0 && (rc = step_counter_to(b->plans[i], b->plans[i]->t, st))) return rc;
-    CK(cudaGraphLaunch(g->exec, st));
-    b->launches += g->nlaunch;
+    if (m >= 4 && g->loop_exec) {
+      k_loop_set<<<1, 1, 0, st>>>(b->d_loop, m);
+      CK(cudaGetLastError());
+      CK(cudaGraphLaunch(g->loop_exec, st));
+      b->launches += 1 + (long long)m * (g->nlaunch + 1);
+    } else {
+      m = 1;
+      CK(cudaGraphLaunch(g->exec, st));
+      b->launches += g->nlaunch;
+    }
+    b->graph_launches += 1;
     for (size_t i = 0; i < n; ++i) {
       if (keys[i] < 0) continue;
       kw_plan* p = b->plans[i];
-      p->tstep_val = p->t + 1;
-      p->launches += g->nl[i];
-      p->t += 1;
+      p->tstep_val = p->t + m;
+      p->launches += (long long)m * g->nl[i];
+      p->t += m;
     }
+    s += m - 1;
   }
   return KW_OK;
 }
@@ -1866,11 +1951,18 @@ int32_t kw_batch_run(kw_batch* b, int32_t nsteps, void* stream) {
   return batch_run(b, nsteps, reinterpret_cast<cudaStream_t>(stream), true);
 }
 
+static void batch_free_graphs(kw_batch* b) {
+  for (auto& g : b->graphs) {
+    if (g.loop_exec) cudaGraphExecDestroy(g.loop_exec);
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
+  b->graphs.clear();
+}
+
 static void batch_clear(kw_batch* b) {
   cudaDeviceSynchronize();
-  for (auto& g : b->graphs)
-    if (g.exec) cudaGraphExecDestroy(g.exec);
-  b->graphs.clear();
+  batch_free_graphs(b);
   for (void* a : b->allocs) cudaFree(a);
   b->allocs.clear();
 }
@@ -2018,6 +2110,18 @@ int32_t kw_batch_autotune_radix(kw_batch* b, int32_t nsteps, void* stream, int32
   return rc;
 }
 
+int32_t kw_batch_set_loops(kw_batch* b, int32_t enable) {
+  if (!b) return fail(KW_ERR_INVALID, "null batch");
+  b->loops = enable != 0;
+  return KW_OK;
+}
+
+int32_t kw_batch_graph_launches(const kw_batch* b, int64_t* count) {
+  if (!b || !count) return fail(KW_ERR_INVALID, "kw_batch_graph_launches: null argument");
+  *count = b->graph_launches;
+  return KW_OK;
+}
+
 int32_t kw_batch_launch_count(const kw_batch* b, int64_t* count) {
   if (!b || !count) return fail(KW_ERR_INVALID, "null argument");
   long long c = b->launches;
@@ -2029,8 +2133,8 @@ int32_t kw_batch_launch_count(const kw_batch* b, int64_t* count) {
 int32_t kw_batch_destroy(kw_batch* b) {
   if (!b) return KW_OK;
   cudaDeviceSynchronize();  // replays and side-stream work may still be in flight
-  for (auto& g : b->graphs)
-    if (g.exec) cudaGraphExecDestroy(g.exec);
+  batch_free_graphs(b);
+  if (b->d_loop) cudaFree(b->d_loop);
   if (b->cap) cudaStreamDestroy(b->cap);
   for (cudaStream_t x : b->side) cudaStreamDestroy(x);
   for (cudaEvent_t e : b->side_done) cudaEventDestroy(e);

@@ -447,6 +447,17 @@ class SimulationBatch:
         K.check(self.lib.kw_batch_launch_count(self._h, C.byref(c)))
         return c.value
 
+    def graph_launches(self):
+        """Graph launches of the batch's steps so far (kw_batch_graph_launches)."""
+        c = C.c_int64()
+        K.check(self.lib.kw_batch_graph_launches(self._h, C.byref(c)))
+        return c.value
+
+    def set_loops(self, enable):
+        """Runs of steps with one launch sequence as one device-side loop
+        launch (default) or one launch per step (kw_batch_set_loops)."""
+        K.check(self.lib.kw_batch_set_loops(self._h, int(bool(enable))))
+
     def run_steps(self, nsteps):
         st = C.c_void_p(self.stream) if self.stream is not None else None
         K.check(self.lib.kw_batch_run(self._h, int(nsteps), st))

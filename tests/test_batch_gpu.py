@@ -248,3 +248,29 @@ def test_radix_schedules_vs_oracle():
             sim.close()
         for k in r32:
             assert rel_l2(res[k], r32[k]) <= TOL, (name, order, k)
+
+
+@pytest.mark.parametrize("grouped", [False, True])
+def test_device_loop_runs_bit_exact(grouped):
+    """Runs of steps with one launch sequence as one launch of a device-side
+    loop graph (conditional while node over the batch's step graph) give the
+    same results bit for bit as one graph launch per step, with far fewer
+    graph launches."""
+    import bench
+    from kwave_gb300.solver import SimulationBatch
+
+    probs = [bench.transmit_problem(shape, seed, nt=160, n_elem=6, pml=12) for shape, seed in TRANSMIT[:4]]
+    out, counts = [], []
+    for loops in (False, True):
+        b = SimulationBatch.from_problems(probs, grouped=grouped)
+        try:
+            b.set_loops(loops)
+            out.append(b.run())
+            counts.append(b.graph_launches())
+        finally:
+            b.close()
+    print(f"grouped={grouped}: graph launches per step {counts[0]} -> with loops {counts[1]}")
+    for ra, rb in zip(*out):
+        for k in ra:
+            assert np.array_equal(ra[k], rb[k]), k
+    assert counts[1] < counts[0] // 4, counts
