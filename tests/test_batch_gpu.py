@@ -96,9 +96,10 @@ def test_batch_bit_exact_and_parity(golden_generic):
             else:
                 assert e32 <= TOL, (name, k, e32)
     # grouped: far fewer launches than the members' steps would take one by one
+    # (about a dozen each); device-side loop runs add one counting kernel per step
     steps = sum(golden_generic[n][0]["Nt"] for n in names)
     print(f"{len(names)} members, {steps} member-steps, {launches} launches")
-    assert launches < 4 * steps
+    assert launches < 5 * steps
 
 
 def test_batch_mixed_members(golden_plain, golden_generic):
