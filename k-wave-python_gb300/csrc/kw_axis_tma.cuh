@@ -112,21 +112,6 @@ __device__ __forceinline__ float kappa_kk(const AxisParams& A, float kk) {
   return kwreg::sinc_taylor_sq(y);
 }
 
-// Base-2 logarithm and power of two with the SFU's approximate instructions
-// (lg2.approx / ex2.approx, relative error about 2^-22): |k|^a of the
-// fractional Laplacians as exp2(a/2 log2 |k|^2), well inside the 1e-5 parity
-// bar, for a fraction of the instructions of the correctly rounded forms.
-__device__ __forceinline__ float lg2_approx(float x) {
-  float y;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float ex2_approx(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
 __device__ __forceinline__ float kk_of(const float* k0s, int ndim, int x, const ColK& g) {
   const float kx = k0s[x];
   float kk = __fadd_rn(__fmul_rn(kx, kx), g.ky2);
@@ -473,12 +458,12 @@ __global__ void __launch_bounds__(T * P + 32, MINB)
 #pragma unroll
             for (int m = 0; m < E / P; ++m)
 #pragma unroll
-              for (int k2 = 0; k2 < P; ++k2) kc[m * P + k2] = lg2_approx(kk_of(k0s, A.ndim, t + P * m + E * k2, g));
+              for (int k2 = 0; k2 < P; ++k2) kc[m * P + k2] = log2f(kk_of(k0s, A.ndim, t + P * m + E * k2, g));
           }
           const float hp = 0.5f * (q == 0 ? A.pow1 : A.pow2);
 #pragma unroll
           for (int r = 0; r < E; ++r) {
-            const float val = (kc[r] == -INFINITY) ? 0.f : ex2_approx(hp * kc[r]);
+            const float val = (kc[r] == -INFINITY) ? 0.f : exp2f(hp * kc[r]);
             const float2 op = make_float2(val * A.scale, 0.f);
             v[r] = on ? cconj(kwreg::cmulf(op, v[r])) : make_float2(0.f, 0.f);
           }

@@ -35,16 +35,9 @@ __device__ __forceinline__ float sinc_taylor(float x) {
   return s;
 }
 
-// sin(x)/x from the same series given y = x^2 < 9; below y = 1 (every |k| of
-// a grid at a Courant number up to 0.36) six terms leave a remainder under
-// y^6 / 13! < 2e-10, so the series stops there.
+// sin(x)/x from the same series given y = x^2 < 9
 __device__ __forceinline__ float sinc_taylor_sq(float y) {
   float s = 1.0f;
-  if (y < 1.0f) {
-#pragma unroll
-    for (int n = 6; n >= 1; --n) s = fmaf(-y * (1.0f / float((2 * n) * (2 * n + 1))), s, 1.0f);
-    return s;
-  }
 #pragma unroll
   for (int n = 10; n >= 1; --n) s = fmaf(-y * (1.0f / float((2 * n) * (2 * n + 1))), s, 1.0f);
   return s;

@@ -35,7 +35,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "../../include/kwave_gb300.h"
@@ -60,15 +62,27 @@ constexpr int kATile = kBM * kBK * 2;         // 16 KB
 constexpr uint64_t kWaitNs = 2000000000ull;
 constexpr int kErrUmmaTimeout = 0x55;
 
-// tcgen05 shared-memory matrix descriptor: K-major, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+// tcgen05 shared-memory matrix descriptor: K-major, no swizzle; lbo = bytes
+// between core matrices adjacent along K, sbo = bytes between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo = kLBO, uint32_t sbo = kSBO) {
   uint64_t d = 0;
   d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((kLBO >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((kSBO >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
   d |= (uint64_t)1 << 46;  // descriptor version of the 5th-generation tensor cores
   return d;                // base offset 0, swizzle mode 0 (none)
 }
+
+// Halo-tile convolution (mode 3): a tile is 128 consecutive pixels of one
+// image row; a stage holds, for 16 input channels, the 3-row x 130-column
+// halo around them (two 8-channel groups of 16-byte pixel chunks, rows of
+// pixels contiguous) and the 9 taps' weights for those channels.  The nine
+// taps' A operands are the same halo at nine start addresses: with one pixel
+// per 16-byte row of the core matrices (SBO 128 bytes), a shift by one pixel
+// is 16 bytes and by one row 130 x 16 bytes.
+constexpr int kHaloCols = 130;
+constexpr uint32_t kHaloGroup = 3 * kHaloCols * 16;           // bytes of one 8-channel group
+constexpr uint32_t kAHalo = ((2 * kHaloGroup + 127) / 128) * 128;  // A stage bytes (16 channels)
 
 // Instruction descriptor of kind::f16: D f32, A and B bf16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
@@ -294,12 +308,42 @@ __device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA,
   }
 }
 
+// Fill a halo stage: A halo of channels ci0..ci0+15 around pixels (y, x0..x0+127)
+// of image bimg, and the 9 taps x NT output channels of weights for them.
+__device__ __forceinline__ void fill_halo(const UmmaArgs& a, unsigned char* sA, unsigned char* sB, int bimg, int y,
+                                          int x0, int n0, int ci0) {
+  const int tid = threadIdx.x;
+  for (int q = tid; q < 2 * 3 * kHaloCols; q += kThreads) {
+    const int kg = q / (3 * kHaloCols), rem = q - kg * (3 * kHaloCols);
+    const int r = rem / kHaloCols, col = rem - r * kHaloCols;
+    const int yy = y + r - 1, xx = x0 + col - 1, ci = ci0 + kg * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W) {
+      if (ci < a.C1)
+        v = ldg16(a.X1 + ((long long)bimg + yy * a.W + xx) * a.C1 + ci);
+      else
+        v = ldg16(a.X2 + ((long long)(bimg >> 2) + (yy >> 1) * (a.W >> 1) + (xx >> 1)) * a.C2 + (ci - a.C1));
+    }
+    *reinterpret_cast<uint4*>(sA + kg * kHaloGroup + rem * 16) = v;
+  }
+  const int cin = a.C1 + a.C2;
+  for (int q = tid; q < 18 * a.NT; q += kThreads) {
+    const int kg = q & 1, nt = q >> 1;
+    const int n = nt / 9, tap = nt - n * 9;
+    const uint4 v = (n0 + n < a.N) ? ldg16(a.Wt + ((long long)(n0 + n) * 9 + tap) * cin + ci0 + kg * 8)
+                                   : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(sB + ((tap * 2 + kg) * a.NT + n) * 16) = v;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  // stage s: A at base + s kATile, B at base + 2 kATile + s bstage
-  const uint32_t bstage = (uint32_t)a.NT * (kBK * 2);  // NT rows of 128 bytes
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * kATile + 2 * bstage);
+  // stage s: A at base + s astage, B at base + 2 astage + s bstage
+  const bool halo = a.mode == 3;
+  const uint32_t astage = halo ? kAHalo : (uint32_t)kATile;
+  const uint32_t bstage = halo ? (uint32_t)a.NT * 288u : (uint32_t)a.NT * (kBK * 2);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * astage + 2 * bstage);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
   __shared__ int s_fail;
 
@@ -323,8 +367,15 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
     kbeg = blockIdx.z * a.ksplit;
     kend = min(a.K, kbeg + a.ksplit);
   }
-  const int nchunks = (kend - kbeg + kBK - 1) / kBK;
+  const int nchunks = halo ? (a.C1 + a.C2) / 16 : (kend - kbeg + kBK - 1) / kBK;
   const uint32_t idesc = idesc_bf16(kBM, a.NT);
+  int hb = 0, hy = 0, hx = 0;  // halo tiles: image, row and first column of the tile
+  if (halo) {
+    const int hw = a.H * a.W;
+    hb = (m0 / hw) * hw;
+    hy = (m0 - hb) / a.W;
+    hx = m0 - hb - hy * a.W;
+  }
   ConvRows cr;
   if (a.mode == 1) cr.init(a, m0, kbeg);
   bool ok = true;
@@ -337,17 +388,30 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
         break;
       }
     }
-    unsigned char* sAs = base + s * kATile;
-    unsigned char* sBs = base + 2 * kATile + s * bstage;
-    fill_stage(a, sAs, sBs, m0, n0, kbeg + c * kBK, cr);
+    unsigned char* sAs = base + s * astage;
+    unsigned char* sBs = base + 2 * astage + s * bstage;
+    if (halo)
+      fill_halo(a, sAs, sBs, hb, hy, hx, n0, c * 16);
+    else
+      fill_stage(a, sAs, sBs, m0, n0, kbeg + c * kBK, cr);
     fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc_fence_after();
       const uint32_t ab = smem_u32(sAs), bb = smem_u32(sBs);
+      if (halo) {
+        // tap (dy, dx): the halo from row 1 + dy, column 1 + dx; the tap's weights
 #pragma unroll
-      for (int kk = 0; kk < kBK / 16; ++kk)
-        umma_bf16(tmem, smem_desc(ab + kk * 2 * kLBO), smem_desc(bb + kk * 2 * kLBO), idesc, (c | kk) != 0);
+        for (int tap = 0; tap < 9; ++tap) {
+          const uint32_t aoff = (uint32_t)(((tap / 3) * kHaloCols + (tap % 3)) * 16);
+          umma_bf16(tmem, smem_desc(ab + aoff, kHaloGroup, 128), smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128),
+                    idesc, (c | tap) != 0);
+        }
+      } else {
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; ++kk)
+          umma_bf16(tmem, smem_desc(ab + kk * 2 * kLBO), smem_desc(bb + kk * 2 * kLBO), idesc, (c | kk) != 0);
+      }
       umma_commit(&bar[s]);
     }
   }
@@ -370,7 +434,7 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 #pragma unroll
         for (int j = 0; j < 16; ++j)
           if (n0 + j0 + j < a.N) a.C[(long long)m * a.N + n0 + j0 + j] = v[j];
-      } else if (a.mode == 1) {
+      } else if (a.mode == 1 || a.mode == 3) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int n = n0 + j0 + j;
@@ -587,8 +651,8 @@ int umma_fail(int code, const char* msg) { return kw_internal_fail(code, msg); }
 // launch's tile width, barriers and alignment slack -- at least enough that no
 // more CTAs share an SM than its 512 TMEM columns hold (256-column tiles: 2
 // CTAs, 128-column tiles: 4), so that tcgen05.alloc never has to wait.
-int umma_smem(int NT) {
-  const int need = 2 * kATile + 2 * NT * kBK * 2 + 64 + 1024;
+int umma_smem(int NT, bool halo = false) {
+  const int need = halo ? 2 * (int)kAHalo + 2 * NT * 288 + 64 + 1024 : 2 * kATile + 2 * NT * kBK * 2 + 64 + 1024;
   const int ncols = NT <= 32 ? 32 : NT <= 64 ? 64 : NT <= 128 ? 128 : 256;
   const int floor_bytes = ncols == 256 ? 80 * 1024 : ncols == 128 ? 48 * 1024 : 0;
   return need > floor_bytes ? need : floor_bytes;
@@ -597,9 +661,10 @@ int umma_smem(int NT) {
 int umma_launch(UmmaArgs& a, dim3 grid, cudaStream_t st) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return umma_fail(KW_ERR_CUDA, "cudaGetDevice failed");
-  const int smem = umma_smem(a.NT);
+  const int smem = umma_smem(a.NT, a.mode == 3);
   if (g_umma_attr_dev != dev) {
-    if (cudaFuncSetAttribute(k_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, umma_smem(kMaxNT)) != cudaSuccess)
+    const int most = std::max(umma_smem(kMaxNT), umma_smem(kMaxNT, true));
+    if (cudaFuncSetAttribute(k_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, most) != cudaSuccess)
       return umma_fail(KW_ERR_CUDA, "k_umma: cannot set the shared-memory size");
     g_umma_attr_dev = dev;
   }
@@ -652,7 +717,13 @@ int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32
     return umma_fail(KW_ERR_INVALID, "kw_conv3x3: bad geometry");
   UmmaArgs a;
   memset(&a, 0, sizeof a);
-  a.mode = 1;
+  // 3x3 convolutions on rows of a multiple of 128 pixels with 16-channel
+  // inputs run on halo tiles (KWAVE_GB300_CONV_HALO=0: the gather tiles)
+  static const bool halo_ok = [] {
+    const char* env = getenv("KWAVE_GB300_CONV_HALO");
+    return !(env && env[0] == '0');
+  }();
+  a.mode = (halo_ok && W % 128 == 0 && c1 % 16 == 0 && c2 % 16 == 0) ? 3 : 1;
   a.nb = nb;
   a.H = H;
   a.W = W;

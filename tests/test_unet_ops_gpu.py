@@ -97,6 +97,28 @@ def test_conv3x3_forward(concat):
     assert e32 <= F32_TOL and e16 <= BF16_TOL
 
 
+@pytest.mark.parametrize("W,c1,c2,cout", [(128, 32, 0, 32), (128, 16, 32, 48), (256, 64, 0, 96)])
+def test_conv3x3_halo_tiles(W, c1, c2, cout):
+    """Rows of a multiple of 128 pixels with 16-channel inputs run on halo
+    tiles (the nine taps as nine shifted views of one shared-memory halo):
+    forward with and without the upsampled concatenation, against torch."""
+    import torch
+
+    from kwave_gb300 import unet_ops as U
+
+    nb, H = 2, 6
+    x1 = bf((nb, H, W, c1), 30)
+    x2 = bf((nb, H // 2, W // 2, c2), 31) if c2 else None
+    w = bf((cout, 9, c1 + c2), 32, 0.15)
+    bias = torch.randn(cout, generator=torch.Generator().manual_seed(33))
+    _, yf = U.conv3x3(x1.cuda(), w.cuda(), bias.cuda(), relu=True, x2=None if x2 is None else x2.cuda(),
+                      yf=torch.empty((nb, H, W, cout), dtype=torch.float32, device="cuda"))
+    torch.cuda.synchronize()
+    e = rel(yf, ref_conv(x1, w, bias, x2, relu=True))
+    print(f"halo conv W={W} c1={c1} c2={c2} cout={cout}: {e:.2e}")
+    assert e <= F32_TOL
+
+
 def test_conv3x3_data_and_weight_gradients():
     """Data gradient as the flipped-weight convolution, weight and bias
     gradients, against torch autograd of the same convolution (concatenated
