@@ -320,6 +320,9 @@ int32_t kw_gradient_noalloc(const float* f, float* out, int32_t ndim, const int3
  * gradients f32; every call enqueues on `stream` (NULL = default stream). */
 /* C[M][N] (f32) = sum_k A[m][k] B[n][k], A and B row-major bf16, K % 8 == 0. */
 int32_t kw_umma_gemm(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, void* stream);
+/* C[M][N] (f32) = sum_k A[k][m] B[k][n] on MN-major shared-memory tiles (A and
+ * B row-major bf16 with M and N contiguous), M % 8 == 0, N % 8 == 0. */
+int32_t kw_umma_gemm_mn(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, void* stream);
 /* 3x3 convolution, stride 1, zero padding: y[p][co] = act(bias[co] + sum over
  * taps and input channels of w[co][tap][ci] x[p + tap][ci]), where the input is
  * x1 (nb, H, W, c1) followed along channels by x2 (nb, H/2, W/2, c2) read with

@@ -28,9 +28,14 @@
 //          decoder's skip + upsampled input).  The data gradient of a 3x3
 //          convolution is the same gather with the flipped, transposed
 //          weights and the output gradient as input.
-//   WGRAD  weight gradient: m = output channel, n = (tap, input channel),
-//          k = pixel (split over CTAs, partial tiles added with red.add);
-//          8 x 8 blocks are loaded along channels and transposed in registers.
+//   WGRAD  weight gradient, k = pixel (split over CTAs, partial tiles added
+//          with red.add): by default m = (tap, input channel), n = output
+//          channel on MN-major tiles -- both operands are contiguous along m
+//          and n in the NHWC tensors, so their 16-byte groups are copied as
+//          they are (instruction descriptor bits 15/16; LBO = 128 bytes between
+//          K core matrices, SBO = 1024 bytes between 8-element groups); the
+//          K-major form (m = output channel) transposes 8 x 8 blocks in
+//          registers instead.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -88,6 +93,8 @@ constexpr uint32_t kAHalo = ((2 * kHaloGroup + 127) / 128) * 128;  // A stage by
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// The same with both operands MN-major (bits 15 and 16: A and B transposed).
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) { return idesc_bf16(M, N) | (1u << 15) | (1u << 16); }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
@@ -160,7 +167,7 @@ __device__ __forceinline__ void transpose8(const uint4 (&in)[8], uint4 (&out)[8]
 // gather policies
 // ---------------------------------------------------------------------------
 struct UmmaArgs {
-  int mode;  // 0 GEMM, 1 CONV, 2 WGRAD
+  int mode;  // 0 GEMM, 1 CONV, 2 WGRAD, 3 CONV on halo tiles, 4 GEMM of MN-major operands, 5 WGRAD MN-major
   int M, N, K;
   int NT;    // tile columns (multiple of 16, <= 256)
   // GEMM
@@ -234,6 +241,61 @@ struct ConvRows {
 __device__ __forceinline__ void fill_stage(const UmmaArgs& a, unsigned char* sA, unsigned char* sB, int m0, int n0,
                                            int k0, ConvRows& cr) {
   const int tid = threadIdx.x;
+  if (a.mode == 5) {
+    // weight gradient on MN-major tiles: m = (tap, input channel), n = output
+    // channel, k = pixel; A(p, m) = input[p + tap][ci], B(p, n) = dz[p][co]:
+    // both 8-wide groups are 16 contiguous bytes of the NHWC tensors, copied
+    // as they are (chunk layout as in mode 4)
+    const int k = tid & 63;
+    const int p = k0 + k;
+    const bool pin = p < a.K;
+    int bimg = 0, y = 0, x = 0;
+    if (pin) {
+      const int hw = a.H * a.W;
+      const int b = p / hw, rem = p - b * hw;
+      bimg = b * hw;
+      y = rem / a.W;
+      x = rem - y * a.W;
+    }
+    const int cin = a.C1 + a.C2;
+#pragma unroll
+    for (int it = 0; it < 8; ++it) {
+      const int g = it * 2 + (tid >> 6);
+      const int m = m0 + g * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (pin && m < a.M) {
+        const int tap = m / cin;
+        v = conv_chunk_at(a, bimg, y, x, tap, m - tap * cin);
+      }
+      *reinterpret_cast<uint4*>(sA + g * 1024 + (k >> 3) * 128 + (k & 7) * 16) = v;
+    }
+    for (int c = tid; c < a.NT * 8; c += kThreads) {
+      const int kk = c & 63, g = c >> 6;
+      const int n = n0 + g * 8, pp = k0 + kk;
+      const uint4 v = (n < a.N && pp < a.K) ? ldg16(a.dZ + (long long)pp * a.N + n) : make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(sB + g * 1024 + (kk >> 3) * 128 + (kk & 7) * 16) = v;
+    }
+    return;
+  }
+  if (a.mode == 4) {
+    // MN-major tiles: A[k][m], B[k][n] row-major; chunk (8-row group g of M or N,
+    // k) = 8 consecutive m (n) at one k, stored at g * 1024 + (k / 8) * 128 + (k % 8) * 16
+#pragma unroll
+    for (int it = 0; it < 8; ++it) {
+      const int c = it * kThreads + tid;
+      const int k = c & 63, g = c >> 6;
+      const int m = m0 + g * 8, kk = k0 + k;
+      const uint4 v = (m < a.M && kk < a.K) ? ldg16(a.A + (long long)kk * a.M + m) : make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(sA + g * 1024 + (k >> 3) * 128 + (k & 7) * 16) = v;
+    }
+    for (int c = tid; c < a.NT * 8; c += kThreads) {
+      const int k = c & 63, g = c >> 6;
+      const int n = n0 + g * 8, kk = k0 + k;
+      const uint4 v = (n < a.N && kk < a.K) ? ldg16(a.B + (long long)kk * a.N + n) : make_uint4(0, 0, 0, 0);
+      *reinterpret_cast<uint4*>(sB + g * 1024 + (k >> 3) * 128 + (k & 7) * 16) = v;
+    }
+    return;
+  }
   if (a.mode == 2) {
     // WGRAD: A(co, p) = dZ[p][co], B((tap, ci), p) = input[p + tap][ci]; 8 x 8 blocks transposed
     {
@@ -363,12 +425,15 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
   const uint32_t tmem = *tslot;
 
   int kbeg = 0, kend = a.K;
-  if (a.mode == 2) {
+  if (a.mode == 2 || a.mode == 5) {
     kbeg = blockIdx.z * a.ksplit;
     kend = min(a.K, kbeg + a.ksplit);
   }
   const int nchunks = halo ? (a.C1 + a.C2) / 16 : (kend - kbeg + kBK - 1) / kBK;
-  const uint32_t idesc = idesc_bf16(kBM, a.NT);
+  // MN-major tiles (modes 4, 5): 8-element groups along M / N 1024 bytes apart
+  // (SBO), K core matrices 128 bytes apart (LBO), as in the K-major layout
+  const bool mn = a.mode == 4 || a.mode == 5;
+  const uint32_t idesc = mn ? idesc_bf16_mn(kBM, a.NT) : idesc_bf16(kBM, a.NT);
   int hb = 0, hy = 0, hx = 0;  // halo tiles: image, row and first column of the tile
   if (halo) {
     const int hw = a.H * a.W;
@@ -407,6 +472,11 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
           umma_bf16(tmem, smem_desc(ab + aoff, kHaloGroup, 128), smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128),
                     idesc, (c | tap) != 0);
         }
+      } else if (mn) {
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; ++kk)
+          umma_bf16(tmem, smem_desc(ab + kk * 256, 128, 1024), smem_desc(bb + kk * 256, 128, 1024), idesc,
+                    (c | kk) != 0);
       } else {
 #pragma unroll
         for (int kk = 0; kk < kBK / 16; ++kk)
@@ -430,7 +500,7 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
       float v[16];
       tmem_ld16(trow + (uint32_t)j0, v);
       if (m >= a.M) continue;
-      if (a.mode == 0) {
+      if (a.mode == 0 || a.mode == 4) {
 #pragma unroll
         for (int j = 0; j < 16; ++j)
           if (n0 + j0 + j < a.N) a.C[(long long)m * a.N + n0 + j0 + j] = v[j];
@@ -464,6 +534,13 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
             if (a.Y) a.Y[o + j] = __float2bfloat16_rn(v[j]);
             if (a.Yf) a.Yf[o + j] = v[j];
           }
+        }
+      } else if (a.mode == 5) {
+        // WGRAD on MN-major tiles: row m = (tap, ci), column n = co -> dW[co][tap][ci]
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + j0 + j;
+          if (n < a.N) atomicAdd(a.dW + (long long)n * a.M + m, v[j]);
         }
       } else {
         // WGRAD: add this pixel range's partial tile
@@ -580,13 +657,33 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, __nv_bfloat1
   }
 }
 
-// Bias gradient: db[c] += sum over pixels of dz[p][c] (one block per 256 pixels, red.add).
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dz, float* __restrict__ db, long long npix, int C) {
-  const long long p0 = (long long)blockIdx.x * 256;
-  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+// Bias gradient: db[c] += sum over pixels of dz[p][c].  Each block sums a
+// range of pixels with coalesced loads (consecutive threads read consecutive
+// elements of the NHWC rows; C divides 256 or is a multiple of it), reduces
+// per channel in shared memory and adds one value per channel (red.add).
+__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dz, float* __restrict__ db, long long npix, int C,
+                            long long pix_per_block) {
+  __shared__ float acc[256];
+  const long long p0 = (long long)blockIdx.x * pix_per_block;
+  const long long p1 = min(npix, p0 + pix_per_block);
+  const long long e0 = p0 * C, e1 = p1 * C;
+  if (C <= 256 && 256 % C == 0) {
+    // thread t always meets channel t % C
     float s = 0.f;
-    for (long long p = p0; p < min(npix, p0 + 256); ++p) s += __bfloat162float(dz[p * C + c]);
-    atomicAdd(db + c, s);
+    for (long long e = e0 + threadIdx.x; e < e1; e += 256) s += __bfloat162float(dz[e]);
+    acc[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < C) {
+      float t = 0.f;
+      for (int j = threadIdx.x; j < 256; j += C) t += acc[j];
+      atomicAdd(db + threadIdx.x, t);
+    }
+  } else {
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+      float t = 0.f;
+      for (long long p = p0; p < p1; ++p) t += __bfloat162float(dz[p * C + c]);
+      atomicAdd(db + c, t);
+    }
   }
 }
 
@@ -708,6 +805,23 @@ int32_t kw_umma_gemm(const void* A, const void* B, float* C, int32_t M, int32_t 
   return umma_launch(a, dim3((N + a.NT - 1) / a.NT, (M + kBM - 1) / kBM), static_cast<cudaStream_t>(stream));
 }
 
+int32_t kw_umma_gemm_mn(const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K, void* stream) {
+  if (!A || !B || !C) return umma_fail(KW_ERR_INVALID, "kw_umma_gemm_mn: null argument");
+  if (M <= 0 || N <= 0 || K <= 0 || M % 8 || N % 8)
+    return umma_fail(KW_ERR_INVALID, "kw_umma_gemm_mn: M, N, K > 0, M % 8 == 0 and N % 8 == 0");
+  UmmaArgs a;
+  memset(&a, 0, sizeof a);
+  a.mode = 4;
+  a.M = M;
+  a.N = N;
+  a.K = K;
+  a.NT = tile_cols(N);
+  a.A = static_cast<const __nv_bfloat16*>(A);
+  a.B = static_cast<const __nv_bfloat16*>(B);
+  a.C = C;
+  return umma_launch(a, dim3((N + a.NT - 1) / a.NT, (M + kBM - 1) / kBM), static_cast<cudaStream_t>(stream));
+}
+
 int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
                    const void* w, const float* bias, int32_t cout, int32_t relu, void* y, float* yf, void* stream) {
   if (!x1 || !w || (!y && !yf)) return umma_fail(KW_ERR_INVALID, "kw_conv3x3: null argument");
@@ -748,23 +862,29 @@ int32_t kw_conv3x3_wgrad(const void* x1, int32_t c1, const void* x2, int32_t c2,
   if (!x1 || !dz || !dw) return umma_fail(KW_ERR_INVALID, "kw_conv3x3_wgrad: null argument");
   if (c1 <= 0 || c1 % 8 || c2 < 0 || c2 % 8 || (c2 && !x2) || cout <= 0 || cout % 8)
     return umma_fail(KW_ERR_INVALID, "kw_conv3x3_wgrad: channels must be multiples of 8");
+  // MN-major tiles (rows (tap, input channel), columns output channels) unless
+  // KWAVE_GB300_WGRAD_MN=0 selects the transposing K-major tiles
+  static const bool mn_ok = [] {
+    const char* env = getenv("KWAVE_GB300_WGRAD_MN");
+    return !(env && env[0] == '0');
+  }();
   UmmaArgs a;
   memset(&a, 0, sizeof a);
-  a.mode = 2;
+  a.mode = mn_ok ? 5 : 2;
   a.nb = nb;
   a.H = H;
   a.W = W;
   a.C1 = c1;
   a.C2 = c2;
-  a.M = cout;
-  a.N = 9 * (c1 + c2);
+  a.M = mn_ok ? 9 * (c1 + c2) : cout;
+  a.N = mn_ok ? cout : 9 * (c1 + c2);
   a.K = nb * H * W;
   a.NT = tile_cols(a.N);
   a.X1 = static_cast<const __nv_bfloat16*>(x1);
   a.X2 = static_cast<const __nv_bfloat16*>(x2);
   a.dZ = static_cast<const __nv_bfloat16*>(dz);
   a.dW = dw;
-  const int ntile = (a.N + a.NT - 1) / a.NT, mtile = (cout + kBM - 1) / kBM;
+  const int ntile = (a.N + a.NT - 1) / a.NT, mtile = (a.M + kBM - 1) / kBM;
   // split the pixels so that the grid covers the GPU a few times over
   int dev = 0, nsm = 148;
   cudaGetDevice(&dev);
@@ -832,8 +952,9 @@ int32_t kw_unet_flip_weights(const void* w, void* wt, int32_t cout, int32_t cin,
 
 int32_t kw_unet_bias_grad(const void* dz, float* db, int64_t npix, int32_t C, void* stream) {
   if (!dz || !db) return umma_fail(KW_ERR_INVALID, "kw_unet_bias_grad: null argument");
-  k_bias_grad<<<(int)((npix + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const __nv_bfloat16*>(dz), db, npix, C);
+  const long long per = 1024;  // pixels per block
+  k_bias_grad<<<(int)((npix + per - 1) / per), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const __nv_bfloat16*>(dz), db, npix, C, per);
   KW_UNET_CK();
   return KW_OK;
 }

@@ -90,6 +90,7 @@ _PROTOS = {
     "kw_plan_set_wait_test": (C.c_int32, [_P, C.c_int32]),
     # learned warm start (kw_unet.cu)
     "kw_umma_gemm": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, _P]),
+    "kw_umma_gemm_mn": (C.c_int32, [_P, _P, _P, C.c_int32, C.c_int32, C.c_int32, _P]),
     "kw_conv3x3": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, C.c_int32,
                                C.c_int32, _P, _P, _P]),
     "kw_conv3x3_wgrad": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, C.c_int32,

@@ -42,6 +42,19 @@ def gemm(A, B, out=None):
     return C_
 
 
+def gemm_mn(A, B, out=None):
+    """C = A.T @ B in f32 on the tensor cores from MN-major tiles (A: (K, M),
+    B: (K, N) bf16, M and N multiples of 8)."""
+    import torch
+
+    _contig(A, B)
+    Kd, M = A.shape
+    N = B.shape[1]
+    C_ = out if out is not None else torch.empty((M, N), dtype=torch.float32, device=A.device)
+    K.check(_lib().kw_umma_gemm_mn(_p(A), _p(B), _p(C_), M, N, Kd, _st()))
+    return C_
+
+
 def conv3x3(x1, w, bias=None, relu=False, x2=None, y=None, yf=None):
     """3x3 same convolution of x1 (nb, H, W, c1) [+ upsampled x2 (nb, H/2,
     W/2, c2)] with w (cout, 9, c1 + c2) bf16; returns (y bf16, yf f32) as

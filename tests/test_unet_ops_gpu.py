@@ -62,6 +62,21 @@ def test_gemm_on_tensor_cores(M, N, K):
     assert e <= F32_TOL
 
 
+@pytest.mark.parametrize("M,N,K", [(128, 16, 64), (256, 64, 192), (384, 40, 320), (1152, 256, 4096)])
+def test_gemm_on_mn_major_tiles(M, N, K):
+    """The MN-major operand layout of the weight gradients, as a plain GEMM."""
+    import torch
+
+    from kwave_gb300 import unet_ops as U
+
+    A, B = bf((K, M), 3), bf((K, N), 4)
+    got = U.gemm_mn(A.cuda(), B.cuda())
+    torch.cuda.synchronize()
+    e = rel(got, A.float().T @ B.float())
+    print(f"gemm MN-major {M}x{N}x{K}: {e:.2e}")
+    assert e <= F32_TOL
+
+
 def ref_conv(x1, w, bias=None, x2=None, relu=False):
     import torch
     import torch.nn.functional as F
