@@ -566,6 +566,8 @@ def run_transmit(args):
     t_setup = time.perf_counter()
     b = SimulationBatch.from_problems(probs, stream=stream.cuda_stream, grouped=args.grouped, autotune=args.autotune,
                                       radix=args.radix)
+    if args.fft_schedule is not None:
+        b.set_radix_order(args.fft_schedule)
     t_setup = time.perf_counter() - t_setup
     tuned = b.tuned
     radix_order = b.radix_order
@@ -921,6 +923,8 @@ def main(argv=None):
                     help="transmit / warmstart workloads: grouped launches across the batch members")
     ap.add_argument("--autotune", action="store_true", help="transmit workload: autotune each member's launch geometry")
     ap.add_argument("--radix", action="store_true", help="transmit workload: autotune the FFT radix schedule too")
+    ap.add_argument("--fft-schedule", type=int, default=None,
+                    help="transmit workload: FFT schedule of every member (0-2 Stockham radix orders, 3 two-level)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

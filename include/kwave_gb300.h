@@ -232,13 +232,17 @@ int32_t kw_batch_run(kw_batch* batch, int32_t nsteps, void* stream);
  * bit-identical for every choice. */
 int32_t kw_batch_autotune(kw_batch* batch, int32_t nsteps, void* stream, int32_t* T_out, int32_t* R_num,
                           int32_t* R_den);
-/* Radix schedule of the run-time-length (shared-memory Stockham) FFTs: the
- * order in which a length's factors become stages -- 0: 4, 2, 3, 5, 7
- * (default), 1: 5, 3, 7, 4, 2, 2: 3, 4, 5, 2, 7.  Every schedule computes the
- * same transform; they differ in speed and in rounding (results stay within
- * the 1e-5 parity bar; they are not bit-identical across schedules).  No
- * counterpart in the reference. */
+/* Schedule of the run-time-length shared-memory FFTs.  0-2: Stockham stages
+ * with the factors in the order 0: 4, 2, 3, 5, 7 (default), 1: 5, 3, 7, 4, 2,
+ * 2: 3, 4, 5, 2, 7.  3: the two-level schedule (two passes of register DFTs)
+ * for lengths n1 n2 with both factors 5-smooth and at most 20, schedule 0 for
+ * the other lengths.  Every schedule computes the same transform; they differ
+ * in speed and in rounding (results stay within the 1e-5 parity bar; they are
+ * not bit-identical across schedules).  No counterpart in the reference. */
 int32_t kw_plan_set_radix_order(kw_plan* plan, int32_t order);
+/* The same schedule for every member of a batch (drops the batch's graphs;
+ * members keep their time index). */
+int32_t kw_batch_set_radix_order(kw_batch* batch, int32_t order);
 /* Batch radix autotuner: times each schedule on `nsteps` graph steps of the
  * whole batch after the t = 0 step (every member on the same schedule), keeps
  * the fastest and rewinds every plan to t = 0; *order_out (may be NULL)

@@ -171,7 +171,20 @@ __device__ __forceinline__ ColK col_geometry(const AxisParams& A, int c) {
   return g;
 }
 
-__global__ void k_axis(const __grid_constant__ AxisParams P);
+// Host launchers of the generic-length kernels (kw_generic.cuh: k_rows,
+// k_axis and their grouped forms, 256 threads per block), one set per FFT
+// schedule family F: 0 the Stockham stages (kw_kernels.cu), 1 the two-level
+// schedule for plans whose KwFftLen.n1 != 0 (kw_generic_fft2.cu).
+#define KW_GENERIC_DECL(F)                                                                                        \
+  cudaError_t kw_generic_attr_##F(int smem_max);                                                                  \
+  cudaError_t kw_rows_launch_##F(dim3 grid, size_t smem, cudaStream_t st, const RowsParams& P);                   \
+  cudaError_t kw_axis_launch_##F(dim3 grid, size_t smem, cudaStream_t st, const AxisParams& A);                   \
+  cudaError_t kw_rows_group_launch_##F(int nblk, size_t smem, cudaStream_t st, const RowsParams* Ps, const int4* blk, \
+                                       int n);                                                                    \
+  cudaError_t kw_axis_group_launch_##F(int nblk, size_t smem, cudaStream_t st, const AxisParams* Ps, const int4* blk, \
+                                       int n);
+KW_GENERIC_DECL(0)
+KW_GENERIC_DECL(1)
 // Register-FFT variants for power-of-two lengths 64..1024, launched through
 // these host helpers (defined next to the template instantiations).
 bool kw_reg_shape(int n, int* E, int* P);
@@ -216,9 +229,6 @@ __global__ void k_step_tick(int* tdev);
 __global__ void k_loop_set(int* left, int n);
 __global__ void k_loop_tick(cudaGraphConditionalHandle h, int* left);
 __global__ void k_step_tick_group(int* const* tdev, int n);
-// grouped generic passes over several plans (blk: per member first block and grid shape)
-__global__ void k_axis_group(const AxisParams* Ps, const int4* blk, int n);
-__global__ void k_rows_group(const RowsParams* Ps, const int4* blk, int n);
 // Medium grids derived on the device (kw_plan_derive_medium); any output may be null.
 struct DeriveParams {
   int ndim, N[3];
@@ -246,7 +256,6 @@ int* kw_device_error_ptr();
 // power-of-two row lengths; stage is ST_U or ST_RHO_PL.
 cudaError_t kw_rows_tma_attr(int m, int Hp, int ex_stride);
 cudaError_t kw_rows_tma_launch(int m, int stage, int nsm, cudaStream_t st, const RowsParams& Q, int* err, int pdl);
-__global__ void k_rows(const __grid_constant__ RowsParams P);
 __global__ void k_series_gather(const float* __restrict__ rec, int nrec, int nslots, int npts, int ncorner,
                                 const int* __restrict__ slot, const double* __restrict__ w, float* __restrict__ out);
 __global__ void k_series_reduce(const float* __restrict__ series, int npts, int nrec, int kind, float* __restrict__ out);

@@ -225,7 +225,7 @@ int na_setup(int dev, NaDevice** out) {
     NA_CK(cudaGetSymbolAddress((void**)&d.twpost, g_na_twpost));
     NA_CK(cudaGetSymbolAddress((void**)&d.k, g_na_k));
     NA_CK(cudaGetSymbolAddress((void**)&d.op, g_na_op));
-    NA_CK(cudaFuncSetAttribute(k_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    NA_CK(kw_generic_attr_0(200 * 1024));
     NA_CK(cudaFuncSetAttribute(k_na_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     d.ready = true;
   }
@@ -334,7 +334,7 @@ extern "C" int32_t kw_gradient_noalloc(const float* f, float* out, int32_t ndim,
     A.njobs = 0;
     A.plain[0] = 3;
     dim3 g((A.ncols + A.T - 1) / A.T, N[0], 1);
-    k_axis<<<g, 256, sizeof(float2) * ((size_t)A.n + 2 * (size_t)A.n * A.T), st>>>(A);
+    NA_CK(kw_axis_launch_0(g, sizeof(float2) * ((size_t)A.n + 2 * (size_t)A.n * A.T), st, A));
     NA_CK(cudaGetLastError());
     return KW_OK;
   };
@@ -345,7 +345,7 @@ extern "C" int32_t kw_gradient_noalloc(const float* f, float* out, int32_t ndim,
   A.jobs[0] = AxisJob{3, 3, OP_GRAD, axis};
   {
     dim3 g((A.ncols + A.T - 1) / A.T, 1, 1);
-    k_axis<<<g, 256, sizeof(float2) * ((size_t)A.n + 3 * (size_t)A.n * A.T), st>>>(A);
+    NA_CK(kw_axis_launch_0(g, sizeof(float2) * ((size_t)A.n + 3 * (size_t)A.n * A.T), st, A));
     NA_CK(cudaGetLastError());
   }
   if (ndim == 3 && (rc = plain(1))) return rc;

@@ -194,17 +194,21 @@ static int ev_end(kw_plan* p, cudaStream_t st, int cls, size_t slot) {
   return KW_OK;
 }
 
-// Radix schedules of the shared-memory Stockham FFTs: the order in which the
-// factors 4, 2, 3, 5, 7 of a length become stages.  Every schedule computes
-// the same DFT; they differ in shared-memory traffic, bank conflicts and
-// rounding (kw_batch_autotune_radix picks one by timing).
-static const int kRadixOrders[KW_RADIX_ORDERS][5] = {{4, 2, 3, 5, 7}, {5, 3, 7, 4, 2}, {3, 4, 5, 2, 7}};
+// Schedules of the run-time-length shared-memory FFTs.  Orders 0-2: the
+// order in which the factors 4, 2, 3, 5, 7 of a length become Stockham
+// stages.  Order 3: the two-level schedule (two passes of register DFTs,
+// kw_fft.cuh: fft2_smem) for lengths n1 n2 with both factors register-DFT
+// sizes, the Stockham order 0 for the others.  Every schedule computes the
+// same DFT; they differ in shared-memory traffic, instruction count, bank
+// conflicts and rounding (kw_batch_autotune_radix picks one by timing).
+static const int kRadixOrders[3][5] = {{4, 2, 3, 5, 7}, {5, 3, 7, 4, 2}, {3, 4, 5, 2, 7}};
+static const int kTwoLevelOrder = 3;
 
 static bool factor_len(int n, KwFftLen& f, int order = 0) {
   f.n = n;
   f.nst = 0;
   int m = n;
-  const int* rs = kRadixOrders[order];
+  const int* rs = kRadixOrders[order == kTwoLevelOrder ? 0 : order];
   for (int i = 0; i < 5; ++i) {
     const int r = rs[i];
     while (m % r == 0 && m > 1) {
@@ -214,6 +218,7 @@ static bool factor_len(int n, KwFftLen& f, int order = 0) {
     }
   }
   kw_fft_len_finish(f);
+  if (order == kTwoLevelOrder && m == 1) kw_fft_len_two_level(f);
   return m == 1;
 }
 
@@ -662,10 +667,8 @@ int32_t kw_plan_finalize(kw_plan* p) {
 
   // launch geometry
   set_generic_geometry(p, 0, 0);
-  CK(cudaFuncSetAttribute(k_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  CK(cudaFuncSetAttribute(k_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  CK(cudaFuncSetAttribute(k_rows_group, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  CK(cudaFuncSetAttribute(k_axis_group, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  CK(kw_generic_attr_0(200 * 1024));
+  CK(kw_generic_attr_1(200 * 1024));
   {
     const char* env = getenv("KWAVE_GB300_GENERIC_FFT");
     p->generic_only = (env && env[0] == '1') || (p->g.flags & KW_DESC_GENERIC_FFT);
@@ -903,7 +906,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
       CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
   } else {
     const int grid = (p->nrows + p->R - 1) / p->R;
-    k_rows<<<grid, kThreads, p->smem_rows, st>>>(P);
+    CK(P.flen.n1 ? kw_rows_launch_1(dim3(grid), p->smem_rows, st, P) : kw_rows_launch_0(dim3(grid), p->smem_rows, st, P));
   }
   CK(cudaGetLastError());
   return ev_end(p, st, rows_class(stage), slot);
@@ -968,7 +971,8 @@ static int launch_axis_plain(kw_plan* p, int axis, int inv, const int* bufs, int
     CK(kw_axis_reg_launch(n, grid, sizeof(float2) * ((size_t)n + (size_t)T * (n + E + 1)), st, A));
   } else {
     dim3 grid((A.ncols + A.T - 1) / A.T, nouter, nb);
-    k_axis<<<grid, kThreads, p->smem_axis_plain[axis], st>>>(A);
+    CK(A.flen.n1 ? kw_axis_launch_1(grid, p->smem_axis_plain[axis], st, A)
+                 : kw_axis_launch_0(grid, p->smem_axis_plain[axis], st, A));
   }
   CK(cudaGetLastError());
   return ev_end(p, st, KW_K_AXIS_PLAIN, slot);
@@ -1027,7 +1031,7 @@ static int launch_axis_ops(kw_plan* p, const AxisJob* jobs, int nj, cudaStream_t
     CK(kw_axis_reg_launch(n, grid, sizeof(float2) * ((size_t)n + (size_t)T * (n + E + 1)), st, A));
   } else {
     dim3 grid((A.ncols + A.T - 1) / A.T, 1, 1);
-    k_axis<<<grid, kThreads, p->smem_axis_ops, st>>>(A);
+    CK(A.flen.n1 ? kw_axis_launch_1(grid, p->smem_axis_ops, st, A) : kw_axis_launch_0(grid, p->smem_axis_ops, st, A));
   }
   CK(cudaGetLastError());
   return ev_end(p, st, KW_K_AXIS_OPS, slot);
@@ -1674,6 +1678,7 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
     size_t smem;
     void* params;
     int4* blk;
+    int sched;  // FFT schedule family of the grouped kernel (kw_generic.cuh)
   };
   std::vector<Pending> pend;
   std::vector<int*> ticks;
@@ -1683,8 +1688,11 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
       maxlen = std::max(maxlen, lists[i].size());
       ticks.push_back(b->plans[i]->d_tstep);
     }
+  // launch j of the members: one grouped launch per kind (rows, axis) and FFT
+  // schedule family
   for (size_t j = 0; j < maxlen; ++j)
-    for (int kind = 0; kind < 2; ++kind) {
+    for (int ks = 0; ks < 4; ++ks) {
+      const int kind = ks >> 1, sched = ks & 1;
       std::vector<RowsParams> rp;
       std::vector<AxisParams> ap;
       std::vector<int4> blk;
@@ -1693,6 +1701,7 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
       for (size_t i = 0; i < n; ++i) {
         if (!G.grouped[i] || lists[i].size() <= j || lists[i][j].kind != kind) continue;
         const kw_plan::LaunchRec& r = lists[i][j];
+        if ((kind == 0 ? r.rp.flen.n1 : r.ap.flen.n1) != 0 ? !sched : sched) continue;
         blk.push_back(make_int4((int)total, r.gx, r.gy, 0));
         if (kind == 0)
           rp.push_back(r.rp);
@@ -1705,7 +1714,7 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
       if (total >= (1LL << 31)) return fail(KW_ERR_UNSUPPORTED, "grouped launch of %lld blocks", total);
       const int m = (int)blk.size();
       blk.push_back(make_int4((int)total, 0, 0, 0));
-      Pending q{kind, m, (int)total, smem, nullptr, nullptr};
+      Pending q{kind, m, (int)total, smem, nullptr, nullptr, sched};
       if (kind == 0)
         rc = batch_upload(b, rp.data(), rp.size() * sizeof(RowsParams), &q.params);
       else
@@ -1731,14 +1740,21 @@ static int batch_graph(kw_batch* b, const std::vector<int>& keys, kw_batch::Grap
     }
   if (!b->cap) CK(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
   CK(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed));
+  cudaError_t elaunch = cudaSuccess;
   for (const Pending& q : pend) {
+    const RowsParams* rq = static_cast<const RowsParams*>(q.params);
+    const AxisParams* aq = static_cast<const AxisParams*>(q.params);
+    cudaError_t e;
     if (q.kind == 0)
-      k_rows_group<<<q.total, kThreads, q.smem, b->cap>>>(static_cast<const RowsParams*>(q.params), q.blk, q.m);
+      e = q.sched ? kw_rows_group_launch_1(q.total, q.smem, b->cap, rq, q.blk, q.m)
+                  : kw_rows_group_launch_0(q.total, q.smem, b->cap, rq, q.blk, q.m);
     else
-      k_axis_group<<<q.total, kThreads, q.smem, b->cap>>>(static_cast<const AxisParams*>(q.params), q.blk, q.m);
+      e = q.sched ? kw_axis_group_launch_1(q.total, q.smem, b->cap, aq, q.blk, q.m)
+                  : kw_axis_group_launch_0(q.total, q.smem, b->cap, aq, q.blk, q.m);
+    if (elaunch == cudaSuccess) elaunch = e;
   }
   if (dticks) k_step_tick_group<<<((int)ticks.size() + 127) / 128, 128, 0, b->cap>>>(dticks, (int)ticks.size());
-  const cudaError_t el = cudaGetLastError();
+  const cudaError_t el = elaunch != cudaSuccess ? elaunch : cudaGetLastError();
   cudaGraph_t graph = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(b->cap, &graph);
   if (el != cudaSuccess || ec != cudaSuccess) {
@@ -2063,6 +2079,19 @@ int32_t kw_plan_set_radix_order(kw_plan* p, int32_t order) {
                                                           KW_RADIX_ORDERS);
   if (p->finalized) CK(cudaDeviceSynchronize());
   return set_radix_order(p, order);
+}
+
+int32_t kw_batch_set_radix_order(kw_batch* b, int32_t order) {
+  if (!b) return fail(KW_ERR_INVALID, "null batch");
+  if (order < 0 || order >= KW_RADIX_ORDERS) return fail(KW_ERR_INVALID, "radix schedule %d outside [0, %d)", order,
+                                                          KW_RADIX_ORDERS);
+  CK(cudaDeviceSynchronize());
+  for (kw_plan* p : b->plans) {
+    const int rc = set_radix_order(p, order);
+    if (rc) return rc;
+  }
+  batch_clear(b);
+  return KW_OK;
 }
 
 int32_t kw_batch_autotune_radix(kw_batch* b, int32_t nsteps, void* stream, int32_t* order_out) {

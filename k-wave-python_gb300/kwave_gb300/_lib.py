@@ -85,6 +85,7 @@ _PROTOS = {
     "kw_plan_update_source": (C.c_int32, [_P, C.c_int32, _P, C.c_int32, C.c_int32]),
     "kw_plan_set_radix_order": (C.c_int32, [_P, C.c_int32]),
     "kw_batch_autotune_radix": (C.c_int32, [_P, C.c_int32, _P, C.POINTER(C.c_int32)]),
+    "kw_batch_set_radix_order": (C.c_int32, [_P, C.c_int32]),
     "kw_batch_set_loops": (C.c_int32, [_P, C.c_int32]),
     "kw_batch_graph_launches": (C.c_int32, [_P, C.POINTER(C.c_int64)]),
     "kw_plan_set_wait_test": (C.c_int32, [_P, C.c_int32]),

@@ -425,6 +425,12 @@ class SimulationBatch:
             s.t = s._plan.time_index()
         return T.value, num.value / den.value
 
+    def set_radix_order(self, order):
+        """The same FFT schedule for every member (kw_batch_set_radix_order;
+        0-2 Stockham radix orders, 3 the two-level schedule)."""
+        K.check(self.lib.kw_batch_set_radix_order(self._h, int(order)))
+        self.radix_order = int(order)
+
     def autotune_radix(self, nsteps=8):
         """One radix schedule of the run-time-length FFTs for all members,
         timed on the batch itself (kw_batch_autotune_radix); every member must

@@ -220,7 +220,7 @@ def test_radix_schedules_vs_oracle():
 
     probs = [bench.transmit_problem(shape, seed, nt=90, n_elem=6, pml=12) for shape, seed in TRANSMIT[:3]]
     refs = [OracleSimulation(p, np.float32).run()["p"] for p in probs]
-    for order in range(3):
+    for order in range(4):
         for prob, ref in zip(probs, refs):
             sim = Simulation.from_problem(prob).setup(generic_fft=True)
             try:
@@ -240,7 +240,7 @@ def test_radix_schedules_vs_oracle():
         b.close()
     name = "het2d_abs_nl"
     prob, r32, _, _ = load_case(name)
-    for order in (1, 2):
+    for order in (1, 2, 3):
         sim = Simulation.from_problem(prob).setup(generic_fft=True)
         try:
             sim._plan.set_radix_order(order)
