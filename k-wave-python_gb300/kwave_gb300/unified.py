@@ -22,13 +22,15 @@ neither ``kwave`` nor its grid classes:
 
 Differences, all stated where they apply: the computation is float32 (a
 float64 ``dtype`` only draws a warning, as ``backend="cpp"`` does in the
-reference, :262-268); ``device`` must be ``"gpu"``; HDF5 staging
-(``save_only``/``data_path``) and the binary-only arguments are not
-supported.
+reference, :262-268); ``device`` must be ``"gpu"``; ``binary_path`` is
+refused.  ``save_only=True`` writes the HDF5 input file of the C++ binary
+into ``data_path``, as ``backend="cpp"`` does (:mod:`kwave_gb300.cpp_io`),
+instead of running.
 """
 from __future__ import annotations
 
 import warnings
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -276,15 +278,17 @@ def kspaceFirstOrder(kgrid, medium, source, sensor=None, *, pml_size=20, pml_alp
     ``backend="gb300"``: 2-D and 3-D grids; time series are
     ``(n_sensor, Nt)`` with sensor points in C order, aggregates
     ``(n_sensor,)``, ``*_final`` fields on the user's grid.  ``stream`` is an
-    optional CUDA stream handle (int) for the device plan.
+    optional CUDA stream handle (int) for the device plan.  ``save_only=True``
+    writes ``data_path/kwave_input.h5`` (the C++ binary's input file) and
+    returns ``{"input_file", "output_file"[, "pml_size"]}`` without running.
     """
     if backend != BACKEND:
         raise ValueError(f"Unknown backend: {backend!r}. This entry point runs backend={BACKEND!r}; "
                          "use kwave.kspaceFirstOrder.kspaceFirstOrder for 'python' or 'cpp'.")
     if device != "gpu":
         raise ValueError(f"device must be 'gpu' for backend={BACKEND!r}, got {device!r}")
-    if save_only or data_path is not None or binary_path is not None:
-        raise NotImplementedError("HDF5 staging and external binaries belong to backend='cpp'")
+    if binary_path is not None:
+        raise NotImplementedError("external binaries belong to backend='cpp'")
     if device_num not in (None, 0):
         raise NotImplementedError("backend='gb300' runs on the current CUDA device; select it with "
                                   "CUDA_VISIBLE_DEVICES")
@@ -302,6 +306,8 @@ def kspaceFirstOrder(kgrid, medium, source, sensor=None, *, pml_size=20, pml_alp
     prob, pml_size = prepare_problem(kgrid, medium, source, sensor, pml_size=pml_size, pml_alpha=pml_alpha,
                                      pml_inside=pml_inside, use_sg=use_sg, use_kspace=use_kspace,
                                      smooth_p0=smooth_p0)
+    if save_only:
+        return _save_input_files(prob, pml_size, pml_inside, sensor, data_path)
 
     from .solver import Simulation
 
@@ -312,6 +318,47 @@ def kspaceFirstOrder(kgrid, medium, source, sensor=None, *, pml_size=20, pml_alp
         sim.close()
     if not pml_inside:
         result = strip_pml(result, pml_size, ndim)
+    return result
+
+
+_NO_CPP_ALPHA_MODES = ("no_absorption", "no_dispersion", "stokes")
+
+
+def _save_input_files(prob, pml_size, pml_inside, sensor, data_path):
+    """``save_only=True``: the HDF5 input file of the C++ binary for this
+    problem in ``data_path`` (kwave/kspaceFirstOrder.py:271-316 with
+    backend='cpp'): p0 smoothed on the host as that path does, Cartesian
+    sensor points mapped to grid points; returns the file names (and the PML
+    size when it lies outside the user's grid)."""
+    from . import cpp_io
+    from .conversion import cart2grid
+
+    if data_path is None:
+        raise ValueError("data_path must be provided when save_only=True (the HDF5 files must persist for cluster "
+                         "submission).")
+    if prob.get("alpha_mode") in _NO_CPP_ALPHA_MODES:
+        raise ValueError(f"medium.alpha_mode={prob['alpha_mode']!r} cannot be stored: the HDF5 input format of the "
+                         "C++ binary has no alpha_mode, and the binary applies power-law absorption and dispersion.")
+    if sensor is not None and getattr(sensor, "record", None) is not None:
+        warnings.warn("sensor.record is not stored in the HDF5 input file; the C++ binary records its default "
+                      "fields.", stacklevel=3)
+    rsi = getattr(sensor, "record_start_index", 1) if sensor is not None else 1
+    if rsi not in (None, 1):
+        warnings.warn("sensor.record_start_index is not stored in the HDF5 input file; the C++ binary records from "
+                      "the first time step.", stacklevel=3)
+    shape = tuple(int(n) for n in prob["shape"])
+    prob = dict(prob)
+    m = prob.get("sensor_mask")
+    if m is not None and _is_cartesian(m, len(shape)):
+        kg = SimpleNamespace(N=np.array(shape), spacing=np.array(prob["spacing"]), dim=len(shape))
+        prob["sensor_mask"] = cart2grid(kg, np.asarray(m), order="C")[0]
+    if prob.get("smooth_p0", True) and prob.get("p0") is not None and np.asarray(prob["p0"]).size > 1 \
+            and len(shape) >= 2:
+        prob["p0"] = cpp_io.smooth_host(np.asarray(prob["p0"], dtype=float).reshape(shape))
+    input_file, output_file = cpp_io.save_input_files(prob, data_path)
+    result = {"input_file": input_file, "output_file": output_file}
+    if not pml_inside:
+        result["pml_size"] = pml_size
     return result
 
 

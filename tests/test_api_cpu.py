@@ -159,8 +159,8 @@ def test_entry_point_rejections():
         unified.kspaceFirstOrder(kgrid, medium, source, sensor, backend="python")
     with pytest.raises(ValueError, match="device must be 'gpu'"):
         unified.kspaceFirstOrder(kgrid, medium, source, sensor, device="cpu")
-    with pytest.raises(NotImplementedError, match="HDF5"):
-        unified.kspaceFirstOrder(kgrid, medium, source, sensor, save_only=True)
+    with pytest.raises(ValueError, match="data_path must be provided"):
+        unified.kspaceFirstOrder(kgrid, medium, source, sensor, save_only=True, pml_size=4)
     with pytest.raises(ValueError, match="must be set before"):
         unified.kspaceFirstOrder(NS(N=(32, 30), spacing=(1e-4, 1e-4), Nt="auto", dt="auto"), medium, source, sensor)
     k1 = NS(N=np.array([64]), spacing=np.array([1e-4]), Nt=10, dt=1e-8)

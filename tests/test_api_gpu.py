@@ -69,3 +69,31 @@ def test_time_reversal():
     check("tr2d", {"p0_recon": got}, r32, r64)
     # the reconstruction resembles the true p0 on the region the line sees
     assert np.corrcoef(got.T.ravel(), prob["p0_true"][10:-10, 10:-10].ravel())[0, 1] > 0.5
+
+
+@pytest.mark.parametrize("name", ["ivp2d", "src3d"])
+def test_run_input_file(name, tmp_path):
+    """An input file of the C++ binary (written by save_only for a golden
+    call of tests/golden/cpp_io) runs on the device: the pressure at its
+    sensor points matches the run of the same call through the entry point
+    (p0 smoothed on the host in float64 for the file, on the device for the
+    direct run) within the parity bar."""
+    from fixtures import load_case
+
+    from kwave_gb300 import cpp_io, kspaceFirstOrder
+
+    prob, _, _, meta = load_case(name, "cpp_io")
+    opts = {k[4:]: (v.item() if v.ndim == 0 else tuple(v.tolist())) for k, v in meta.items() if k.startswith("opt_")}
+    kgrid, medium, source, sensor = api_cases.objects(prob)
+    if sensor is not None:
+        sensor.record = None
+    res = kspaceFirstOrder(kgrid, medium, source, sensor, backend="gb300", save_only=True, data_path=str(tmp_path),
+                           **opts)
+    got = cpp_io.run_input_file(res["input_file"])
+    if sensor is None:
+        sensor = NS(mask=np.ones(tuple(prob["shape"]), bool), record=None, record_start_index=None)
+    direct = kspaceFirstOrder(kgrid, medium, source, sensor, backend="gb300", **opts)
+    e = rel_l2(got["p"], direct["p"])
+    print(f"{name}: input file run vs entry point {e:.2e}, p {got['p'].shape}")
+    assert got["p"].shape == direct["p"].shape
+    assert e <= TOL, e
