@@ -111,7 +111,7 @@ def case_ivp2d():
     from make_golden import gaussian_blobs, smooth_random_field
 
     rng = np.random.default_rng(201)
-    shape = (40, 36)
+    shape = (40, 40)  # 56 x 56 with the PML: lengths the device FFTs take
     prob = dict(shape=shape, spacing=(1e-4, 1.2e-4), Nt=60, dt=1.5e-8,
                 sound_speed=smooth_random_field(shape, rng, rel=0.04),
                 density=smooth_random_field(shape, rng, rel=0.05, base=1000.0),
