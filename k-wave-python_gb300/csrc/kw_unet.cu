@@ -19,6 +19,12 @@
 // Every mbarrier wait is bounded (2 s of global time); a timeout sets the
 // device error word, skips the epilogue and still frees the TMEM.
 //
+// Persistent convolution (k_conv_tma): the halo-tile convolution of one
+// full-resolution input whose weights fit shared memory runs on persistent,
+// warp-specialised CTAs instead -- a producer lane streams each tile's halo
+// with 4-D TMA boxes into a shared-memory ring, one lane issues the MMAs into
+// two TMEM accumulators, four warps drain the other accumulator.
+//
 // Gathers:
 //   GEMM   A = row-major [M][K], B = row-major [N][K] (tests of the core)
 //   CONV   3x3 convolution, stride 1, zero padding, NHWC bf16: m = output
@@ -559,6 +565,230 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 }
 
 // ---------------------------------------------------------------------------
+// persistent, TMA-fed convolution on halo tiles (k_conv_tma)
+// ---------------------------------------------------------------------------
+// The same halo-tile convolution as k_umma mode 3 for one full-resolution
+// input (no concatenation) whose weights fit shared memory, restructured so
+// that staging, tensor-core work and the epilogue overlap:
+//   * the CTA is persistent over tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+//     (a tile: 128 pixels of one image row, all output channels);
+//   * the weights of all input channels stay in shared memory for the whole
+//     kernel, in the B layout of mode 3 ([16-channel group][tap][8-channel
+//     half][output channel][8 channels]);
+//   * warp 4 (one lane) is the producer: per 16-channel group of a tile it
+//     loads the 3 x 130-pixel halo with two 4-D TMA boxes of 8 channels
+//     (tensor map over the NHWC input, zero fill outside the image) into a
+//     ring of a.stages stages (chosen per launch), completion on full[s];
+//   * warp 5 (one lane) issues the nine tcgen05.mma per group into one of two
+//     TMEM accumulators, commits each group to empty[s] (the producer may
+//     refill the stage) and each finished tile to tfull[b];
+//   * warps 0-3 read accumulator b (warp w: TMEM lanes 32w..32w+31), apply
+//     bias and ReLU, store bf16 and/or f32 rows, and arrive on tempty[b] so
+//     that the tile after next may overwrite it.
+// Every wait is bounded; a timeout sets s_fail, every role leaves its loop,
+// the producer waits (bounded) for its last copies and the MMA lane for its
+// last MMAs before the CTA frees its TMEM.
+constexpr int kCtThreads = 192;
+constexpr int kCtMaxStages = 4;
+constexpr uint32_t kCtGroup = 6272;          // one 8-channel halo box (3 x 130 x 16 = 6240 bytes), 128-byte aligned
+constexpr uint32_t kCtBox = 3 * kHaloCols * 16;
+constexpr uint32_t kCtStage = 2 * kCtGroup;  // 16 channels
+
+struct ConvTmaArgs {
+  int nb, H, W, C1, N, NT;  // NT: N rounded up to 16 (one column tile)
+  int ntiles;               // nb * H * W / 128
+  int stages;               // depth of the halo ring (2..kCtMaxStages)
+  const __nv_bfloat16* Wt;  // [N][9][C1]
+  const float* bias;
+  int relu;
+  __nv_bfloat16* Y;
+  float* Yf;
+};
+
+__host__ __device__ inline uint32_t conv_tma_wbytes(int C1, int NT) { return (uint32_t)(9 * C1 * NT * 2); }
+
+__host__ __device__ inline uint32_t conv_tma_tmem_cols(int NT) {
+  const int c = 2 * NT;
+  return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
+}
+
+__global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__ CUtensorMap xmap, ConvTmaArgs a,
+                                                         int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int groups = a.C1 / 16;
+  const uint32_t wbytes = conv_tma_wbytes(a.C1, a.NT);
+  const int S = a.stages;
+  unsigned char* sW = base;
+  float* sBias = reinterpret_cast<float*>(base + ((wbytes + 1023) & ~1023u));
+  unsigned char* sH = reinterpret_cast<unsigned char*>(sBias) + 1024;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sH + S * kCtStage);
+  uint64_t* empty = full + S;
+  uint64_t* tfull = empty + S;
+  uint64_t* tempty = tfull + 2;
+  uint64_t* done = tempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  __shared__ volatile int s_fail;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t ncols = conv_tma_tmem_cols(a.NT);
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 128);
+    }
+    mbar_init(done, 1);
+    s_fail = 0;
+    kwtma::fence_barrier_init();
+  }
+  if (warp == 0) tmem_alloc(tslot, ncols);
+  // weights of every 16-channel group: [c][tap][half][n][8 channels]
+  const int wrows = groups * 18 * a.NT;
+  for (int q = tid; q < wrows; q += kCtThreads) {
+    const int c = q / (18 * a.NT), r = q - c * 18 * a.NT;
+    const int th = r / a.NT, n = r - th * a.NT;
+    const int tap = th >> 1, half = th & 1;
+    const uint4 v = (n < a.N) ? ldg16(a.Wt + ((long long)n * 9 + tap) * a.C1 + c * 16 + half * 8)
+                              : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(sW + (uint32_t)q * 16) = v;
+  }
+  for (int n = tid; n < a.NT; n += kCtThreads) sBias[n] = (a.bias && n < a.N) ? a.bias[n] : 0.f;
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int segs = a.W / 128;
+
+  if (warp == 4) {
+    if (lane == 0) {
+      // producer, TMA: two 4-D boxes per stage
+      int q = 0;
+      for (int t = blockIdx.x; t < a.ntiles && !s_fail; t += gridDim.x) {
+        const int seg = t % segs, row = t / segs;
+        const int y = row % a.H, b = row / a.H;
+        for (int c = 0; c < groups; ++c, ++q) {
+          const int s = q % S;
+          if (q >= S && !mbar_wait(&empty[s], ((q / S) - 1) & 1, kWaitNs)) {
+            s_fail = 1;
+            break;
+          }
+          if (s_fail) break;
+          kwtma::mbar_arrive_expect_tx(&full[s], 2 * kCtBox);
+          kwtma::tma_load_4d(sH + s * kCtStage, &xmap, c * 16, seg * 128 - 1, y - 1, b, &full[s]);
+          kwtma::tma_load_4d(sH + s * kCtStage + kCtGroup, &xmap, c * 16 + 8, seg * 128 - 1, y - 1, b, &full[s]);
+        }
+      }
+      // the last use of each stage: its copies must have landed before the CTA ends
+      for (int k = q - 1; k >= 0 && k >= q - S; --k)
+        if (!mbar_wait(&full[k % S], (k / S) & 1, kWaitNs)) s_fail = 1;
+    }
+  } else if (warp == 5) {
+    if (lane == 0) {
+      // tensor-core issuer
+      const uint32_t idesc = idesc_bf16(kBM, a.NT);
+      int q = 0, i = 0;
+      for (int t = blockIdx.x; t < a.ntiles && !s_fail; t += gridDim.x, ++i) {
+        const int b = i & 1;
+        if (i >= 2 && !mbar_wait(&tempty[b], ((i >> 1) - 1) & 1, kWaitNs)) {
+          s_fail = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * a.NT);
+        bool ok = true;
+        for (int c = 0; c < groups; ++c, ++q) {
+          const int s = q % S;
+          if (!mbar_wait(&full[s], (q / S) & 1, kWaitNs) || s_fail) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t ab = smem_u32(sH + s * kCtStage);
+          const uint32_t bb = smem_u32(sW + (uint32_t)c * 18 * a.NT * 16);
+#pragma unroll
+          for (int tap = 0; tap < 9; ++tap) {
+            const uint32_t aoff = (uint32_t)(((tap / 3) * kHaloCols + (tap % 3)) * 16);
+            umma_bf16(acc, smem_desc(ab + aoff, kCtGroup, 128), smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128),
+                      idesc, (c | tap) != 0);
+          }
+          umma_commit(&empty[s]);
+        }
+        if (!ok) {
+          s_fail = 1;
+          break;
+        }
+        umma_commit(&tfull[b]);
+      }
+      // every MMA issued by this thread has completed before the TMEM is freed
+      umma_commit(done);
+      if (!mbar_wait(done, 0, kWaitNs)) s_fail = 1;
+    }
+  } else {
+    // epilogue: warps 0-3, one accumulator row per thread
+    int i = 0;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, ++i) {
+      const int b = i & 1;
+      // the warp leaves together: tcgen05.ld below is warp-collective
+      const bool ok = mbar_wait(&tfull[b], (i >> 1) & 1, kWaitNs);
+      if (__any_sync(0xffffffffu, !ok || s_fail)) {
+        s_fail = 1;
+        break;
+      }
+      tc_fence_after();
+      const int r = warp * 32 + lane;
+      const long long m = (long long)t * kBM + r;
+      const uint32_t trow = tmem + (uint32_t)(b * a.NT) + ((uint32_t)(warp * 32) << 16);
+      for (int j0 = 0; j0 < a.NT; j0 += 16) {
+        float v[16];
+        tmem_ld16(trow + (uint32_t)j0, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = j0 + j;
+          float yv = v[j] + sBias[n];
+          if (a.relu) yv = fmaxf(yv, 0.f);
+          v[j] = yv;
+        }
+        const long long o = m * a.N + j0;
+        if (j0 + 16 <= a.N) {
+          if (a.Y) {
+            uint32_t w[8];
+#pragma unroll
+            for (int qq = 0; qq < 8; ++qq) {
+              const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * qq], v[2 * qq + 1]);
+              w[qq] = *reinterpret_cast<const uint32_t*>(&h);
+            }
+            *reinterpret_cast<uint4*>(a.Y + o) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4*>(a.Y + o + 8) = make_uint4(w[4], w[5], w[6], w[7]);
+          }
+          if (a.Yf) {
+#pragma unroll
+            for (int qq = 0; qq < 4; ++qq)
+              *reinterpret_cast<float4*>(a.Yf + o + 4 * qq) =
+                  make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+          }
+        } else {
+          for (int j = 0; j < 16 && j0 + j < a.N; ++j) {
+            if (a.Y) a.Y[o + j] = __float2bfloat16_rn(v[j]);
+            if (a.Yf) a.Yf[o + j] = v[j];
+          }
+        }
+      }
+      tc_fence_before();
+      kwtma::mbar_arrive(&tempty[b]);
+    }
+  }
+  __syncthreads();
+  if (s_fail && tid == 0 && err) atomicCAS(err, 0, kErrUmmaTimeout);
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
 // elementwise kernels of the network (bf16 NHWC activations, f32 parameters)
 // ---------------------------------------------------------------------------
 // 2 x 2 average pooling, NHWC.
@@ -780,6 +1010,102 @@ int tile_cols(int n) {
   return r > kMaxNT ? kMaxNT : r;
 }
 
+// --- persistent TMA-fed convolution (k_conv_tma) ---------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn conv_encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+int conv_tma_smem(int C1, int NT, int stages) {
+  return 1024 + (int)((conv_tma_wbytes(C1, NT) + 1023) & ~1023u) + 1024 + stages * (int)kCtStage + 256;
+}
+
+int g_conv_tma_attr_dev = -1;
+constexpr int kConvTmaMaxSmem = 220 * 1024;
+
+// Run the convolution on k_conv_tma if it applies: one full-resolution input
+// of 16-channel groups, rows of a multiple of 128 pixels, at most 256 output
+// channels, weights and the halo ring within the shared-memory budget.
+// Returns KW_OK when launched, 1 when the caller should use k_umma.
+int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
+  static const bool enabled = [] {
+    const char* env = getenv("KWAVE_GB300_CONV_TMA");
+    return !(env && env[0] == '0');
+  }();
+  if (!enabled || u.C2 != 0 || u.W % 128 || u.C1 % 16 || u.NT > kMaxNT || u.N > u.NT) return 1;
+  // ring depth: the most CTAs per SM (shared memory, 512 TMEM columns, at
+  // most 4), then the deepest ring that keeps that count
+  const int by_tmem = 512 / (int)conv_tma_tmem_cols(u.NT);
+  int stages = 0, per_sm = 0;
+  for (int sdepth = 2; sdepth <= kCtMaxStages; ++sdepth) {
+    const int sm = conv_tma_smem(u.C1, u.NT, sdepth);
+    if (sm > kConvTmaMaxSmem) break;
+    const int k = std::min(std::min((227 * 1024) / (sm + 1024), by_tmem), 4);
+    if (k >= per_sm) {
+      per_sm = k;
+      stages = sdepth;
+    }
+  }
+  if (stages == 0 || per_sm == 0) return 1;
+  const int smem = conv_tma_smem(u.C1, u.NT, stages);
+  EncodeTiledFn fn = conv_encode_fn();
+  if (!fn) return 1;
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return umma_fail(KW_ERR_CUDA, "k_conv_tma: device query failed");
+  CUtensorMap map;
+  const cuuint64_t C = (cuuint64_t)u.C1, W = (cuuint64_t)u.W, H = (cuuint64_t)u.H;
+  cuuint64_t dims[4] = {C, W, H, (cuuint64_t)u.nb};
+  cuuint64_t strides[3] = {C * 2, W * C * 2, H * W * C * 2};
+  cuuint32_t box[4] = {8, (cuuint32_t)kHaloCols, 3, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(u.X1), dims, strides, box, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return 1;
+  if (g_conv_tma_attr_dev != dev) {
+    if (cudaFuncSetAttribute(k_conv_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvTmaMaxSmem) != cudaSuccess)
+      return umma_fail(KW_ERR_CUDA, "k_conv_tma: cannot set the shared-memory size");
+    g_conv_tma_attr_dev = dev;
+  }
+  ConvTmaArgs a;
+  a.nb = u.nb;
+  a.H = u.H;
+  a.W = u.W;
+  a.C1 = u.C1;
+  a.N = u.N;
+  a.NT = u.NT;
+  a.ntiles = u.nb * u.H * (u.W / 128);
+  a.stages = stages;
+  a.Wt = u.Wt;
+  a.bias = u.bias;
+  a.relu = u.relu;
+  a.Y = u.Y;
+  a.Yf = u.Yf;
+  const int grid = std::min(a.ntiles, nsm * per_sm);
+  k_conv_tma<<<grid, kCtThreads, smem, st>>>(map, a, kw_device_error_ptr());
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "k_conv_tma launch: %s", cudaGetErrorString(e));
+    return umma_fail(KW_ERR_CUDA, buf);
+  }
+  return KW_OK;
+}
+
 inline int grid1(long long n) {
   long long g = (n + 255) / 256;
   return (int)(g < 1 ? 1 : g > 4096 ? 4096 : g);
@@ -854,6 +1180,12 @@ int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32
   a.relu = relu;
   a.Y = static_cast<__nv_bfloat16*>(y);
   a.Yf = yf;
+  // halo tiles of one input: the persistent TMA-fed kernel when it applies
+  // (KWAVE_GB300_CONV_TMA=0: always k_umma)
+  if (a.mode == 3) {
+    const int rc = conv_tma_try(a, static_cast<cudaStream_t>(stream));
+    if (rc != 1) return rc;
+  }
   return umma_launch(a, dim3((cout + a.NT - 1) / a.NT, (a.M + kBM - 1) / kBM), static_cast<cudaStream_t>(stream));
 }
 

@@ -134,6 +134,30 @@ def test_conv3x3_halo_tiles(W, c1, c2, cout):
     assert e <= F32_TOL
 
 
+@pytest.mark.parametrize("nb,H,W,c1,cout", [(4, 64, 256, 32, 32), (2, 128, 128, 64, 64), (1, 20, 384, 16, 8),
+                                           (2, 40, 128, 32, 128)])
+def test_conv3x3_persistent_tma(nb, H, W, c1, cout):
+    """One full-resolution input on rows of a multiple of 128 pixels runs on
+    the persistent TMA-fed kernel (k_conv_tma): more tiles than CTAs (the
+    halo ring and the two TMEM accumulators wrap around), 1-4 channel groups,
+    8-128 output channels, bf16 and f32 outputs, against torch."""
+    import torch
+
+    from kwave_gb300 import unet_ops as U
+
+    x1 = bf((nb, H, W, c1), 40)
+    w = bf((cout, 9, c1), 41, 0.15)
+    bias = torch.randn(cout, generator=torch.Generator().manual_seed(42))
+    yb, yf = U.conv3x3(x1.cuda(), w.cuda(), bias.cuda(), relu=True,
+                       y=torch.empty((nb, H, W, cout), dtype=torch.bfloat16, device="cuda"),
+                       yf=torch.empty((nb, H, W, cout), dtype=torch.float32, device="cuda"))
+    torch.cuda.synchronize()
+    ref = ref_conv(x1, w, bias, relu=True)
+    e32, e16 = rel(yf, ref), rel(yb, ref)
+    print(f"persistent conv {nb}x{H}x{W} {c1}->{cout}: f32 {e32:.2e} bf16 {e16:.2e}")
+    assert e32 <= F32_TOL and e16 <= BF16_TOL
+
+
 def test_conv3x3_data_and_weight_gradients():
     """Data gradient as the flipped-weight convolution, weight and bias
     gradients, against torch autograd of the same convolution (concatenated
