@@ -831,7 +831,7 @@ def run_unet(args):
     """Throughput of the U-Net training step on the tensor cores: ``value`` =
     images per second; the roofline is the convolution flops of a step over
     its device time against the measured bf16 tensor peak, and the dominant
-    kernel (the tcgen05 convolution, ``k_umma``) is timed alone on the
+    kernel (the tcgen05 convolution, ``k_conv_tma``) is timed alone on the
     largest layer for its own fraction."""
     import torch
 
@@ -888,7 +888,7 @@ def run_unet(args):
             "config": {"workload": UNET_WORKLOAD, "batch": nb, "image": n},
             "step_roofline": {"bound": "tensor", "flops_per_step": flops, "achieved": step_tf, "peak": peak,
                               "unit": "TFLOP/s", "frac": step_tf / peak, "peak_source": "measured" if peaks else "fallback"},
-            "roofline": {"bound": "tensor", "kernel": "k_umma (conv3x3 32->32, 16 x 256^2)", "achieved": k_tf,
+            "roofline": {"bound": "tensor", "kernel": "k_conv_tma (conv3x3 32->32, 16 x 256^2)", "achieved": k_tf,
                          "peak": peak, "unit": "TFLOP/s", "frac": k_tf / peak, "traffic": None,
                          "kernel_ms": kms},
             "clocks": clk.summary()}
