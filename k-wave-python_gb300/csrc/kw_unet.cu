@@ -590,13 +590,17 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 // last MMAs before the CTA frees its TMEM.
 constexpr int kCtThreads = 192;
 constexpr int kCtMaxStages = 4;
-constexpr uint32_t kCtGroup = 6272;          // one 8-channel halo box (3 x 130 x 16 = 6240 bytes), 128-byte aligned
-constexpr uint32_t kCtBox = 3 * kHaloCols * 16;
-constexpr uint32_t kCtStage = 2 * kCtGroup;  // 16 channels
+
+// One 8-channel halo box of a tile of `rows` image rows: (rows + 2) x 130
+// pixels x 16 bytes; its stride in a stage rounded up to 128 bytes.  A stage
+// holds 16 channels (two boxes).
+__host__ __device__ inline uint32_t conv_tma_box(int rows) { return (uint32_t)((rows + 2) * kHaloCols * 16); }
+__host__ __device__ inline uint32_t conv_tma_group(int rows) { return (conv_tma_box(rows) + 127u) & ~127u; }
 
 struct ConvTmaArgs {
   int nb, H, W, C1, N, NT;  // NT: N rounded up to 16 (one column tile)
-  int ntiles;               // nb * H * W / 128
+  int rows;                 // image rows per tile (1 or 2; H % rows == 0)
+  int ntiles;               // nb * (H / rows) * (W / 128)
   int stages;               // depth of the halo ring (2..kCtMaxStages)
   const __nv_bfloat16* Wt;  // [N][9][C1]
   const float* bias;
@@ -607,8 +611,9 @@ struct ConvTmaArgs {
 
 __host__ __device__ inline uint32_t conv_tma_wbytes(int C1, int NT) { return (uint32_t)(9 * C1 * NT * 2); }
 
-__host__ __device__ inline uint32_t conv_tma_tmem_cols(int NT) {
-  const int c = 2 * NT;
+// two tiles' accumulators of `rows` x NT columns
+__host__ __device__ inline uint32_t conv_tma_tmem_cols(int NT, int rows) {
+  const int c = 2 * rows * NT;
   return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
 }
 
@@ -618,11 +623,12 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int groups = a.C1 / 16;
   const uint32_t wbytes = conv_tma_wbytes(a.C1, a.NT);
-  const int S = a.stages;
+  const int S = a.stages, R = a.rows;
+  const uint32_t gstride = conv_tma_group(R), stage_bytes = 2 * gstride;
   unsigned char* sW = base;
   float* sBias = reinterpret_cast<float*>(base + ((wbytes + 1023) & ~1023u));
   unsigned char* sH = reinterpret_cast<unsigned char*>(sBias) + 1024;
-  uint64_t* full = reinterpret_cast<uint64_t*>(sH + S * kCtStage);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sH + S * stage_bytes);
   uint64_t* empty = full + S;
   uint64_t* tfull = empty + S;
   uint64_t* tempty = tfull + 2;
@@ -631,7 +637,7 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
   __shared__ volatile int s_fail;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint32_t ncols = conv_tma_tmem_cols(a.NT);
+  const uint32_t ncols = conv_tma_tmem_cols(a.NT, R);
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
@@ -669,8 +675,9 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
       // producer, TMA: two 4-D boxes per stage
       int q = 0;
       for (int t = blockIdx.x; t < a.ntiles && !s_fail; t += gridDim.x) {
-        const int seg = t % segs, row = t / segs;
-        const int y = row % a.H, b = row / a.H;
+        const int seg = t % segs, blk = t / segs;
+        const int hb = a.H / R;
+        const int y = (blk % hb) * R, b = blk / hb;
         for (int c = 0; c < groups; ++c, ++q) {
           const int s = q % S;
           if (q >= S && !mbar_wait(&empty[s], ((q / S) - 1) & 1, kWaitNs)) {
@@ -678,9 +685,9 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
             break;
           }
           if (s_fail) break;
-          kwtma::mbar_arrive_expect_tx(&full[s], 2 * kCtBox);
-          kwtma::tma_load_4d(sH + s * kCtStage, &xmap, c * 16, seg * 128 - 1, y - 1, b, &full[s]);
-          kwtma::tma_load_4d(sH + s * kCtStage + kCtGroup, &xmap, c * 16 + 8, seg * 128 - 1, y - 1, b, &full[s]);
+          kwtma::mbar_arrive_expect_tx(&full[s], 2 * conv_tma_box(R));
+          kwtma::tma_load_4d(sH + s * stage_bytes, &xmap, c * 16, seg * 128 - 1, y - 1, b, &full[s]);
+          kwtma::tma_load_4d(sH + s * stage_bytes + gstride, &xmap, c * 16 + 8, seg * 128 - 1, y - 1, b, &full[s]);
         }
       }
       // the last use of each stage: its copies must have landed before the CTA ends
@@ -699,7 +706,7 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
           break;
         }
         tc_fence_after();
-        const uint32_t acc = tmem + (uint32_t)(b * a.NT);
+        const uint32_t acc = tmem + (uint32_t)(b * R * a.NT);
         bool ok = true;
         for (int c = 0; c < groups; ++c, ++q) {
           const int s = q % S;
@@ -708,13 +715,16 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
             break;
           }
           tc_fence_after();
-          const uint32_t ab = smem_u32(sH + s * kCtStage);
+          const uint32_t ab = smem_u32(sH + s * stage_bytes);
           const uint32_t bb = smem_u32(sW + (uint32_t)c * 18 * a.NT * 16);
+          // output row rr of the tile: halo rows rr .. rr + 2, accumulator rr
+          for (int rr = 0; rr < R; ++rr) {
 #pragma unroll
-          for (int tap = 0; tap < 9; ++tap) {
-            const uint32_t aoff = (uint32_t)(((tap / 3) * kHaloCols + (tap % 3)) * 16);
-            umma_bf16(acc, smem_desc(ab + aoff, kCtGroup, 128), smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128),
-                      idesc, (c | tap) != 0);
+            for (int tap = 0; tap < 9; ++tap) {
+              const uint32_t aoff = (uint32_t)(((tap / 3 + rr) * kHaloCols + (tap % 3)) * 16);
+              umma_bf16(acc + (uint32_t)(rr * a.NT), smem_desc(ab + aoff, gstride, 128),
+                        smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128), idesc, (c | tap) != 0);
+            }
           }
           umma_commit(&empty[s]);
         }
@@ -741,40 +751,45 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
       }
       tc_fence_after();
       const int r = warp * 32 + lane;
-      const long long m = (long long)t * kBM + r;
-      const uint32_t trow = tmem + (uint32_t)(b * a.NT) + ((uint32_t)(warp * 32) << 16);
-      for (int j0 = 0; j0 < a.NT; j0 += 16) {
-        float v[16];
-        tmem_ld16(trow + (uint32_t)j0, v);
+      const int seg = t % segs, blk = t / segs;
+      const int hb = a.H / R;
+      const int y0 = (blk % hb) * R, bimg = blk / hb;
+      for (int rr = 0; rr < R; ++rr) {
+        const long long m = ((long long)(bimg * a.H + y0 + rr) * a.W + seg * 128) + r;
+        const uint32_t trow = tmem + (uint32_t)((b * R + rr) * a.NT) + ((uint32_t)(warp * 32) << 16);
+        for (int j0 = 0; j0 < a.NT; j0 += 16) {
+          float v[16];
+          tmem_ld16(trow + (uint32_t)j0, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int n = j0 + j;
-          float yv = v[j] + sBias[n];
-          if (a.relu) yv = fmaxf(yv, 0.f);
-          v[j] = yv;
-        }
-        const long long o = m * a.N + j0;
-        if (j0 + 16 <= a.N) {
-          if (a.Y) {
-            uint32_t w[8];
+          for (int j = 0; j < 16; ++j) {
+            const int n = j0 + j;
+            float yv = v[j] + sBias[n];
+            if (a.relu) yv = fmaxf(yv, 0.f);
+            v[j] = yv;
+          }
+          const long long o = m * a.N + j0;
+          if (j0 + 16 <= a.N) {
+            if (a.Y) {
+              uint32_t w[8];
 #pragma unroll
-            for (int qq = 0; qq < 8; ++qq) {
-              const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * qq], v[2 * qq + 1]);
-              w[qq] = *reinterpret_cast<const uint32_t*>(&h);
+              for (int qq = 0; qq < 8; ++qq) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * qq], v[2 * qq + 1]);
+                w[qq] = *reinterpret_cast<const uint32_t*>(&h);
+              }
+              *reinterpret_cast<uint4*>(a.Y + o) = make_uint4(w[0], w[1], w[2], w[3]);
+              *reinterpret_cast<uint4*>(a.Y + o + 8) = make_uint4(w[4], w[5], w[6], w[7]);
             }
-            *reinterpret_cast<uint4*>(a.Y + o) = make_uint4(w[0], w[1], w[2], w[3]);
-            *reinterpret_cast<uint4*>(a.Y + o + 8) = make_uint4(w[4], w[5], w[6], w[7]);
-          }
-          if (a.Yf) {
+            if (a.Yf) {
 #pragma unroll
-            for (int qq = 0; qq < 4; ++qq)
-              *reinterpret_cast<float4*>(a.Yf + o + 4 * qq) =
-                  make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
-          }
-        } else {
-          for (int j = 0; j < 16 && j0 + j < a.N; ++j) {
-            if (a.Y) a.Y[o + j] = __float2bfloat16_rn(v[j]);
-            if (a.Yf) a.Yf[o + j] = v[j];
+              for (int qq = 0; qq < 4; ++qq)
+                *reinterpret_cast<float4*>(a.Yf + o + 4 * qq) =
+                    make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+            }
+          } else {
+            for (int j = 0; j < 16 && j0 + j < a.N; ++j) {
+              if (a.Y) a.Y[o + j] = __float2bfloat16_rn(v[j]);
+              if (a.Yf) a.Yf[o + j] = v[j];
+            }
           }
         }
       }
@@ -1029,8 +1044,8 @@ EncodeTiledFn conv_encode_fn() {
   return fn;
 }
 
-int conv_tma_smem(int C1, int NT, int stages) {
-  return 1024 + (int)((conv_tma_wbytes(C1, NT) + 1023) & ~1023u) + 1024 + stages * (int)kCtStage + 256;
+int conv_tma_smem(int C1, int NT, int stages, int rows) {
+  return 1024 + (int)((conv_tma_wbytes(C1, NT) + 1023) & ~1023u) + 1024 + stages * 2 * (int)conv_tma_group(rows) + 256;
 }
 
 int g_conv_tma_attr_dev = -1;
@@ -1048,10 +1063,13 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
   if (!enabled || u.C2 != 0 || u.W % 128 || u.C1 % 16 || u.NT > kMaxNT || u.N > u.NT) return 1;
   // ring depth: the most CTAs per SM (shared memory, 512 TMEM columns, at
   // most 4), then the deepest ring that keeps that count
-  const int by_tmem = 512 / (int)conv_tma_tmem_cols(u.NT);
+  // tiles of two image rows where the four accumulators fit TMEM: each input
+  // row is staged for two output rows instead of three
+  const int rows = (u.H % 2 == 0 && 4 * u.NT <= 512) ? 2 : 1;
+  const int by_tmem = 512 / (int)conv_tma_tmem_cols(u.NT, rows);
   int stages = 0, per_sm = 0;
   for (int sdepth = 2; sdepth <= kCtMaxStages; ++sdepth) {
-    const int sm = conv_tma_smem(u.C1, u.NT, sdepth);
+    const int sm = conv_tma_smem(u.C1, u.NT, sdepth, rows);
     if (sm > kConvTmaMaxSmem) break;
     const int k = std::min(std::min((227 * 1024) / (sm + 1024), by_tmem), 4);
     if (k >= per_sm) {
@@ -1060,7 +1078,7 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
     }
   }
   if (stages == 0 || per_sm == 0) return 1;
-  const int smem = conv_tma_smem(u.C1, u.NT, stages);
+  const int smem = conv_tma_smem(u.C1, u.NT, stages, rows);
   EncodeTiledFn fn = conv_encode_fn();
   if (!fn) return 1;
   int dev = 0, nsm = 0;
@@ -1070,7 +1088,7 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
   const cuuint64_t C = (cuuint64_t)u.C1, W = (cuuint64_t)u.W, H = (cuuint64_t)u.H;
   cuuint64_t dims[4] = {C, W, H, (cuuint64_t)u.nb};
   cuuint64_t strides[3] = {C * 2, W * C * 2, H * W * C * 2};
-  cuuint32_t box[4] = {8, (cuuint32_t)kHaloCols, 3, 1};
+  cuuint32_t box[4] = {8, (cuuint32_t)kHaloCols, (cuuint32_t)(rows + 2), 1};
   cuuint32_t estr[4] = {1, 1, 1, 1};
   if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(u.X1), dims, strides, box, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1088,7 +1106,8 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
   a.C1 = u.C1;
   a.N = u.N;
   a.NT = u.NT;
-  a.ntiles = u.nb * u.H * (u.W / 128);
+  a.rows = rows;
+  a.ntiles = u.nb * (u.H / rows) * (u.W / 128);
   a.stages = stages;
   a.Wt = u.Wt;
   a.bias = u.bias;

@@ -135,12 +135,14 @@ def test_conv3x3_halo_tiles(W, c1, c2, cout):
 
 
 @pytest.mark.parametrize("nb,H,W,c1,cout", [(4, 64, 256, 32, 32), (2, 128, 128, 64, 64), (1, 20, 384, 16, 8),
-                                           (2, 40, 128, 32, 128)])
+                                           (2, 40, 128, 32, 128), (3, 7, 128, 16, 16), (1, 9, 256, 32, 160)])
 def test_conv3x3_persistent_tma(nb, H, W, c1, cout):
     """One full-resolution input on rows of a multiple of 128 pixels runs on
     the persistent TMA-fed kernel (k_conv_tma): more tiles than CTAs (the
-    halo ring and the two TMEM accumulators wrap around), 1-4 channel groups,
-    8-128 output channels, bf16 and f32 outputs, against torch."""
+    halo ring and the two TMEM accumulators wrap around), tiles of two image
+    rows (even heights, up to 128 output channels) and of one (odd heights,
+    160 channels), 1-4 channel groups, 8-160 output channels, bf16 and f32
+    outputs, against torch."""
     import torch
 
     from kwave_gb300 import unet_ops as U
