@@ -571,17 +571,20 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 // input (no concatenation) whose weights fit shared memory, restructured so
 // that staging, tensor-core work and the epilogue overlap:
 //   * the CTA is persistent over tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-//     (a tile: 128 pixels of one image row, all output channels);
+//     (a tile: 128 pixels of a.rows = 1 or 2 image rows, all output
+//     channels; two rows stage each input row for two outputs instead of
+//     three);
 //   * the weights of all input channels stay in shared memory for the whole
 //     kernel, in the B layout of mode 3 ([16-channel group][tap][8-channel
 //     half][output channel][8 channels]);
 //   * warp 4 (one lane) is the producer: per 16-channel group of a tile it
-//     loads the 3 x 130-pixel halo with two 4-D TMA boxes of 8 channels
+//     loads the (rows + 2) x 130-pixel halo with two 4-D TMA boxes of 8 channels
 //     (tensor map over the NHWC input, zero fill outside the image) into a
 //     ring of a.stages stages (chosen per launch), completion on full[s];
-//   * warp 5 (one lane) issues the nine tcgen05.mma per group into one of two
-//     TMEM accumulators, commits each group to empty[s] (the producer may
-//     refill the stage) and each finished tile to tfull[b];
+//   * warp 5 (one lane) issues the nine tcgen05.mma per group and output row
+//     (row rr reads the halo from row rr on) into the tile's accumulators in
+//     one of two TMEM buffers, commits each group to empty[s] (the producer
+//     may refill the stage) and each finished tile to tfull[b];
 //   * warps 0-3 read accumulator b (warp w: TMEM lanes 32w..32w+31), apply
 //     bias and ReLU, store bf16 and/or f32 rows, and arrive on tempty[b] so
 //     that the tile after next may overwrite it.
