@@ -848,6 +848,16 @@ static int rows_class(int stage) {
   }
 }
 
+// The adjoint stages run on the register row kernels where the plan's rows
+// do (KWAVE_GB300_ADJ_GENERIC=1: on the generic row kernels).
+static bool adjoint_rows_reg() {
+  static const bool on = [] {
+    const char* e = getenv("KWAVE_GB300_ADJ_GENERIC");
+    return !(e && e[0] == '1');
+  }();
+  return on;
+}
+
 static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cudaStream_t st) {
   int crc = check_rows(p, stage, init);
   if (crc) return crc;
@@ -870,7 +880,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   P.init_r2c = p->init_r2c;
   if (p->rec_list) {
     kw_plan::LaunchRec r{};
-    r.kind = (p->rows_reg && stage < ST_ADJ_A) ? 2 : 0;
+    r.kind = (p->rows_reg && (stage < ST_ADJ_A || adjoint_rows_reg())) ? 2 : 0;
     r.rp = P;
     r.gx = (p->nrows + p->R - 1) / p->R;
     r.gy = r.gz = 1;
@@ -881,7 +891,7 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
   size_t slot = 0;
   int rc = ev_begin(p, st, &slot);
   if (rc) return rc;
-  if (p->rows_reg && stage < ST_ADJ_A) {
+  if (p->rows_reg && (stage < ST_ADJ_A || adjoint_rows_reg())) {
     P.R = p->rows_R;
     P.ex_stride = p->rows_RS;
     // the power-law density stage keeps the divergence in shared memory (one

@@ -33,10 +33,12 @@ static cudaError_t kw_rows_v2_attr_a(int m) {
 
 cudaError_t kw_rows_v2_attr(int m) {
   cudaError_t e = kw_rows_v2_attr_a(m);
-  return e == cudaSuccess ? kw_rows_v2_attr_b(m) : e;
+  if (e == cudaSuccess) e = kw_rows_v2_attr_b(m);
+  return e == cudaSuccess ? kw_rows_v2_attr_c(m) : e;
 }
 
 cudaError_t kw_rows_v2_launch(int m, int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
+  if (stage >= ST_ADJ_A) return kw_rows_v2_launch_c(m, stage, grid, smem, st, Q);
   if (stage != ST_INIT && stage != ST_U && stage != ST_RHO) return kw_rows_v2_launch_b(m, stage, grid, smem, st, Q);
 #define KW_R(E, P) rows_a_launch<E, P>(stage, grid, smem, st, Q)
   KW_V2_SWITCH(m, KW_R)

@@ -156,6 +156,29 @@ struct RowCtx {
       out[en.z] = val;
     }
   }
+
+  // v += S^T r at this row's sensor points (binary sensor: one slot per grid
+  // point; r is time-major in rec[0], row kw_rec_row(Q))
+  __device__ __forceinline__ void add_residual(float2 (&v)[E]) const {
+    const int rr = kw_rec_row(Q);
+    const float* res = Q.rec[0];
+    if (res == nullptr || rr < 0 || Q.sens_row_ptr == nullptr || !ok) return;
+    const int e0 = Q.sens_row_ptr[grow], e1 = Q.sens_row_ptr[grow + 1];
+    const float* in = res + (long long)rr * Q.nslots;
+    for (int e = e0; e < e1; ++e) {
+      const int4 en = Q.sens_ent[e];
+      const int n = en.y >> 1;
+      if ((n % P) != t) continue;
+      const int jj = n / P;
+      const float val = in[en.z];
+#pragma unroll
+      for (int j = 0; j < E; ++j)
+        if (j == jj) {
+          float& f = (en.y & 1) ? v[j].y : v[j].x;
+          f = __fadd_rn(f, val);
+        }
+    }
+  }
 };
 
 // velocity on the pressure grid, Re F^-1[e^{-i k d/2} F[u_i]] (kspace_solver.py:740-743)
@@ -566,6 +589,106 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
     return;
   }
 
+  if constexpr (STAGE >= ST_ADJ_A) {
+    // transposed step of the lossless, source-free loop: the arithmetic of
+    // the generic row kernels' adjoint stages (kw_generic.cuh: adjoint_body),
+    // on register-resident rows
+    if constexpr (STAGE == ST_ADJ_A || STAGE == ST_ADJ_D) {
+      float2 lp[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) lp[j] = c.ok ? ld2(Q.p, c.rbase + t + P * j) : make_float2(0.f, 0.f);
+      c.add_residual(lp);
+      for (int a = 0; a < D; ++a) {
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int n = t + P * j;
+          const uint32_t i = c.rbase + n;
+          v[j] = make_float2(0.f, 0.f);
+          if (!c.ok) continue;
+          if constexpr (STAGE == ST_ADJ_A) {
+            if (a == 0 && Q.gacc) {
+              const float2 fs = ld2(Q.fsum, i), ga = ld2(Q.gacc, i);
+              st2(Q.gacc, i, make_float2(__fmaf_rn(fs.x, lp[j].x, ga.x), __fmaf_rn(fs.y, lp[j].y, ga.y)));
+            }
+            const float2 cc = fld2(Q.c0, Q.c0_s, i);
+            const float2 r0v = fld2(Q.rho0, Q.rho0_s, i);
+            const float2 pm = c.pml2(Q.pml[a], a, n);
+            const float2 rho = ld2(Q.rho[a], i);
+            const float c2x = __fmul_rn(cc.x, cc.x), c2y = __fmul_rn(cc.y, cc.y);
+            const float bx = __fmul_rn(Q.dt, r0v.x), by = __fmul_rn(Q.dt, r0v.y);
+            const float lrx = __fadd_rn(rho.x, __fmul_rn(c2x, lp[j].x));
+            const float lry = __fadd_rn(rho.y, __fmul_rn(c2y, lp[j].y));
+            st2(Q.rho[a], i, make_float2(__fmul_rn(__fmul_rn(pm.x, pm.x), lrx), __fmul_rn(__fmul_rn(pm.y, pm.y), lry)));
+            v[j] = make_float2(__fmul_rn(__fmul_rn(bx, pm.x), lrx), __fmul_rn(__fmul_rn(by, pm.y), lry));
+          } else {
+            if (a == 0) st2(Q.p, i, lp[j]);
+            const float2 dtr = fld2(Q.dtrsg[a], Q.dtrsg_s[a], i);
+            const float2 u = ld2(Q.u[a], i);
+            v[j] = make_float2(__fmul_rn(__fmul_rn(dtr.x, 0.5f), u.x), __fmul_rn(__fmul_rn(dtr.y, 0.5f), u.y));
+          }
+        }
+        c.r2c(v, Q.S[a]);
+      }
+    } else if constexpr (STAGE == ST_ADJ_B) {
+      for (int a = 0; a < D; ++a) {
+        c.c2r(Q.S[a], v);
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int n = t + P * j;
+          const uint32_t i = c.rbase + n;
+          if (!c.ok) continue;
+          const float2 sg = c.pml2(Q.pmlsg[a], a, n);
+          const float2 u = ld2(Q.u[a], i);
+          const float2 dtr = fld2(Q.dtrsg[a], Q.dtrsg_s[a], i);
+          const float lux = __fadd_rn(u.x, v[j].x), luy = __fadd_rn(u.y, v[j].y);
+          st2(Q.u[a], i, make_float2(__fmul_rn(__fmul_rn(sg.x, sg.x), lux), __fmul_rn(__fmul_rn(sg.y, sg.y), luy)));
+          v[j] = make_float2(__fmul_rn(__fmul_rn(dtr.x, sg.x), lux), __fmul_rn(__fmul_rn(dtr.y, sg.y), luy));
+        }
+        c.r2c(v, Q.S[a]);
+      }
+    } else {
+      // ST_ADJ_C / ST_ADJ_E: sum_i F^-1 S_i
+      float2 sum[E];
+      for (int a = 0; a < D; ++a) {
+        c.c2r(Q.S[a], v);
+#pragma unroll
+        for (int j = 0; j < E; ++j)
+          sum[j] = a == 0 ? v[j] : make_float2(__fadd_rn(sum[j].x, v[j].x), __fadd_rn(sum[j].y, v[j].y));
+      }
+      if (c.ok) {
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const uint32_t i = c.rbase + t + P * j;
+          if constexpr (STAGE == ST_ADJ_C) {
+            st2(Q.p, i, sum[j]);
+          } else {
+            const float2 cc = fld2(Q.c0, Q.c0_s, i);
+            const float denx = __fmul_rn(__fmul_rn(cc.x, cc.x), (float)D);
+            const float deny = __fmul_rn(__fmul_rn(cc.y, cc.y), (float)D);
+            const float2 pv = ld2(Q.p, i);
+            float accx = pv.x, accy = pv.y;
+            float2 lr = make_float2(0.f, 0.f);
+            for (int a = 0; a < D; ++a) {
+              const float2 rho = ld2(Q.rho[a], i);
+              accx = __fadd_rn(accx, __fdiv_rn(rho.x, denx));
+              accy = __fadd_rn(accy, __fdiv_rn(rho.y, deny));
+              lr = a == 0 ? rho : make_float2(__fadd_rn(lr.x, rho.x), __fadd_rn(lr.y, rho.y));
+            }
+            st2(Q.p, i, make_float2(__fsub_rn(accx, sum[j].x), __fsub_rn(accy, sum[j].y)));
+            if (Q.gacc) {
+              const float2 p0 = ld2(Q.p0, i), ga = ld2(Q.gacc, i);
+              const float ovx = __fdiv_rn(__fmul_rn(p0.x, lr.x), __fmul_rn(denx, __fmul_rn(cc.x, cc.x)));
+              const float ovy = __fdiv_rn(__fmul_rn(p0.y, lr.y), __fmul_rn(deny, __fmul_rn(cc.y, cc.y)));
+              st2(Q.gacc, i, make_float2(__fmul_rn(__fmul_rn(2.f, cc.x), __fsub_rn(ga.x, ovx)),
+                                         __fmul_rn(__fmul_rn(2.f, cc.y), __fsub_rn(ga.y, ovy))));
+            }
+          }
+        }
+      }
+    }
+    return;
+  }
+
   if constexpr (STAGE == ST_EOS) {
   // p = c0^2 (rho + tau F^-1[nabla1 F[rho0 div]] - eta F^-1[nabla2 F[rho]] + B/A rho^2 / (2 rho0))
   float2 w[E];
@@ -635,3 +758,6 @@ static cudaError_t rows_v2_attr_stage() {
 // second stage group (kw_rows_reg2.cu)
 cudaError_t kw_rows_v2_attr_b(int m);
 cudaError_t kw_rows_v2_launch_b(int m, int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q);
+// third stage group: the adjoint stages (kw_rows_reg3.cu)
+cudaError_t kw_rows_v2_attr_c(int m);
+cudaError_t kw_rows_v2_launch_c(int m, int stage, dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q);

@@ -18,7 +18,7 @@ INCLUDE = PKG_DIR.parent.parent / "include"
 BUILD_DIR = PKG_DIR.parent / "_build"
 LIB = PKG_DIR / "libkwave_gb300.so"
 SOURCES = ["kw_kernels.cu", "kw_generic_fft2.cu", "kw_axis_tma.cu", "kw_axis_tma_plain.cu", "kw_axis_tma_ops.cu", "kw_axis_tma_ops2.cu",
-           "kw_rows_reg.cu", "kw_rows_reg2.cu", "kw_rows_tma.cu", "kw_plan.cu", "kw_noalloc.cu", "kw_unet.cu"]
+           "kw_rows_reg.cu", "kw_rows_reg2.cu", "kw_rows_reg3.cu", "kw_rows_tma.cu", "kw_plan.cu", "kw_noalloc.cu", "kw_unet.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "--extended-lambda"]
 
