@@ -41,9 +41,20 @@ static EncodeTiledFn encode_fn() {
 // Tensor-map storage for one plan: 2 axes x 4 buffers.
 struct KwTmaPlan {
   TmaMaps maps[2];
+  bool small[2] = {false, false};  // operator passes along the axis on small tiles
 };
 
 void* kw_tma_plan_create() { return new KwTmaPlan(); }
+void kw_tma_set_small(void* h, int axis, bool small) { static_cast<KwTmaPlan*>(h)->small[axis] = small; }
+
+// Small tiles for an operator pass of length n over ncols columns (one outer
+// block) when the normal tile width gives fewer tiles than SMs.
+bool kw_tma_small_wanted(int n, int ncols, int nsm) {
+  int E, P;
+  if (!kw_tma_small_ok(n, KK_GEN) || !kw_tma_shape(n, KK_GEN, &E, &P)) return false;
+  const int T = kw_tma_tile_cols(n, P, 0, KK_GEN);
+  return (ncols + T - 1) / T < nsm;
+}
 void kw_tma_plan_destroy(void* h) { delete static_cast<KwTmaPlan*>(h); }
 
 // Describe buffer `b` for a pass along `axis`: a 3-D tensor of 8-byte elements
@@ -57,7 +68,7 @@ bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long 
   int Ek, Pk;
   if (!kw_tma_shape(n, kind, &Ek, &Pk)) return false;
   (void)P;
-  const int T = kw_tma_tile_cols(n, Pk, axis, kind);
+  const int T = kw_tma_tile_cols(n, Pk, axis, kind, tp->small[axis]);
   cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)n, (cuuint64_t)nouter};
   cuuint64_t strides[2] = {(cuuint64_t)xs * 8, (cuuint64_t)(nouter > 1 ? os : xs * n) * 8};
   cuuint32_t box[3] = {(cuuint32_t)T, (cuuint32_t)(n < 256 ? n : 256), 1};
@@ -92,13 +103,13 @@ static int ops_kind(const AxisParams& A) {
   return nab ? KK_NAB : KK_GEN;
 }
 
-cudaError_t kw_tma_attr(int n, int axis) {
-  cudaError_t e = kw_tma_attr_plain(n, axis);
+cudaError_t kw_tma_attr(int n, int axis, bool small) {
+  cudaError_t e = kw_tma_attr_plain(n, axis, false);
   if (e != cudaSuccess || axis != 0) return e;
-  if ((e = kw_tma_attr_gen(n, 0)) != cudaSuccess) return e;
-  if ((e = kw_tma_attr_grad(n, 0)) != cudaSuccess) return e;
-  if ((e = kw_tma_attr_div(n, 0)) != cudaSuccess) return e;
-  return kw_tma_attr_nab(n, 0);
+  if ((e = kw_tma_attr_gen(n, 0, small)) != cudaSuccess) return e;
+  if ((e = kw_tma_attr_grad(n, 0, small)) != cudaSuccess) return e;
+  if ((e = kw_tma_attr_div(n, 0, small)) != cudaSuccess) return e;
+  return kw_tma_attr_nab(n, 0, small);
 }
 
 // Launch one persistent pass along `axis` (0: operator or plain pass along x;
@@ -109,7 +120,8 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
   int E, P;
   const int kind = A.mode < 2 ? KK_PLAIN : ops_kind(A);
   if (!kw_tma_shape(n, kind, &E, &P)) return cudaErrorInvalidValue;
-  const int T = kw_tma_tile_cols(n, P, axis, kind);
+  const bool small = tp->small[axis] && kind != KK_PLAIN;
+  const int T = kw_tma_tile_cols(n, P, axis, kind, small);
   TmaWork W;
   W.pdl = pdl;
   W.err = device_error_ptr();
@@ -129,19 +141,19 @@ cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm,
     W.nitems = ni;
     W.nunits = W.ntile * nouter;
   }
-  const int per_sm = kw_tma_per_sm(n, axis, kind);
+  const int per_sm = kw_tma_per_sm(n, axis, kind, small);
   const int grid = W.nunits < nsm * per_sm ? W.nunits : nsm * per_sm;
   W.st_tile = grid % W.ntile;
   W.st_outer = (grid / W.ntile) % W.nouter;
   W.st_b = grid / W.ntile / W.nouter;
-  const size_t smem = kw_tma_smem(n, E, P, axis, kind);
+  const size_t smem = kw_tma_smem(n, E, P, axis, kind, small);
   const TmaMaps& maps = tp->maps[axis];
   switch (kind) {
-    case KK_PLAIN: return kw_tma_launch_plain(n, axis, grid, smem, st, A, maps, W);
-    case KK_GRAD: return kw_tma_launch_grad(n, axis, grid, smem, st, A, maps, W);
-    case KK_DIV: return kw_tma_launch_div(n, axis, grid, smem, st, A, maps, W);
-    case KK_NAB: return kw_tma_launch_nab(n, axis, grid, smem, st, A, maps, W);
-    default: return kw_tma_launch_gen(n, axis, grid, smem, st, A, maps, W);
+    case KK_PLAIN: return kw_tma_launch_plain(n, axis, grid, smem, st, A, maps, W, false);
+    case KK_GRAD: return kw_tma_launch_grad(n, axis, grid, smem, st, A, maps, W, small);
+    case KK_DIV: return kw_tma_launch_div(n, axis, grid, smem, st, A, maps, W, small);
+    case KK_NAB: return kw_tma_launch_nab(n, axis, grid, smem, st, A, maps, W, small);
+    default: return kw_tma_launch_gen(n, axis, grid, smem, st, A, maps, W, small);
   }
 }
 

@@ -544,17 +544,23 @@ inline bool kw_tma_shape(int n, int kind, int* E, int* P) {
 // threads plus the producer warp) at three CTAs per SM, which leaves each
 // thread 128 registers; 512 and 1024 use 256 / P columns at one CTA per SM.
 inline bool kw_tma_narrow(int n, int axis, int kind) { return n <= 256; }
-inline int kw_tma_tile_cols(int n, int P, int axis, int kind) { return kw_tma_narrow(n, axis, kind) ? 128 / P : 256 / P; }
-inline int kw_tma_per_sm(int n, int axis, int kind) {
-  return (n == 256 && kind == KK_PLAIN) ? 2 : kw_tma_narrow(n, axis, kind) ? 3 : 1;
+// Small tiles (operator passes of lengths 128..512): one warp of consumers
+// (32 / P columns) at four CTAs per SM, for grids with too few columns to
+// give every SM a tile at the normal width (2-D grids up to 512 columns).
+inline bool kw_tma_small_ok(int n, int kind) { return kind != KK_PLAIN && (n == 128 || n == 256 || n == 512); }
+inline int kw_tma_tile_cols(int n, int P, int axis, int kind, bool small = false) {
+  return small ? 32 / P : kw_tma_narrow(n, axis, kind) ? 128 / P : 256 / P;
+}
+inline int kw_tma_per_sm(int n, int axis, int kind, bool small = false) {
+  return small ? 4 : (n == 256 && kind == KK_PLAIN) ? 2 : kw_tma_narrow(n, axis, kind) ? 3 : 1;
 }
 
 // Stages of the TMA ring (a third stage measured no faster for the plain passes).
 inline int kw_tma_stages(int n, int kind) { return 2; }
 #define KW_NST_S 2
 
-inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
-  const int T = kw_tma_tile_cols(n, P, axis, kind), RS = kw_tma_rs(n, E, T), NST = kw_tma_stages(n, kind);
+inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind, bool small = false) {
+  const int T = kw_tma_tile_cols(n, P, axis, kind, small), RS = kw_tma_rs(n, E, T), NST = kw_tma_stages(n, kind);
   const size_t nt = (n <= 512 && kind != KK_PLAIN) ? (size_t)n : 0;
   return sizeof(float2) * ((size_t)NST * n * T + (size_t)T * RS + 2 * (size_t)P * (E + 2) + 3 * nt) + sizeof(float) * nt +
          2 * NST * sizeof(uint64_t) + 16;
@@ -573,25 +579,40 @@ inline size_t kw_tma_smem(int n, int E, int P, int axis, int kind) {
     default: return cudaErrorInvalidValue;   \
   }
 
+// Small-tile instantiations (kw_tma_small_ok): T = 32 / P, 4 CTAs per SM.
+#define KW_TMA_SWITCH_SMALL(n, CALL)                 \
+  switch (n) {                                       \
+    case 128: return CALL(16, 8, KW_NST_S, 4, 4);    \
+    case 256: return CALL(16, 16, KW_NST_S, 4, 2);   \
+    case 512: return CALL(32, 16, 2, 4, 2);          \
+    default: return cudaErrorInvalidValue;           \
+  }
+
 // Attribute set-up and launch of one KIND (instantiated in the translation
 // unit that calls them).
 template <int KIND>
-cudaError_t kw_tma_attr_kind(int n, int axis) {
+cudaError_t kw_tma_attr_kind(int n, int axis, bool small) {
   int E, P;
   if (!kw_tma_shape(n, KIND, &E, &P)) return cudaErrorInvalidValue;
-  const int smem = (int)kw_tma_smem(n, E, P, axis, KIND);
+  const int smem = (int)kw_tma_smem(n, E, P, axis, KIND, small);
 #define KW_T(E_, P_, S_, B_, T_) \
   cudaFuncSetAttribute(k_axis_tma<E_, P_, S_, B_, T_, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+  if constexpr (KIND != KK_PLAIN) {
+    if (small) KW_TMA_SWITCH_SMALL(n, KW_T)
+  }
   KW_TMA_SWITCH(n, 0, KW_T)
 #undef KW_T
 }
 
 template <int KIND>
 cudaError_t kw_tma_launch_kind(int n, int axis, int grid, size_t smem, cudaStream_t st, const AxisParams& A,
-                               const TmaMaps& maps, const TmaWork& W) {
+                               const TmaMaps& maps, const TmaWork& W, bool small) {
 #define KW_T(E_, P_, S_, B_, T_)                                                                              \
   kwtma::launch_k(k_axis_tma<E_, P_, S_, B_, T_, KIND>, dim3(grid), dim3(T_ * P_ + 32), smem, st, W.pdl != 0, A, \
                   maps, W)
+  if constexpr (KIND != KK_PLAIN) {
+    if (small) KW_TMA_SWITCH_SMALL(n, KW_T)
+  }
   KW_TMA_SWITCH(n, 0, KW_T)
 #undef KW_T
 }
@@ -600,14 +621,14 @@ cudaError_t kw_tma_launch_kind(int n, int axis, int grid, size_t smem, cudaStrea
 // translation unit that instantiates that kind, so that the kinds compile in
 // parallel.
 #define KW_TMA_DECLARE_KIND(name)                                                                             \
-  cudaError_t kw_tma_attr_##name(int n, int axis);                                                            \
+  cudaError_t kw_tma_attr_##name(int n, int axis, bool small);                                                \
   cudaError_t kw_tma_launch_##name(int n, int axis, int grid, size_t smem, cudaStream_t st, const AxisParams& A, \
-                                   const TmaMaps& maps, const TmaWork& W);
+                                   const TmaMaps& maps, const TmaWork& W, bool small);
 #define KW_TMA_DEFINE_KIND(name, KIND)                                                                         \
-  cudaError_t kw_tma_attr_##name(int n, int axis) { return kw_tma_attr_kind<KIND>(n, axis); }                  \
+  cudaError_t kw_tma_attr_##name(int n, int axis, bool small) { return kw_tma_attr_kind<KIND>(n, axis, small); } \
   cudaError_t kw_tma_launch_##name(int n, int axis, int grid, size_t smem, cudaStream_t st, const AxisParams& A, \
-                                   const TmaMaps& maps, const TmaWork& W) {                                    \
-    return kw_tma_launch_kind<KIND>(n, axis, grid, smem, st, A, maps, W);                                      \
+                                   const TmaMaps& maps, const TmaWork& W, bool small) {                        \
+    return kw_tma_launch_kind<KIND>(n, axis, grid, smem, st, A, maps, W, small);                               \
   }
 KW_TMA_DECLARE_KIND(plain)
 KW_TMA_DECLARE_KIND(gen)

@@ -199,7 +199,10 @@ void* kw_tma_plan_create();
 void kw_tma_plan_destroy(void* h);
 bool kw_tma_supported(int n);
 bool kw_tma_encode(void* h, int axis, int b, void* base, int ncols, int n, long long xs, int nouter, long long os, int P);
-cudaError_t kw_tma_attr(int n, int axis);
+cudaError_t kw_tma_attr(int n, int axis, bool small);
+// operator passes along `axis` on small tiles (set before encoding the maps)
+void kw_tma_set_small(void* h, int axis, bool small);
+bool kw_tma_small_wanted(int n, int ncols, int nsm);
 // pdl != 0: launched as a programmatic dependent of the previous kernel of the
 // stream (its prologue overlaps that kernel's tail)
 cudaError_t kw_tma_launch(void* h, int axis, int n, int nouter, int nb, int nsm, cudaStream_t st, const AxisParams& A,

@@ -688,6 +688,14 @@ int32_t kw_plan_finalize(kw_plan* p) {
       if (!p->tma) p->tma = kw_tma_plan_create();
       int E, Pt;
       kw_reg_shape(p->N[a], &E, &Pt);
+      // 2-D grids whose operator passes would leave SMs without a tile at
+      // the normal tile width take the small tiles (KWAVE_GB300_SMALL_TILES=0: never)
+      static const bool small_on = [] {
+        const char* e = getenv("KWAVE_GB300_SMALL_TILES");
+        return !(e && e[0] == '0');
+      }();
+      const bool small = small_on && D == 2 && kw_tma_small_wanted(p->N[0], p->Hp, p->nsm);
+      kw_tma_set_small(p->tma, 0, small);
       bool ok = true;
       for (int b = 0; b < KW_NBUF; ++b) {
         if (!p->d_S[b]) continue;
@@ -699,7 +707,7 @@ int32_t kw_plan_finalize(kw_plan* p) {
           ok &= kw_tma_encode(p->tma, 0, b, p->d_S[b], p->Hp, p->N[0], p->Hp, 1, 0, Pt);
       }
       if (ok) {
-        CK(kw_tma_attr(p->N[a], D == 3 ? a : 0));
+        CK(kw_tma_attr(p->N[a], D == 3 ? a : 0, small));
         p->tma_axis[a] = true;
       }
     }
@@ -897,9 +905,6 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
     // the power-law density stage keeps the divergence in shared memory (one
     // float2 per thread and register pair)
     const bool dsm = stage == ST_RHO && p->g.absorb_mode == 1 && p->d_rhosum;
-    const size_t smem = sizeof(float2) * (2 * (size_t)p->Mfft + 1 + (size_t)p->rows_R * p->rows_RS +
-                                          (dsm ? (size_t)128 * p->rows_regE : 0));
-    const int grid = (p->nrows + p->rows_R - 1) / p->rows_R;
     const bool extra = P.srcp_on || P.srcu_on[0] || P.srcu_on[1] || P.srcu_on[2] || P.rec_us;
     if (stage == ST_U && !init && !extra && p->rows_tma) {
       if (p->wait_test) {
@@ -912,8 +917,11 @@ static int launch_rows(kw_plan* p, int stage, int init, int t, int write_p, cuda
       CK(kw_rows_tma_launch(p->Mfft, ST_RHO_PL, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
     else if (stage == ST_EOS && p->rows_tma)
       CK(kw_rows_tma_launch(p->Mfft, ST_EOS, p->nsm, st, P, kw_device_error_ptr(), pdl_ok(p)));
-    else
-      CK(kw_rows_v2_launch(p->Mfft, stage, dim3(grid), smem, st, P));
+    else {
+      const size_t smem = sizeof(float2) * (2 * (size_t)p->Mfft + 1 + (size_t)p->rows_R * p->rows_RS +
+                                            (dsm ? (size_t)128 * p->rows_regE : 0));
+      CK(kw_rows_v2_launch(p->Mfft, stage, dim3((p->nrows + p->rows_R - 1) / p->rows_R), smem, st, P));
+    }
   } else {
     const int grid = (p->nrows + p->R - 1) / p->R;
     CK(P.flen.n1 ? kw_rows_launch_1(dim3(grid), p->smem_rows, st, P) : kw_rows_launch_0(dim3(grid), p->smem_rows, st, P));

@@ -727,13 +727,15 @@ __global__ void __launch_bounds__(128, kw_rows_min_blocks(STAGE)) k_rows_v2(cons
 
 // Launch and attribute helpers for one stage (instantiated by the translation
 // unit that owns the stage: kw_rows_reg.cu or kw_rows_reg2.cu).
+// Q.R rows of P threads per block (128 threads, or fewer for small grids).
 template <int E, int P, int STAGE>
 static cudaError_t rows_v2_launch_stage(dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
   const bool extra = Q.srcp_on || Q.srcu_on[0] || Q.srcu_on[1] || Q.srcu_on[2] || Q.rec_us;
+  const dim3 block(Q.R * P);
   if (extra)
-    k_rows_v2<E, P, STAGE, true><<<grid, 128, smem, st>>>(Q);
+    k_rows_v2<E, P, STAGE, true><<<grid, block, smem, st>>>(Q);
   else
-    k_rows_v2<E, P, STAGE, false><<<grid, 128, smem, st>>>(Q);
+    k_rows_v2<E, P, STAGE, false><<<grid, block, smem, st>>>(Q);
   return cudaGetLastError();
 }
 

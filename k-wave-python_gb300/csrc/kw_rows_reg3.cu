@@ -8,7 +8,7 @@
 // EXTRA = false form of each stage is compiled.
 template <int E, int P, int STAGE>
 static cudaError_t adj_launch(dim3 grid, size_t smem, cudaStream_t st, const RowsParams& Q) {
-  k_rows_v2<E, P, STAGE, false><<<grid, 128, smem, st>>>(Q);
+  k_rows_v2<E, P, STAGE, false><<<grid, dim3(Q.R * P), smem, st>>>(Q);
   return cudaGetLastError();
 }
 
