@@ -316,6 +316,25 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(ms, device="cuda"):
+    """The largest of the ranks' timed-region lengths (all_reduce MAX over the
+    process group); ``ms`` itself outside a group of more than one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells, steps, ms_max, ws):
+    """Whole-job Mcell-steps/s of ``ws`` independent replicas of ``cells``
+    cells over ``steps`` steps, timed by the slowest rank."""
+    return ws * cells * steps / (ms_max / 1e3) / 1e6
+
+
 def cpu_baseline_sample(n=256, steps=1, warm=1):
     """Oracle (the reference's CPU implementation, restated) on the same
     workload: set-up and ``warm`` untimed steps (the first is the t=0 step),
@@ -451,13 +470,9 @@ def run_gb300(args):
     kcnt = (ctypes.c_int64 * 6)()
     K.check(lib.kw_plan_read_timing(plan.handle, kms, kcnt))
     K.check(lib.kw_plan_set_timing(plan.handle, 0))
-    ms_max = ms
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = max_over_ranks(ms)
     cells = int(np.prod(S.shape))
-    value = ws * cells * K_steps / (ms_max / 1e3) / 1e6
+    value = replica_throughput(cells, K_steps, ms_max, ws)
 
     # roofline of the dominant kernel class (algorithmic bytes / average launch time)
     names = K.KW_K_NAMES
