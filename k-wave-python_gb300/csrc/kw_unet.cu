@@ -577,12 +577,13 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 //   * the weights of all input channels stay in shared memory for the whole
 //     kernel, in the B layout of mode 3 ([16-channel group][tap][8-channel
 //     half][output channel][8 channels]);
-//   * warp 4 (one lane) is the producer: per 16-channel group of a tile it
-//     loads the (rows + 2) x 130-pixel halo with two 4-D TMA boxes of 8 channels
-//     (tensor map over the NHWC input, zero fill outside the image) into a
-//     ring of a.stages stages (chosen per launch), completion on full[s];
-//   * warp 5 (one lane) issues the nine tcgen05.mma per group and output row
-//     (row rr reads the halo from row rr on) into the tile's accumulators in
+//   * warp 4 (one lane) is the producer: per group of a.gc channels of a
+//     tile it loads the (rows + 2) x 130-pixel halo with one 4-D TMA box
+//     (tensor map over the NHWC input, whole pixels as swizzled rows, zero
+//     fill outside the image) into a ring of a.stages stages (chosen per
+//     launch), completion on full[s];
+//   * warp 5 (one lane) issues nine tcgen05.mma per 16 channels and output
+//     row (row rr reads the halo from row rr on) into the tile's accumulators in
 //     one of two TMEM buffers, commits each group to empty[s] (the producer
 //     may refill the stage) and each finished tile to tfull[b];
 //   * warps 0-3 read accumulator b (warp w: TMEM lanes 32w..32w+31), apply
@@ -594,15 +595,41 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 constexpr int kCtThreads = 192;
 constexpr int kCtMaxStages = 4;
 
-// One 8-channel halo box of a tile of `rows` image rows: (rows + 2) x 130
-// pixels x 16 bytes; its stride in a stage rounded up to 128 bytes.  A stage
-// holds 16 channels (two boxes).
-__host__ __device__ inline uint32_t conv_tma_box(int rows) { return (uint32_t)((rows + 2) * kHaloCols * 16); }
-__host__ __device__ inline uint32_t conv_tma_group(int rows) { return (conv_tma_box(rows) + 127u) & ~127u; }
+// A stage is the halo of one channel group of gc = 16, 32 or 64 channels for
+// a tile of `rows` image rows: (rows + 2) x 130 pixels of gc * 2 bytes, one
+// TMA box written in the K-major swizzled layout of that row width (32-, 64-
+// or 128-byte swizzle: each pixel is one row of the tensor-core operand, its
+// 16-byte chunks permuted by the shared-memory address bits of the row).  The
+// tensor cores apply the same permutation from the absolute address, so the
+// nine taps stay nine descriptor start addresses, whole pixel rows apart,
+// with base offset 0 (verified on the GPU for all three widths and row shifts
+// that are not multiples of the 8-row swizzle atom).  Stages start 1024-byte
+// aligned.
+__host__ __device__ inline uint32_t conv_tma_box(int rows, int gc) {
+  return (uint32_t)((rows + 2) * kHaloCols * gc * 2);
+}
+__host__ __device__ inline uint32_t conv_tma_stage(int rows, int gc) { return (conv_tma_box(rows, gc) + 1023u) & ~1023u; }
+// tcgen05 layout code of a K-major swizzle for rows of `rowbytes` bytes
+__host__ __device__ inline uint32_t conv_tma_layout(int rowbytes) {
+  return rowbytes == 128 ? 2u : rowbytes == 64 ? 4u : 6u;
+}
+
+// Shared-memory descriptor of a swizzled K-major operand (rows of rowbytes,
+// 8-row atoms rowbytes * 8 apart; LBO unused within the atom).
+__device__ __forceinline__ uint64_t smem_desc_swz(uint32_t addr, uint32_t rowbytes) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(((8 * rowbytes) >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)conv_tma_layout((int)rowbytes) << 61;
+  return d;
+}
 
 struct ConvTmaArgs {
   int nb, H, W, C1, N, NT;  // NT: N rounded up to 16 (one column tile)
   int rows;                 // image rows per tile (1 or 2; H % rows == 0)
+  int gc;                   // channels per stage (16, 32 or 64; C1 % gc == 0)
   int ntiles;               // nb * (H / rows) * (W / 128)
   int stages;               // depth of the halo ring (2..kCtMaxStages)
   const __nv_bfloat16* Wt;  // [N][9][C1]
@@ -624,10 +651,10 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
                                                          int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int groups = a.C1 / 16;
+  const int groups = a.C1 / a.gc, k16 = a.gc / 16;
   const uint32_t wbytes = conv_tma_wbytes(a.C1, a.NT);
   const int S = a.stages, R = a.rows;
-  const uint32_t gstride = conv_tma_group(R), stage_bytes = 2 * gstride;
+  const uint32_t rowbytes = (uint32_t)a.gc * 2, stage_bytes = conv_tma_stage(R, a.gc);
   unsigned char* sW = base;
   float* sBias = reinterpret_cast<float*>(base + ((wbytes + 1023) & ~1023u));
   unsigned char* sH = reinterpret_cast<unsigned char*>(sBias) + 1024;
@@ -656,7 +683,7 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
   }
   if (warp == 0) tmem_alloc(tslot, ncols);
   // weights of every 16-channel group: [c][tap][half][n][8 channels]
-  const int wrows = groups * 18 * a.NT;
+  const int wrows = (a.C1 / 16) * 18 * a.NT;  // every 16-channel chunk
   for (int q = tid; q < wrows; q += kCtThreads) {
     const int c = q / (18 * a.NT), r = q - c * 18 * a.NT;
     const int th = r / a.NT, n = r - th * a.NT;
@@ -688,9 +715,8 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
             break;
           }
           if (s_fail) break;
-          kwtma::mbar_arrive_expect_tx(&full[s], 2 * conv_tma_box(R));
-          kwtma::tma_load_4d(sH + s * stage_bytes, &xmap, c * 16, seg * 128 - 1, y - 1, b, &full[s]);
-          kwtma::tma_load_4d(sH + s * stage_bytes + gstride, &xmap, c * 16 + 8, seg * 128 - 1, y - 1, b, &full[s]);
+          kwtma::mbar_arrive_expect_tx(&full[s], conv_tma_box(R, a.gc));
+          kwtma::tma_load_4d(sH + s * stage_bytes, &xmap, c * a.gc, seg * 128 - 1, y - 1, b, &full[s]);
         }
       }
       // the last use of each stage: its copies must have landed before the CTA ends
@@ -719,14 +745,17 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
           }
           tc_fence_after();
           const uint32_t ab = smem_u32(sH + s * stage_bytes);
-          const uint32_t bb = smem_u32(sW + (uint32_t)c * 18 * a.NT * 16);
-          // output row rr of the tile: halo rows rr .. rr + 2, accumulator rr
+          // output row rr of the tile: halo rows rr .. rr + 2, accumulator rr;
+          // 16 channels per MMA, 32 bytes further along the pixel row
           for (int rr = 0; rr < R; ++rr) {
+            for (int kk = 0; kk < k16; ++kk) {
+              const uint32_t bb = smem_u32(sW + (uint32_t)(c * k16 + kk) * 18 * a.NT * 16);
 #pragma unroll
-            for (int tap = 0; tap < 9; ++tap) {
-              const uint32_t aoff = (uint32_t)(((tap / 3 + rr) * kHaloCols + (tap % 3)) * 16);
-              umma_bf16(acc + (uint32_t)(rr * a.NT), smem_desc(ab + aoff, gstride, 128),
-                        smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128), idesc, (c | tap) != 0);
+              for (int tap = 0; tap < 9; ++tap) {
+                const uint32_t aoff = (uint32_t)((tap / 3 + rr) * kHaloCols + (tap % 3)) * rowbytes + kk * 32;
+                umma_bf16(acc + (uint32_t)(rr * a.NT), smem_desc_swz(ab + aoff, rowbytes),
+                          smem_desc(bb + tap * 2 * a.NT * 16, a.NT * 16, 128), idesc, (c | kk | tap) != 0);
+              }
             }
           }
           umma_commit(&empty[s]);
@@ -1047,8 +1076,8 @@ EncodeTiledFn conv_encode_fn() {
   return fn;
 }
 
-int conv_tma_smem(int C1, int NT, int stages, int rows) {
-  return 1024 + (int)((conv_tma_wbytes(C1, NT) + 1023) & ~1023u) + 1024 + stages * 2 * (int)conv_tma_group(rows) + 256;
+int conv_tma_smem(int C1, int NT, int stages, int rows, int gc) {
+  return 1024 + (int)((conv_tma_wbytes(C1, NT) + 1023) & ~1023u) + 1024 + stages * (int)conv_tma_stage(rows, gc) + 256;
 }
 
 int g_conv_tma_attr_dev = -1;
@@ -1068,20 +1097,25 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
   // most 4), then the deepest ring that keeps that count
   // tiles of two image rows where the four accumulators fit TMEM: each input
   // row is staged for two output rows instead of three
-  const int rows = (u.H % 2 == 0 && 4 * u.NT <= 512) ? 2 : 1;
-  const int by_tmem = 512 / (int)conv_tma_tmem_cols(u.NT, rows);
+  // channels per stage: the widest swizzle row (64 channels = 128 bytes) that divides C1
+  const int gc = u.C1 % 64 == 0 ? 64 : u.C1 % 32 == 0 ? 32 : 16;
+  int rows = (u.H % 2 == 0 && 4 * u.NT <= 512) ? 2 : 1;
   int stages = 0, per_sm = 0;
-  for (int sdepth = 2; sdepth <= kCtMaxStages; ++sdepth) {
-    const int sm = conv_tma_smem(u.C1, u.NT, sdepth, rows);
-    if (sm > kConvTmaMaxSmem) break;
-    const int k = std::min(std::min((227 * 1024) / (sm + 1024), by_tmem), 4);
-    if (k >= per_sm) {
-      per_sm = k;
-      stages = sdepth;
+  for (; rows >= 1 && stages == 0; --rows) {
+    const int by_tmem = 512 / (int)conv_tma_tmem_cols(u.NT, rows);
+    for (int sdepth = 2; sdepth <= kCtMaxStages; ++sdepth) {
+      const int sm = conv_tma_smem(u.C1, u.NT, sdepth, rows, gc);
+      if (sm > kConvTmaMaxSmem) break;
+      const int k = std::min(std::min((227 * 1024) / (sm + 1024), by_tmem), 4);
+      if (k >= per_sm) {
+        per_sm = k;
+        stages = sdepth;
+      }
     }
+    if (stages) break;
   }
-  if (stages == 0 || per_sm == 0) return 1;
-  const int smem = conv_tma_smem(u.C1, u.NT, stages, rows);
+  if (stages == 0 || per_sm == 0 || rows < 1) return 1;
+  const int smem = conv_tma_smem(u.C1, u.NT, stages, rows, gc);
   EncodeTiledFn fn = conv_encode_fn();
   if (!fn) return 1;
   int dev = 0, nsm = 0;
@@ -1091,11 +1125,13 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
   const cuuint64_t C = (cuuint64_t)u.C1, W = (cuuint64_t)u.W, H = (cuuint64_t)u.H;
   cuuint64_t dims[4] = {C, W, H, (cuuint64_t)u.nb};
   cuuint64_t strides[3] = {C * 2, W * C * 2, H * W * C * 2};
-  cuuint32_t box[4] = {8, (cuuint32_t)kHaloCols, (cuuint32_t)(rows + 2), 1};
+  cuuint32_t box[4] = {(cuuint32_t)gc, (cuuint32_t)kHaloCols, (cuuint32_t)(rows + 2), 1};
   cuuint32_t estr[4] = {1, 1, 1, 1};
+  const CUtensorMapSwizzle swz = gc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : gc == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                                                                 : CU_TENSOR_MAP_SWIZZLE_32B;
   if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(u.X1), dims, strides, box, estr,
-         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+         CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+      CUDA_SUCCESS)
     return 1;
   if (g_conv_tma_attr_dev != dev) {
     if (cudaFuncSetAttribute(k_conv_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvTmaMaxSmem) != cudaSuccess)
@@ -1110,6 +1146,7 @@ int conv_tma_try(const UmmaArgs& u, cudaStream_t st) {
   a.N = u.N;
   a.NT = u.NT;
   a.rows = rows;
+  a.gc = gc;
   a.ntiles = u.nb * (u.H / rows) * (u.W / 128);
   a.stages = stages;
   a.Wt = u.Wt;
