@@ -127,6 +127,19 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// 16 consecutive f32 columns of this thread's TMEM lane into v[0..15]
+// without waiting (tmem_wait_ld before using them).
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, float* v) {
+  uint32_t* r = reinterpret_cast<uint32_t*>(v);
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // 16 consecutive f32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
@@ -786,16 +799,26 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
       const int seg = t % segs, blk = t / segs;
       const int hb = a.H / R;
       const int y0 = (blk % hb) * R, bimg = blk / hb;
-      for (int rr = 0; rr < R; ++rr) {
-        const long long m = ((long long)(bimg * a.H + y0 + rr) * a.W + seg * 128) + r;
-        const uint32_t trow = tmem + (uint32_t)((b * R + rr) * a.NT) + ((uint32_t)(warp * 32) << 16);
-        for (int j0 = 0; j0 < a.NT; j0 += 16) {
-          float v[16];
-          tmem_ld16(trow + (uint32_t)j0, v);
+      // the tile's R rows x NT columns as one list of 16-column groups (a group
+      // never straddles two rows, NT being a multiple of 16); up to four
+      // groups per TMEM round trip, their loads in flight together
+      const int ngroups = R * (a.NT / 16), gpr = a.NT / 16;
+      const uint32_t tlane = tmem + (uint32_t)(b * R * a.NT) + ((uint32_t)(warp * 32) << 16);
+      for (int g0 = 0; g0 < ngroups; g0 += 4) {
+        float vv[64];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (g0 + q < ngroups) tmem_ld16_nowait(tlane + (uint32_t)((g0 + q) * 16), vv + q * 16);
+        tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (g0 + q >= ngroups) break;
+          const int rr = (g0 + q) / gpr, j0 = ((g0 + q) - rr * gpr) * 16;
+          const long long m = ((long long)(bimg * a.H + y0 + rr) * a.W + seg * 128) + r;
+          float* v = vv + q * 16;
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int n = j0 + j;
-            float yv = v[j] + sBias[n];
+            float yv = v[j] + sBias[j0 + j];
             if (a.relu) yv = fmaxf(yv, 0.f);
             v[j] = yv;
           }
