@@ -205,7 +205,7 @@ struct UmmaArgs {
   float* Yf;                 // CONV output [pixels][N] f32 (may be null)
   const __nv_bfloat16* dZ;   // WGRAD: output gradient [pixels][M]
   float* dW;                 // WGRAD: [M][N] f32, accumulated
-  int ksplit;                // WGRAD: pixels per CTA (multiple of 64)
+  int ksplit;                // WGRAD: pixels per CTA; CONV split over K: K values per CTA (multiple of 64, 0: no split)
 };
 
 // 16-byte chunk of the convolution input at pixel (b, y, x) of the output
@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
   const uint32_t tmem = *tslot;
 
   int kbeg = 0, kend = a.K;
-  if (a.mode == 2 || a.mode == 5) {
+  if (a.mode == 2 || a.mode == 5 || (a.mode == 1 && a.ksplit > 0)) {
     kbeg = blockIdx.z * a.ksplit;
     kend = min(a.K, kbeg + a.ksplit);
   }
@@ -523,6 +523,14 @@ __global__ void __launch_bounds__(kThreads) k_umma(UmmaArgs a, int* err) {
 #pragma unroll
         for (int j = 0; j < 16; ++j)
           if (n0 + j0 + j < a.N) a.C[(long long)m * a.N + n0 + j0 + j] = v[j];
+      } else if (a.mode == 1 && a.ksplit > 0) {
+        // CONV split over K: this CTA's partial sums; bias, ReLU and the
+        // stores follow in k_conv_finish
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = n0 + j0 + j;
+          if (n < a.N) atomicAdd(a.C + (long long)m * a.N + n, v[j]);
+        }
       } else if (a.mode == 1 || a.mode == 3) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -856,6 +864,18 @@ __global__ void __launch_bounds__(kCtThreads) k_conv_tma(const __grid_constant__
   if (s_fail && tid == 0 && err) atomicCAS(err, 0, kErrUmmaTimeout);
   tc_fence_after();
   if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+// Bias, ReLU and stores of a convolution whose K range was split over CTAs:
+// acc holds the sums of the partial tiles, [pixels][n] f32.
+__global__ void k_conv_finish(const float* __restrict__ acc, const float* __restrict__ bias, int relu,
+                              __nv_bfloat16* __restrict__ y, float* __restrict__ yf, long long total, int n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    float v = acc[i] + (bias ? bias[i % n] : 0.f);
+    if (relu) v = fmaxf(v, 0.f);
+    if (y) y[i] = __float2bfloat16_rn(v);
+    if (yf) yf[i] = v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1264,11 +1284,42 @@ int32_t kw_conv3x3(const void* x1, int32_t c1, const void* x2, int32_t c2, int32
   a.Yf = yf;
   // halo tiles of one input: the persistent TMA-fed kernel when it applies
   // (KWAVE_GB300_CONV_TMA=0: always k_umma)
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (a.mode == 3) {
-    const int rc = conv_tma_try(a, static_cast<cudaStream_t>(stream));
+    const int rc = conv_tma_try(a, st);
     if (rc != 1) return rc;
   }
-  return umma_launch(a, dim3((cout + a.NT - 1) / a.NT, (a.M + kBM - 1) / kBM), static_cast<cudaStream_t>(stream));
+  const int ntile = (cout + a.NT - 1) / a.NT, mtile = (a.M + kBM - 1) / kBM;
+  // gather tiles that leave SMs idle (small images, many channels): the K
+  // range is split over CTAs whose partial tiles are added in f32 scratch,
+  // then bias, ReLU and the stores run as one elementwise pass
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return umma_fail(KW_ERR_CUDA, "kw_conv3x3: device query failed");
+  const int nchunk = (a.K + kBK - 1) / kBK;
+  int split = 1;
+  if (a.mode == 1 && ntile * mtile < nsm) split = std::min((2 * nsm + ntile * mtile - 1) / (ntile * mtile), nchunk / 2);
+  if (split <= 1) return umma_launch(a, dim3(ntile, mtile), st);
+  const int per = (nchunk + split - 1) / split;
+  split = (nchunk + per - 1) / per;
+  float* acc = nullptr;
+  const size_t bytes = (size_t)a.M * cout * sizeof(float);
+  if (cudaMallocAsync(reinterpret_cast<void**>(&acc), bytes, st) != cudaSuccess)
+    return umma_fail(KW_ERR_OOM, "kw_conv3x3: split-K scratch");
+  int rc = KW_OK;
+  if (cudaMemsetAsync(acc, 0, bytes, st) != cudaSuccess) rc = umma_fail(KW_ERR_CUDA, "kw_conv3x3: scratch clear");
+  if (!rc) {
+    a.ksplit = per * kBK;
+    a.C = acc;
+    rc = umma_launch(a, dim3(ntile, mtile, split), st);
+  }
+  if (!rc) {
+    const long long total = (long long)a.M * cout;
+    k_conv_finish<<<grid1(total), 256, 0, st>>>(acc, bias, relu, a.Y, a.Yf, total, cout);
+    if (cudaGetLastError() != cudaSuccess) rc = umma_fail(KW_ERR_CUDA, "kw_conv3x3: finish launch");
+  }
+  cudaFreeAsync(acc, st);
+  return rc;
 }
 
 int32_t kw_conv3x3_wgrad(const void* x1, int32_t c1, const void* x2, int32_t c2, int32_t nb, int32_t H, int32_t W,
