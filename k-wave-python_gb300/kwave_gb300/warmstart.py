@@ -3,7 +3,7 @@
 A small BF16 U-Net (FP32 accumulation on the tensor cores, kw_unet.cu) maps
 a time-reversal image to an estimate of p0; adjoint iterations (CGLS on the
 GPU time loop, ``adjoint.cgls_p0``) refine it, with plain adjoint iterations
-from zero as fallback and as judge of its error.  The reference has no such
+from zero as fallback and as the yardstick of its error.  The reference has no such
 component; the network's input is the reference's time-reversal image
 (kwave/reconstruction/time_reversal.py:129-150: the recorded pressure,
 reversed in time, drives a Dirichlet source on the sensor mask; the final
@@ -358,7 +358,7 @@ def fit_input_scale(images, targets):
 
 
 # ---------------------------------------------------------------------------
-# refinement and its judge
+# refinement and the plain iterations it is measured against
 # ---------------------------------------------------------------------------
 def refine(prob, d_obs, p_init, iterations, p_true=None):
     """CGLS from p_init on the problem's linear map p0 -> recorded p (one plan
