@@ -80,10 +80,14 @@ def noisy(d, rng, level=0.01):
 def tr_problem(prob, data):
     """The time-reversal run of ``data`` (n_sensor, Nt) recorded on the binary
     mask of ``prob``: a Dirichlet pressure source on the mask driven by the
-    time-reversed data (time_reversal.py:129-150), no p0, no sensor."""
-    q = {k: v for k, v in prob.items() if k not in ("p0", "sensor_mask", "record")}
+    time-reversed data, no p0, and a sensor on the same mask that records
+    only ``p_final`` (time_reversal.py:94-98,129-135).  The image is the
+    final pressure field; recording adds no work per step (a sensor on every
+    grid point recording p, the solver's default without a mask, wrote the
+    whole field into the time series at each step)."""
+    q = {k: v for k, v in prob.items() if k not in ("p0", "sensor_mask", "record", "record_start_index")}
     q.update(p_mask=prob["sensor_mask"], p=np.ascontiguousarray(np.flip(data, axis=1)), p_mode="dirichlet",
-             sensor_mask=None, record=None)
+             sensor_mask=prob["sensor_mask"], record=("p_final",))
     return q
 
 

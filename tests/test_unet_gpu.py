@@ -208,3 +208,37 @@ def test_pair_generator_reuses_plans_exactly():
     assert np.array_equal(gp0s, p0s)
     for a, b in zip(gimgs, imgs):
         assert rel(a, b) <= 1e-5
+
+
+def test_time_reversal_image_independent_of_recording():
+    """The time-reversal runs record p_final alone on the sensor mask, as the
+    reference's time reversal does; the image (the final pressure field) is
+    bit-identical to that of the same run recording p on every grid point at
+    every step, and no time series is kept."""
+    from kwave_gb300.solver import Simulation, run_batch
+    from kwave_gb300.warmstart import noisy, pair_problem, time_reversal_images, tr_problem
+
+    kw = dict(n=64, nt=120, n_sensor=32, radius=5e-4)
+    probs = [pair_problem(s, **kw) for s in (11, 12)]
+    datas = [noisy(r["p"].astype(np.float64), np.random.default_rng(1)) for r in run_batch(probs)]
+    imgs = time_reversal_images(probs, datas)
+    for pr, d, img in zip(probs, datas, imgs):
+        q = tr_problem(pr, d)
+        sim = Simulation.from_problem(q).setup()
+        try:
+            res = sim.run()
+            assert set(res) == {"p_final"}, sorted(res)
+        finally:
+            sim.close()
+        full = dict(q, sensor_mask=None, record=None)
+        sim = Simulation.from_problem(full).setup()
+        try:
+            res_full = sim.run()
+            p_full = sim.p
+        finally:
+            sim.close()
+        assert res_full["p"].shape[0] == 64 * 64
+        ref = 2.0 * p_full
+        ref[ref < 0] = 0
+        assert np.array_equal(img, ref)
+        assert np.array_equal(res["p_final"], res_full["p_final"])

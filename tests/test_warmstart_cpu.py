@@ -41,5 +41,7 @@ def test_pair_and_time_reversal_problems():
     assert prob["p0"].shape == (256, 256) and prob["p0"].max() > 0 and not prob["smooth_p0"]
     data = np.arange(int(mask.sum()) * prob["Nt"], dtype=float).reshape(-1, prob["Nt"])
     q = tr_problem(prob, data)
-    assert q["p_mode"] == "dirichlet" and q["sensor_mask"] is None and "p0" not in q
+    assert q["p_mode"] == "dirichlet" and q["sensor_mask"] is mask and "p0" not in q
+    # the reference's time reversal records p_final alone on the sensor mask
+    assert tuple(q["record"]) == ("p_final",)
     assert np.array_equal(q["p"], data[:, ::-1]) and q["p_mask"] is mask
