@@ -341,12 +341,13 @@ class UNet:
         return hist
 
     def predict(self, images, batch=16):
-        """Estimates of p0 for float32 (N, n, n) host images."""
+        """Estimates of p0 for (N, n, n) host images (an array or a list of
+        (n, n) arrays, converted to float32)."""
         import torch
 
         out = []
         for i in range(0, len(images), batch):
-            x = torch.as_tensor(np.ascontiguousarray(images[i:i + batch]), device=self.device)
+            x = torch.as_tensor(np.ascontiguousarray(images[i:i + batch], dtype=np.float32), device=self.device)
             out.append(self.forward(x).cpu().numpy())
         return np.concatenate(out)
 
