@@ -10,6 +10,9 @@ Entry points:
   * ``unified.kspaceFirstOrder`` — the unified entry point
     (``kwave.kspaceFirstOrder.kspaceFirstOrder``) for ``backend="gb300"``;
   * ``backend.kspaceFirstOrder2D`` / ``3D`` — the legacy signatures;
+  * ``backend.kspaceFirstOrder2DC`` / ``3DC`` — the legacy C++ route with
+    ``save_to_disk``: the C++ binary's input file as the legacy route and
+    MATLAB k-Wave write it, run on the GPU time loop in place of the binary;
   * ``reconstruction.TimeReversal`` — time-reversal reconstruction, with
     ``conversion.cart2grid`` for Cartesian sensors;
   * ``solver.SimulationBatch`` / ``solver.run_batch`` — many independent
@@ -17,8 +20,8 @@ Entry points:
 """
 __version__ = "0.1.0"
 
-from .backend import (BACKEND, execution_options, install, kspaceFirstOrder2D, kspaceFirstOrder3D,  # noqa: F401
-                      run_gb300_backend, uninstall)
+from .backend import (BACKEND, execution_options, install, kspaceFirstOrder2D, kspaceFirstOrder2DC,  # noqa: F401
+                      kspaceFirstOrder3D, kspaceFirstOrder3DC, run_gb300_backend, uninstall)
 from .conversion import cart2grid  # noqa: F401
 from .reconstruction import TimeReversal  # noqa: F401
 from .solver import Simulation, SimulationBatch, run_batch, run_problem  # noqa: F401

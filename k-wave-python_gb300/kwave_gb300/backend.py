@@ -87,6 +87,58 @@ kspaceFirstOrder2D = _legacy(2, "kspaceFirstOrder2D")
 kspaceFirstOrder3D = _legacy(3, "kspaceFirstOrder3D")
 
 
+def _input_path(simulation_options):
+    """The input file name of the options: ``input_filename`` inside
+    ``data_path`` (kwave/options/simulation_options.py:111-112 and :189,
+    which join the two unless the name is already absolute)."""
+    import os
+    import tempfile
+
+    name = getattr(simulation_options, "input_filename", None) or "kwave_input.h5"
+    if os.path.isabs(name):
+        return name
+    return os.path.join(getattr(simulation_options, "data_path", None) or tempfile.gettempdir(), name)
+
+
+def _legacy_cpp(ndim_expected, name):
+    def run(kgrid, source, sensor, medium, simulation_options, execution_options=None):
+        from . import cpp_io
+
+        dim = len(grid_of(kgrid)[0])
+        if dim != ndim_expected:
+            raise ValueError(f"{name} needs a {ndim_expected}-D grid, got {dim}-D")
+        if not getattr(simulation_options, "save_to_disk", False):
+            raise ValueError("CPU simulation requires saving to disk. Please set SimulationOptions.save_to_disk=True")
+        prob = cpp_io.legacy_problem(
+            kgrid, medium, source, sensor,
+            # the legacy default PML: 20 points in 2-D, 10 in 3-D (simulation_options.py:264-287)
+            pml_size=_per_axis(getattr(simulation_options, "pml_size", None), dim, 20 if dim == 2 else 10, int),
+            pml_alpha=_per_axis(getattr(simulation_options, "pml_alpha", None), dim, 2.0, float),
+            pml_inside=getattr(simulation_options, "pml_inside", True),
+            smooth_p0=getattr(simulation_options, "smooth_p0", True),
+            use_sg=getattr(simulation_options, "use_sg", True))
+        path = _input_path(simulation_options)
+        cpp_io.write_input_file(path, prob, legacy=True)
+        if getattr(simulation_options, "save_to_disk_exit", False):
+            return None
+        return cpp_io.run_input_file(path, scaled_sources=True)
+
+    run.__name__ = run.__qualname__ = name
+    run.__doc__ = (f"{name}(kgrid, source, sensor, medium, simulation_options, execution_options): the legacy "
+                   "C++ route (kwave/kspaceFirstOrder2D.py:82-139 and :221-384) with ``save_to_disk``.  Writes "
+                   "the input file the legacy route writes (``cpp_io.legacy_problem`` and "
+                   "``cpp_io.input_datasets(legacy=True)``) to ``input_filename`` in ``data_path``; returns None "
+                   "with ``save_to_disk_exit``, otherwise runs that file on the GB300 time loop in place of the "
+                   "C++ binary and returns the native solver's result dict (``cpp_io.run_input_file``).  "
+                   "``simulation_options`` is read for save_to_disk, save_to_disk_exit, data_path, "
+                   "input_filename, pml_size, pml_alpha, pml_inside, smooth_p0 and use_sg.")
+    return run
+
+
+kspaceFirstOrder2DC = _legacy_cpp(2, "kspaceFirstOrder2DC")
+kspaceFirstOrder3DC = _legacy_cpp(3, "kspaceFirstOrder3DC")
+
+
 _installed = {}
 
 

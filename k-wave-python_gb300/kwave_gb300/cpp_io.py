@@ -121,11 +121,70 @@ def file_attributes(description=None):
             "creation_date": datetime.now().strftime("%d-%b-%Y-%H-%M-%S")}
 
 
-def input_datasets(prob):
+def legacy_staggered(rho0, axis):
+    """rho0 at the staggered points x_axis + d/2 as the legacy route
+    interpolates it (kwave/kspaceFirstOrder2D.py:246-249 and the 3-D
+    counterpart, linear ``interpolate2d``/``interpolate3d`` of
+    kwave/utils/interp.py): the mean of each point and its neighbour along
+    ``axis``; the last point's query lies outside the grid and keeps rho0
+    (no wrap-around), in float64."""
+    r = np.asarray(rho0, dtype=np.float64)
+    out = r.copy()
+    lo = [slice(None)] * r.ndim
+    hi = list(lo)
+    lo[axis], hi[axis] = slice(0, -1), slice(1, None)
+    out[tuple(lo)] = 0.5 * (r[tuple(lo)] + r[tuple(hi)])
+    return out
+
+
+def _c0_at(c0, idx, rows):
+    """Sound speed at the first ``rows`` points of a 1-based Fortran-order
+    index list (one value for a homogeneous medium)."""
+    c = np.asarray(c0, dtype=np.float64)
+    if c.size == 1:
+        return np.full(rows, float(c.reshape(-1)[0]))
+    return c.ravel(order="F")[np.asarray(idx, dtype=np.int64).reshape(-1)[:rows] - 1]
+
+
+def legacy_source_factors(prob, field):
+    """Per-row factors by which the legacy route scales a source signal before
+    storing it, in units the C++ binary adds to its split fields as they are
+    (kwave/kWaveSimulation_helper/scale_source_terms_func.py:89-190 and
+    :262-330, the MATLAB k-Wave convention of its input files):
+
+    * pressure, additive modes: 2 dt / (N c0 dx), dirichlet: 1 / (N c0^2),
+      with N the number of dimensions and dx the x spacing;
+    * velocity component ``u_a``, additive modes: 2 c0 dt / d_a, dirichlet: 1.
+
+    c0 is the sound speed at each row's source point (row i belongs to the
+    i-th point of the Fortran-order index list) in a heterogeneous medium."""
+    shape = tuple(int(n) for n in prob["shape"])
+    ndim = len(shape)
+    dt = float(prob["dt"])
+    spacing = [float(d) for d in prob["spacing"]]
+    rows = np.asarray(prob[field]).reshape(-1, np.asarray(prob[field]).shape[-1]).shape[0]
+    if field == "p":
+        c = _c0_at(prob["sound_speed"], _fortran_index(prob["p_mask"], shape), rows)
+        if (prob.get("p_mode") or "additive") == "dirichlet":
+            return 1.0 / (ndim * c ** 2)
+        return 2.0 * dt / (ndim * c * spacing[0])
+    if (prob.get("u_mode") or "additive") == "dirichlet":
+        return np.ones(rows)
+    c = _c0_at(prob["sound_speed"], _fortran_index(prob["u_mask"], shape), rows)
+    return 2.0 * c * dt / spacing[("ux", "uy", "uz").index(field)]
+
+
+def input_datasets(prob, legacy=False):
     """Datasets and their attributes of the input file for a problem dict
     whose grid already holds the PML and whose p0 is final (smoothed or not).
     The set, names, types and values of
-    kwave/solvers/cpp_simulation.py:139-318."""
+    kwave/solvers/cpp_simulation.py:139-318; with ``legacy`` those of the
+    legacy route (kspaceFirstOrder2DC/3DC with ``save_to_disk``,
+    kwave/kWaveSimulation_helper/save_to_disk_func.py), which are the MATLAB
+    k-Wave input files: density 1 when unset, staggered densities by
+    :func:`legacy_staggered`, source signals scaled by
+    :func:`legacy_source_factors` (rows in the order of the Fortran-order
+    index list, as the caller gives them)."""
     shape = tuple(int(n) for n in prob["shape"])
     ndim = len(shape)
     spacing = [float(d) for d in prob["spacing"]]
@@ -137,10 +196,14 @@ def input_datasets(prob):
 
     c0 = np.atleast_1d(np.asarray(prob["sound_speed"], dtype=np.float32))
     dens = prob.get("density")
-    rho0 = np.atleast_1d(np.asarray(dens if dens is not None else 1000.0, dtype=np.float32))
+    if dens is None:
+        dens = 1.0 if legacy else 1000.0
+    rho0 = np.atleast_1d(np.asarray(dens, dtype=np.float32))
     c_ref = float(np.max(c0))
     if rho0.size == 1 or not prob.get("use_sg", True):
         rho0_sg = [rho0] * ndim
+    elif legacy:
+        rho0_sg = [legacy_staggered(np.asarray(dens, dtype=np.float64), axis) for axis in range(ndim)]
     else:
         rho0_sg = [0.5 * (rho0 + np.roll(rho0, -1, axis=axis)) for axis in range(ndim)]
 
@@ -203,7 +266,12 @@ def input_datasets(prob):
     if has_p0:
         out["p0_source_input"] = matrix(np.asarray(p0, dtype=np.float32).reshape(shape))
     if has_p:
-        p_data = np.asarray(ps, dtype=np.float32)
+        if legacy:
+            sig = np.asarray(ps, dtype=np.float64)
+            sig = sig.reshape(-1, sig.shape[-1]) if sig.ndim != 2 else sig
+            p_data = (sig * legacy_source_factors(prob, "p")[:, None]).astype(np.float32)
+        else:
+            p_data = np.asarray(ps, dtype=np.float32)
         out["p_source_input"] = matrix(p_data)
         pm = np.asarray(prob["p_mask"])
         if pm.ndim == 2 and pm.shape[0] == ndim and pm.shape != shape:
@@ -215,7 +283,12 @@ def input_datasets(prob):
         out["p_source_many"] = matrix(np.array(int(_num_dim2(p_data) > 1), dtype=np.uint64))
     for v, on in has_u.items():
         if on:
-            out[f"{v}_source_input"] = matrix(np.asarray(vel[v], dtype=np.float32))
+            if legacy:
+                sig = np.asarray(vel[v], dtype=np.float64)
+                sig = sig.reshape(-1, sig.shape[-1]) if sig.ndim != 2 else sig
+                out[f"{v}_source_input"] = matrix((sig * legacy_source_factors(prob, v)[:, None]).astype(np.float32))
+            else:
+                out[f"{v}_source_input"] = matrix(np.asarray(vel[v], dtype=np.float32))
     if any(has_u.values()):
         um = np.asarray(prob["u_mask"])
         if um.ndim == 2 and um.shape[0] == ndim and um.shape != shape:
@@ -229,11 +302,54 @@ def input_datasets(prob):
     return out
 
 
-def write_input_file(path, prob, description=None):
-    """Write the input file of a (PML-holding, final-p0) problem dict."""
-    ds = input_datasets(prob)
+def write_input_file(path, prob, description=None, legacy=False):
+    """Write the input file of a (PML-holding, final-p0) problem dict
+    (``legacy``: the legacy route's values, see :func:`input_datasets`)."""
+    ds = input_datasets(prob, legacy=legacy)
     h5io.write_file(path, {k: v[0] for k, v in ds.items()}, {k: v[1] for k, v in ds.items()},
                     file_attributes(description))
+
+
+def legacy_problem(kgrid, medium, source, sensor, *, pml_size=20, pml_alpha=2.0, pml_inside=True, smooth_p0=True,
+                   use_sg=True):
+    """The problem dict whose legacy input file the legacy route writes for
+    these arguments (kwave/kspaceFirstOrder2D.py:142-384 with
+    ``save_to_disk``): a homogeneous medium without a density gets density
+    1 (kwave/kWaveSimulation.py:596-602; a heterogeneous one must set it),
+    Cartesian sensor points are mapped to their nearest grid points, p0 is
+    smoothed with its maximum restored before the grid is grown by the PML
+    (kwave/kWaveSimulation.py:1209-1253), and with ``pml_inside=False`` the
+    grid, medium, p0, masks and sensor grow by ``pml_size`` on every side
+    (kwave/kWaveSimulation_helper/expand_grid_matrices.py).  Source rows stay
+    in the caller's order, the Fortran order of the mask's points."""
+    from types import SimpleNamespace
+
+    from .conversion import cart2grid
+    from .precompute import problem_from_kwave
+    from .unified import _is_cartesian, expand_problem, normalize_pml
+
+    prob = problem_from_kwave(kgrid, medium, source, sensor, smooth_p0=False, use_sg=use_sg)
+    shape = tuple(int(n) for n in prob["shape"])
+    ndim = len(shape)
+    if ndim not in (2, 3):
+        raise NotImplementedError("the C++ input file holds 2-D and 3-D grids")
+    pml_size = tuple(int(p) for p in normalize_pml(pml_size, ndim))
+    pml_alpha = tuple(float(a) for a in normalize_pml(pml_alpha, ndim, "pml_alpha"))
+    if prob.get("density") is None:
+        if np.asarray(prob["sound_speed"]).size > 1:
+            raise ValueError("medium.density must be defined for a heterogeneous medium")
+        prob["density"] = 1.0
+    m = prob.get("sensor_mask")
+    if m is not None and _is_cartesian(m, ndim):
+        kg = SimpleNamespace(N=np.array(shape), spacing=np.array(prob["spacing"]), dim=ndim)
+        prob["sensor_mask"] = cart2grid(kg, np.asarray(m), order="C")[0]
+    p0 = prob.get("p0")
+    if smooth_p0 and p0 is not None and np.asarray(p0).size > 1:
+        prob["p0"] = smooth_host(np.asarray(p0, dtype=np.float64).reshape(shape))
+    if not pml_inside:
+        prob = expand_problem(prob, pml_size)
+    prob.update(pml_size=pml_size, pml_alpha=pml_alpha, smooth_p0=False)
+    return prob
 
 
 def save_input_files(prob, data_path):
@@ -280,9 +396,14 @@ def _rows_to_c_order(rows, idx, shape):
     return rows[np.argsort(c, kind="stable")]
 
 
-def problem_from_input_file(path):
+def problem_from_input_file(path, scaled_sources=False):
     """Problem dict of the native solver's time loop for an input file (PML
-    inside the grid, p0 used as stored, ``p`` recorded)."""
+    inside the grid, p0 used as stored, ``p`` recorded).  ``scaled_sources``:
+    the file's source signals carry the legacy route's scaling (files of
+    MATLAB k-Wave and of kspaceFirstOrder2DC/3DC with ``save_to_disk``, see
+    :func:`legacy_source_factors`), which is divided out again; files of
+    ``kspaceFirstOrder(..., save_only=True)`` hold the signals unscaled.  The
+    two kinds carry the same attributes, so the caller says which it is."""
     ds, _, root = h5io.read_file(path)
     if root.get("file_type", "input") != "input":
         raise ValueError(f"{path}: file_type {root.get('file_type')!r}, expected 'input'")
@@ -327,16 +448,39 @@ def problem_from_input_file(path):
             prob[v] = _rows_to_c_order(unmatrix(ds[f"{v}_source_input"], 2), idx, shape)
         prob["u_mode"] = MODE_NAMES[_scalar(ds, "u_source_mode", int)] if "u_source_mode" in ds else "additive"
     prob["sensor_mask"] = _mask_from_index(ds["sensor_mask_index"], shape)
+    if scaled_sources:
+        _unscale_sources(prob, ds)
     return prob
 
 
-def run_input_file(path, stream=None):
+def _unscale_sources(prob, ds):
+    """Divide the legacy scaling out of the source rows of a problem read
+    from a file (rows already in C order: the factors are taken in the
+    file's Fortran order and permuted the same way)."""
+    shape = tuple(prob["shape"])
+    for field, idx_name in (("p", "p_source_index"), ("ux", "u_source_index"), ("uy", "u_source_index"),
+                            ("uz", "u_source_index")):
+        if field not in prob:
+            continue
+        mask_key = "p_mask" if field == "p" else "u_mask"
+        fprob = dict(prob, p=None, ux=None, uy=None, uz=None)
+        fprob[field] = unmatrix(ds[f"{field}_source_input"], 2)
+        fprob[mask_key] = prob[mask_key]
+        f = legacy_source_factors(fprob, field)
+        rows = np.asarray(prob[field], dtype=np.float64)
+        if rows.shape[0] > 1:
+            f = _rows_to_c_order(f[:, None], ds[idx_name], shape)[:, 0]
+        prob[field] = (rows / f[:, None]).astype(np.float32)
+
+
+def run_input_file(path, stream=None, scaled_sources=False):
     """Run an input file of the C++ binary on the GB300 time loop; returns
     the result dict of the native solver (``p`` as (n_sensor, Nt) with the
-    sensor points in C order)."""
+    sensor points in C order).  ``scaled_sources`` as for
+    :func:`problem_from_input_file`."""
     from .solver import Simulation
 
-    sim = Simulation.from_problem(problem_from_input_file(path), stream=stream)
+    sim = Simulation.from_problem(problem_from_input_file(path, scaled_sources=scaled_sources), stream=stream)
     try:
         return sim.run()
     finally:
