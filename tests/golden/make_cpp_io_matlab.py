@@ -170,6 +170,28 @@ def main():
     yz = np.arange(-20, 21, 2) * 1e-4
     _store("tvsp_3D_simulation", "out_tvsp_3D_simulation", root, kg, dict(sound_speed=c3, density=r3),
            dict(p_mask=pm3, p=sig3), np.array([20e-4 * np.ones(yz.shape), yz, yz]))
+    # small photoacoustic sources, 1 mm grids of 64 points, set time axis
+    for d, maker in ((2, make_disc), (3, make_ball)):
+        n = (64,) * d
+        kgp = grid(n, (1e-3 / 64,) * d, nt=round(300e-9 / 2e-9) + 1, dt=2e-9)
+        sens = np.zeros(n)
+        sens[(21,) + (31,) * (d - 1)] = 1
+        _store(f"ivp_photoacoustic_waveforms_{d}d", f"out_ivp_photoacoustic_waveforms/input_{d - 1}", root, kgp,
+               dict(sound_speed=1500.0), dict(p0=maker(Vector(list(n)), Vector(list(n)) / 2, 2)), sens)
+    # the sensor frequency response is applied to the recorded data, not stored
+    kgf = grid((128, 128), (1e-4, 1e-4), 1500)
+    for i in (1, 2):
+        _store(f"ivp_sensor_frequency_response_{i}", f"out_ivp_sensor_frequency_response/input_{i}", root, kgf,
+               absorbing, dict(p0=discs((128, 128))), make_cart_circle(4e-3, 50))
+    # binary sensor from cart2grid, time axis to 6 us, PML switched off / outside
+    from kwave.utils.conversion import cart2grid
+
+    kgm = kWaveGrid(Vector([128, 128]), Vector([1e-4, 1e-4]))
+    kgm.makeTime(1500, 0.3, 6e-6)
+    bm = cart2grid(kgm, make_cart_circle(6.3e-3, 50))[0]
+    for i, opts in ((1, dict(pml_alpha=0.0)), (2, dict(pml_inside=False))):
+        _store(f"ivp_comparison_modelling_functions_{i}", f"out_ivp_comparison_modelling_functions/input_{i}", root,
+               kgm, dict(sound_speed=1500.0), dict(p0=discs((128, 128))), bm, **opts)
     n3b = (12, 44, 44)
     kg = grid(n3b, (2e-4,) * 3, 1500)
     p0b = smooth(10 * make_ball(Vector(list(n3b)), Vector(list(n3b)) / 2, 3), True)
