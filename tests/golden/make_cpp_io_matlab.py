@@ -192,6 +192,22 @@ def main():
     for i, opts in ((1, dict(pml_alpha=0.0)), (2, dict(pml_inside=False))):
         _store(f"ivp_comparison_modelling_functions_{i}", f"out_ivp_comparison_modelling_functions/input_{i}", root,
                kgm, dict(sound_speed=1500.0), dict(p0=discs((128, 128))), bm, **opts)
+    # 256 x 128 x 64 absorbing medium with a ball, a pressure patch source and a sensor plane
+    nr = (256, 128, 64)
+    kgr = grid(nr, (1e-4,) * 3, nt=1200, dt=15e-9)
+    ball = make_ball(Vector(list(nr)), Vector(list(nr)) / 2 + Vector([40, 0, 0]), 20)
+    cr = 1500 * np.ones(nr)
+    rr = 1000 * np.ones(nr)
+    cr[ball == 1] = 1800
+    rr[ball == 1] = 1200
+    med = dict(sound_speed=cr, density=rr, alpha_coeff=0.75, alpha_power=1.5)
+    pmr = np.zeros(nr)
+    pmr[10, 33:94, 16:47] = 1
+    sigr = filter_time_series(kgr, kWaveMedium(**med), 0.5e6 * np.sin(2 * np.pi * 2e6 * kgr.t_array))
+    plane = np.zeros(nr)
+    plane[:, :, 31] = 1
+    _store("cpp_running_simulations", "out_cpp_running_simulations", root, kgr, med, dict(p_mask=pmr, p=sigr),
+           plane, pml_size=(10, 10, 10))
     n3b = (12, 44, 44)
     kg = grid(n3b, (2e-4,) * 3, 1500)
     p0b = smooth(10 * make_ball(Vector(list(n3b)), Vector(list(n3b)) / 2, 3), True)
