@@ -103,8 +103,9 @@ def _input_path(simulation_options):
 def _legacy_cpp(ndim_expected, name):
     def run(kgrid, source, sensor, medium, simulation_options, execution_options=None):
         from . import cpp_io
+        from .precompute import grid_shape_of
 
-        dim = len(grid_of(kgrid)[0])
+        dim = len(grid_shape_of(kgrid)[0])
         if dim != ndim_expected:
             raise ValueError(f"{name} needs a {ndim_expected}-D grid, got {dim}-D")
         if not getattr(simulation_options, "save_to_disk", False):

@@ -310,6 +310,28 @@ def write_input_file(path, prob, description=None, legacy=False):
                     file_attributes(description))
 
 
+def _time_unset(v):
+    return v is None or isinstance(v, str) or (np.ndim(v) == 0 and np.isnan(float(v)))
+
+
+def make_time(shape, spacing, c, cfl=0.3, t_end=None):
+    """(Nt, dt) of kWaveGrid.makeTime (kwave/kgrid.py:455-495): dt = cfl x
+    the smallest spacing / the largest sound speed; by default the time to
+    cross the grid's diagonal at the smallest sound speed, Nt = floor(t_end /
+    dt) + 1, one more when t_end / dt is not whole but MATLAB's rem(t_end,
+    dt) is zero."""
+    c = np.asarray(c, dtype=np.float64)
+    size = np.asarray(shape, dtype=np.float64) * np.asarray(spacing, dtype=np.float64)
+    if t_end is None:
+        t_end = float(np.linalg.norm(size, ord=2)) / float(np.min(c))
+    dt = cfl * float(np.min(spacing)) / float(np.max(c))
+    q = t_end / dt
+    Nt = int(np.floor(q) + 1)
+    if np.floor(q) != np.ceil(q) and t_end - np.trunc(q) * dt == 0:
+        Nt += 1
+    return Nt, dt
+
+
 def legacy_problem(kgrid, medium, source, sensor, *, pml_size=20, pml_alpha=2.0, pml_inside=True, smooth_p0=True,
                    use_sg=True):
     """The problem dict whose legacy input file the legacy route writes for
@@ -325,16 +347,31 @@ def legacy_problem(kgrid, medium, source, sensor, *, pml_size=20, pml_alpha=2.0,
     from types import SimpleNamespace
 
     from .conversion import cart2grid
-    from .precompute import problem_from_kwave
+    from .precompute import _get, grid_shape_of, problem_from_kwave
     from .unified import _is_cartesian, expand_problem, normalize_pml
 
+    shape, spacing = grid_shape_of(kgrid)
+    Nt, dt = _get(kgrid, "Nt"), _get(kgrid, "dt")
+    if _time_unset(Nt) or _time_unset(dt):
+        # kwave/kWaveSimulation.py:1038-1041: a grid without a time axis gets makeTime at the k-space CFL
+        c = _get(medium, "sound_speed")
+        if c is None:
+            raise ValueError("medium.sound_speed must be defined")
+        Nt, dt = make_time(shape, spacing, c)
+    kgrid = SimpleNamespace(N=np.array(shape), spacing=np.array(spacing), Nt=int(Nt), dt=float(dt), dim=len(shape))
     prob = problem_from_kwave(kgrid, medium, source, sensor, smooth_p0=False, use_sg=use_sg)
-    shape = tuple(int(n) for n in prob["shape"])
     ndim = len(shape)
     if ndim not in (2, 3):
         raise NotImplementedError("the C++ input file holds 2-D and 3-D grids")
     pml_size = tuple(int(p) for p in normalize_pml(pml_size, ndim))
     pml_alpha = tuple(float(a) for a in normalize_pml(pml_alpha, ndim, "pml_alpha"))
+    n = int(np.prod(shape))
+    for k in ("sound_speed", "density", "alpha_coeff", "BonA", "p0", "p_mask", "u_mask"):
+        v = prob.get(k)
+        if v is not None and np.asarray(v).size not in (1, n):
+            raise ValueError(f"{k} has {np.asarray(v).size} elements but the grid has {n} points")
+    if pml_inside and any(2 * p >= N for p, N in zip(pml_size, shape)):
+        raise ValueError(f"pml_size {pml_size} is too large for the grid {shape} with the PML inside")
     if prob.get("density") is None:
         if np.asarray(prob["sound_speed"]).size > 1:
             raise ValueError("medium.density must be defined for a heterogeneous medium")

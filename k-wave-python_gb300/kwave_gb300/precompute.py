@@ -56,6 +56,13 @@ def _enabled(x) -> bool:
 def grid_of(kgrid):
     """(shape, spacing, Nt, dt) from a kWaveGrid (N/spacing) or an Nx/dx namespace
     (kspace_solver.py:210-226)."""
+    shape, spacing = grid_shape_of(kgrid)
+    return shape, spacing, int(_get(kgrid, "Nt")), float(_get(kgrid, "dt"))
+
+
+def grid_shape_of(kgrid):
+    """(shape, spacing) of a kWaveGrid or an Nx/dx namespace, whatever its
+    time axis holds."""
     if _get(kgrid, "N") is not None and _get(kgrid, "spacing") is not None:
         shape = tuple(int(n) for n in np.atleast_1d(_get(kgrid, "N")))
         spacing = tuple(float(d) for d in np.atleast_1d(_get(kgrid, "spacing")))
@@ -68,7 +75,7 @@ def grid_of(kgrid):
             shape.append(int(n))
             spacing.append(float(d))
         shape, spacing = tuple(shape), tuple(spacing)
-    return shape, spacing, int(_get(kgrid, "Nt")), float(_get(kgrid, "dt"))
+    return shape, spacing
 
 
 def problem_from_kwave(kgrid, medium, source, sensor, *, pml_size=None, pml_alpha=None, use_sg=True,

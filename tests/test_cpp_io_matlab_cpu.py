@@ -143,3 +143,38 @@ def test_legacy_route_refusals(tmp_path):
                                     NS(save_to_disk=True, save_to_disk_exit=True, data_path=str(tmp_path)))
     with pytest.raises(ValueError, match="3-D"):
         backend.kspaceFirstOrder3DC(kgrid, source, sensor, medium, NS(save_to_disk=True))
+    medium.density = np.ones(7)
+    with pytest.raises(ValueError, match="density has 7 elements"):
+        backend.kspaceFirstOrder2DC(kgrid, source, sensor, medium, NS(save_to_disk=True, data_path=str(tmp_path)))
+    medium.density = 1000.0
+    with pytest.raises(ValueError, match="too large"):
+        backend.kspaceFirstOrder2DC(kgrid, source, sensor, medium,
+                                    NS(save_to_disk=True, data_path=str(tmp_path), pml_size=64))
+
+
+MAKETIME_CASES = ["ivp_homogeneous_medium", "ivp_heterogeneous_medium", "ivp_binary_sensor_mask", "ivp_3D_simulation",
+                  "tvsp_homogeneous_medium_monopole", "tvsp_3D_simulation", "pr_2D_FFT_line_sensor",
+                  "pr_3D_FFT_planar_sensor", "na_controlling_the_PML_1", "ivp_sensor_frequency_response_1"]
+
+
+@pytest.mark.parametrize("name", MAKETIME_CASES)
+def test_make_time_matches_kgrid(name):
+    """cpp_io.make_time gives the Nt and dt the reference's kWaveGrid.makeTime
+    gave for these grids and media (stored by the fixture script)."""
+    inp, _, _ = _load(name)
+    Nt, dt = cpp_io.make_time(tuple(inp["shape"]), tuple(inp["spacing"]), inp["sound_speed"])
+    assert (Nt, dt) == (int(inp["Nt"]), float(inp["dt"]))
+
+
+def test_legacy_route_makes_the_time_axis(tmp_path):
+    """A grid without a time axis gets makeTime's, as the legacy route gives
+    it (the reference's homogeneous-medium example passes such a grid): the
+    file still matches MATLAB's, dt included."""
+    inp, opts, expected = _load("ivp_homogeneous_medium")
+    kgrid, medium, source, sensor = _objects(inp)
+    kgrid.Nt = kgrid.dt = "auto"
+    so = NS(save_to_disk=True, save_to_disk_exit=True, data_path=str(tmp_path), input_filename="auto.h5", **opts)
+    backend.kspaceFirstOrder2DC(kgrid, source, sensor, medium, so)
+    got = _summary(tmp_path / "auto.h5")
+    assert got["dt"]["checksum8"] == expected["dt"]["checksum8"]
+    assert int(np.asarray(h5io.read_file(tmp_path / "auto.h5")[0]["Nt"]).reshape(-1)[0]) == int(inp["Nt"])
