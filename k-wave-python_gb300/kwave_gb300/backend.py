@@ -119,7 +119,10 @@ def _legacy_cpp(ndim_expected, name):
             smooth_p0=getattr(simulation_options, "smooth_p0", True),
             use_sg=getattr(simulation_options, "use_sg", True))
         path = _input_path(simulation_options)
-        cpp_io.write_input_file(path, prob, legacy=True)
+        level = getattr(simulation_options, "hdf_compression_level", None) or 0
+        if not (isinstance(level, (int, np.integer)) and 0 <= level <= 9):
+            raise ValueError("Optional input ''hdf_compression_level'' must be an integer between 0 and 9.")
+        cpp_io.write_input_file(path, prob, legacy=True, compression_level=int(level))
         if getattr(simulation_options, "save_to_disk_exit", False):
             return None
         return cpp_io.run_input_file(path, scaled_sources=True)
@@ -132,7 +135,7 @@ def _legacy_cpp(ndim_expected, name):
                    "with ``save_to_disk_exit``, otherwise runs that file on the GB300 time loop in place of the "
                    "C++ binary and returns the native solver's result dict (``cpp_io.run_input_file``).  "
                    "``simulation_options`` is read for save_to_disk, save_to_disk_exit, data_path, "
-                   "input_filename, pml_size, pml_alpha, pml_inside, smooth_p0 and use_sg.")
+                   "input_filename, hdf_compression_level, pml_size, pml_alpha, pml_inside, smooth_p0 and use_sg.")
     return run
 
 

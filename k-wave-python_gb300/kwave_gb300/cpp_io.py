@@ -302,12 +302,37 @@ def input_datasets(prob, legacy=False):
     return out
 
 
-def write_input_file(path, prob, description=None, legacy=False):
+def _deflate_chunks(stored):
+    """Chunk shape for a deflated matrix, or None for one stored as is:
+    kwave/utils/io.py:78-106 compresses grids and many-row signals (two or
+    more axes longer than 1) and vectors of more than 1 MB of doubles, the
+    rest not.  The chunks split the first axis longer than 1 into at most
+    64 pieces (one B-tree node of chunks)."""
+    a = np.asarray(stored)
+    long_axes = [i for i, n in enumerate(a.shape) if n > 1]
+    if len(long_axes) < 2 and a.size <= (1024 ** 2) // 8:
+        return None
+    ch = list(a.shape)
+    ax = long_axes[0]
+    ch[ax] = -(-a.shape[ax] // 64)
+    return tuple(ch)
+
+
+def write_input_file(path, prob, description=None, legacy=False, compression_level=0):
     """Write the input file of a (PML-holding, final-p0) problem dict
-    (``legacy``: the legacy route's values, see :func:`input_datasets`)."""
+    (``legacy``: the legacy route's values, see :func:`input_datasets`).
+    ``compression_level`` 1-9 deflates the matrices that
+    kwave/utils/io.py:52-188 compresses at ``hdf_compression_level``."""
     ds = input_datasets(prob, legacy=legacy)
-    h5io.write_file(path, {k: v[0] for k, v in ds.items()}, {k: v[1] for k, v in ds.items()},
-                    file_attributes(description))
+    data = {k: v[0] for k, v in ds.items()}
+    chunks, comp = {}, {}
+    if compression_level:
+        for k, a in data.items():
+            ch = _deflate_chunks(a)
+            if ch is not None:
+                chunks[k], comp[k] = ch, int(compression_level)
+    h5io.write_file(path, data, {k: v[1] for k, v in ds.items()}, file_attributes(description), chunks=chunks,
+                    compression=comp)
 
 
 def _time_unset(v):

@@ -12,21 +12,26 @@ HDF5 file format specification:
   symbol table nodes, local heap of names;
 * datasets with version-1 object headers (continuation blocks followed when
   reading): simple dataspaces, IEEE little-endian float32/float64 and
-  little-endian integers, contiguous or unfiltered chunked storage (a single
-  leaf B-tree node of chunks when writing, any depth when reading) and
-  compact storage (read);
+  little-endian integers, contiguous or chunked storage (a single leaf
+  B-tree node of chunks when writing, any depth when reading) and compact
+  storage (read);
+* the filters h5py applies to chunks (``compression=level``, ``shuffle``,
+  ``fletcher32``): deflate (zlib) and shuffle written and read, the Fletcher
+  checksum read (stripped, not verified); filter pipeline messages of
+  version 1 (written) and 1 or 2 (read), per-chunk filter masks honoured;
 * attributes of fixed-length ASCII strings (``<S{n}``, null-padded, scalar),
   on datasets and on the root group.
 
 Data are written and read as stored: the dimensions in the file are the
-array's shape (C order).  Filters (compression), variable-length types,
-version-2 object headers and newer superblocks are refused with
-NotImplementedError.  The format subset is checked by round trips and by
+array's shape (C order).  Other filters (szip, n-bit, scale-offset),
+variable-length types, version-2 object headers and newer superblocks are
+refused with NotImplementedError.  The format subset is checked by round trips and by
 structural tests; no HDF5 library is available to cross-check against.
 """
 from __future__ import annotations
 
 import struct
+import zlib
 
 import numpy as np
 
@@ -136,6 +141,77 @@ def _attr_messages(attrs):
 
 ISTORE_K = 32  # indexed storage internal node K of a version-0 superblock
 
+FILTER_DEFLATE, FILTER_SHUFFLE, FILTER_FLETCHER32 = 1, 2, 3
+
+
+def _filter_message(filters):
+    """Filter pipeline message, version 1: [(filter id, [client data])] for
+    the predefined filters (no names), each optional (flags 0)."""
+    body = struct.pack("<BB6x", 1, len(filters))
+    for fid, cd in filters:
+        body += struct.pack("<HHHH", fid, 0, 0, len(cd)) + b"".join(struct.pack("<I", v) for v in cd)
+        if len(cd) % 2:
+            body += b"\0" * 4
+    return body
+
+
+def _parse_filters(b, off):
+    """[(filter id, [client data])] of a filter pipeline message (versions 1
+    and 2 of the format specification)."""
+    version, n = b[off], b[off + 1]
+    p = off + (8 if version == 1 else 2)
+    if version not in (1, 2):
+        raise NotImplementedError(f"filter pipeline message version {version}")
+    out = []
+    for _ in range(n):
+        fid = struct.unpack_from("<H", b, p)[0]
+        p += 2
+        name_len = 0
+        if version == 1 or fid >= 256:
+            name_len = struct.unpack_from("<H", b, p)[0]
+            p += 2
+        _flags, ncd = struct.unpack_from("<HH", b, p)
+        p += 4
+        p += _pad8(name_len) if version == 1 else name_len
+        cd = list(struct.unpack_from("<" + "I" * ncd, b, p))
+        p += 4 * ncd
+        if version == 1 and ncd % 2:
+            p += 4
+        out.append((fid, cd))
+    return out
+
+
+def _shuffle(raw, size):
+    n = len(raw) // size
+    head = np.frombuffer(raw, dtype=np.uint8, count=n * size).reshape(n, size).T.tobytes()
+    return head + raw[n * size:]
+
+
+def _unshuffle(raw, size):
+    n = len(raw) // size
+    head = np.frombuffer(raw, dtype=np.uint8, count=n * size).reshape(size, n).T.tobytes()
+    return head + raw[n * size:]
+
+
+def _decode_chunk(raw, filters, mask, itemsize):
+    """Undo the pipeline on one chunk's stored bytes, last filter first;
+    bit i of ``mask`` set means filter i was skipped for this chunk."""
+    data = bytes(raw)
+    for i in range(len(filters) - 1, -1, -1):
+        if (mask >> i) & 1:
+            continue
+        fid, cd = filters[i]
+        if fid == FILTER_DEFLATE:
+            data = zlib.decompress(data)
+        elif fid == FILTER_SHUFFLE:
+            data = _unshuffle(data, int(cd[0]) if cd else itemsize)
+        elif fid == FILTER_FLETCHER32:
+            # the checksum the filter appended (4 bytes): stripped, not verified
+            data = data[:-4]
+        else:
+            raise NotImplementedError(f"HDF5 filter {fid}")
+    return data
+
 
 def _chunk_grid(shape, chunk):
     """Offsets (in elements) of the chunks covering `shape`, in C order."""
@@ -143,16 +219,25 @@ def _chunk_grid(shape, chunk):
     return [tuple(int(i) * int(c) for i, c in zip(idx, chunk)) for idx in np.ndindex(*counts)]
 
 
-def write_file(path, datasets, attrs=None, root_attrs=None, chunks=None):
+def write_file(path, datasets, attrs=None, root_attrs=None, chunks=None, compression=None, shuffle=None):
     """Write an HDF5 file with datasets in its root group.
 
     datasets: {name: ndarray} (stored as given: shape and C-order data);
     attrs: {name: {attr: str}}; root_attrs: {attr: str}; chunks: {name:
-    chunk shape} for datasets stored in unfiltered chunks (at most
-    2 * 32 chunks each, one B-tree node), the others contiguous.  Names are
+    chunk shape} for datasets stored in chunks (at most 2 * 32 chunks each,
+    one B-tree node), the others contiguous; compression: {name: deflate
+    level 1-9} and shuffle: {name, ...} filter chunked datasets as h5py's
+    ``compression=level`` and ``shuffle=True`` do (shuffle first).  Names are
     sorted in the group, as the format requires."""
     attrs = attrs or {}
     chunks = {k: tuple(int(c) for c in v) for k, v in (chunks or {}).items()}
+    compression = {k: int(v) for k, v in (compression or {}).items() if v}
+    shuffle = set(shuffle or ())
+    for n in set(compression) | shuffle:
+        if n not in chunks:
+            raise ValueError(f"{n}: filters need chunked storage")
+        if n in compression and not 1 <= compression[n] <= 9:
+            raise ValueError(f"{n}: deflate level {compression[n]}")
     names = sorted(datasets)
     for n in names:
         if "/" in n or not n:
@@ -192,16 +277,43 @@ def write_file(path, datasets, attrs=None, root_attrs=None, chunks=None):
     a_snods = [a_btree + btree_size + i * snod_size for i in range(len(groups))]
     p = a_btree + btree_size + len(groups) * snod_size
 
+    def pipeline(n):
+        f = []
+        if n in shuffle:
+            f.append((FILTER_SHUFFLE, [arrays[n].itemsize]))
+        if n in compression:
+            f.append((FILTER_DEFLATE, [compression[n]]))
+        return f
+
     def dset_msgs(n, data_addr):
         a = arrays[n]
+        filt = []
         if n in chunks:
             ch = chunks[n]
             layout = (struct.pack("<BBBQ", 3, 2, a.ndim + 1, data_addr) +
                       b"".join(struct.pack("<I", c) for c in ch) + struct.pack("<I", a.itemsize))
+            if pipeline(n):
+                filt = [(MSG_FILTERS, _filter_message(pipeline(n)))]
         else:
             layout = struct.pack("<BBQQ", 3, 1, data_addr if a.nbytes else UNDEF, a.nbytes)
         return ([(MSG_DATASPACE, _dataspace_message(a.shape)), (MSG_DATATYPE, _datatype_message(a.dtype)),
-                 (MSG_FILL, struct.pack("<BBBB", 2, 2, 2, 0)), (MSG_LAYOUT, layout)] + _attr_messages(attrs.get(n)))
+                 (MSG_FILL, struct.pack("<BBBB", 2, 2, 2, 0))] + filt + [(MSG_LAYOUT, layout)] +
+                _attr_messages(attrs.get(n)))
+
+    def chunk_blocks(n):
+        """(offsets, stored bytes) of each chunk of a chunked dataset (edge
+        chunks zero-filled to the full chunk shape, then filtered)."""
+        a, ch = arrays[n], chunks[n]
+        out = []
+        for o in _chunk_grid(a.shape, ch):
+            blk = np.zeros(ch, dtype=a.dtype)
+            sl = tuple(slice(x, min(x + c, d)) for x, c, d in zip(o, ch, a.shape))
+            blk[tuple(slice(0, t.stop - t.start) for t in sl)] = a[sl]
+            raw = blk.tobytes()
+            for fid, cd in pipeline(n):
+                raw = _shuffle(raw, cd[0]) if fid == FILTER_SHUFFLE else zlib.compress(raw, cd[0])
+            out.append((o, raw))
+        return out
 
     for n, ch in chunks.items():
         a = arrays[n]
@@ -214,7 +326,7 @@ def write_file(path, datasets, attrs=None, root_attrs=None, chunks=None):
     for n in names:
         a_obj[n] = p
         p += len(_object_header(dset_msgs(n, 0)))
-    a_data, a_chunks = {}, {}
+    a_data, a_chunks, blocks = {}, {}, {}
     for n in names:
         p = _pad8(p)
         a_data[n] = p
@@ -222,12 +334,12 @@ def write_file(path, datasets, attrs=None, root_attrs=None, chunks=None):
             a = arrays[n]
             ksize = 8 + 8 * (a.ndim + 1)
             p += 24 + 2 * ISTORE_K * 8 + (2 * ISTORE_K + 1) * ksize
-            cbytes = int(np.prod(chunks[n])) * a.itemsize
+            blocks[n] = chunk_blocks(n)
             a_chunks[n] = []
-            for _ in _chunk_grid(a.shape, chunks[n]):
+            for _, raw in blocks[n]:
                 p = _pad8(p)
                 a_chunks[n].append(p)
-                p += cbytes
+                p += len(raw)
         else:
             p += arrays[n].nbytes
     eof = _pad8(p)
@@ -264,16 +376,11 @@ def write_file(path, datasets, attrs=None, root_attrs=None, chunks=None):
         # chunk offsets, 0), child i = chunk address; the last key bounds the
         # dataset
         ch = chunks[n]
-        offs = _chunk_grid(a.shape, ch)
-        cbytes = int(np.prod(ch)) * a.itemsize
-        bt = bytearray(b"TREE" + struct.pack("<BBHQQ", 1, 0, len(offs), UNDEF, UNDEF))
-        for o, ca in zip(offs, a_chunks[n]):
-            bt += struct.pack("<II", cbytes, 0) + b"".join(struct.pack("<Q", x) for x in o) + struct.pack("<Q", 0)
+        bt = bytearray(b"TREE" + struct.pack("<BBHQQ", 1, 0, len(blocks[n]), UNDEF, UNDEF))
+        for (o, raw), ca in zip(blocks[n], a_chunks[n]):
+            bt += struct.pack("<II", len(raw), 0) + b"".join(struct.pack("<Q", x) for x in o) + struct.pack("<Q", 0)
             bt += struct.pack("<Q", ca)
-            blk = np.zeros(ch, dtype=a.dtype)
-            sl = tuple(slice(x, min(x + c, d)) for x, c, d in zip(o, ch, a.shape))
-            blk[tuple(slice(0, t.stop - t.start) for t in sl)] = a[sl]
-            out[ca:ca + cbytes] = blk.tobytes()
+            out[ca:ca + len(raw)] = raw
         end = tuple(-(-d // c) * c for d, c in zip(a.shape, ch))
         bt += struct.pack("<II", 0, 0) + b"".join(struct.pack("<Q", x) for x in end) + struct.pack("<Q", 0)
         out[a_data[n]:a_data[n] + len(bt)] = bt
@@ -401,8 +508,9 @@ class _Reader:
             val = val.reshape(shape).copy() if shape else val[0]
         return name, val
 
-    def chunks(self, btree, rank, dt, shape, chunk):
-        """Assemble an unfiltered chunked dataset from its version-1 B-tree."""
+    def chunks(self, btree, rank, dt, shape, chunk, filters=()):
+        """Assemble a chunked dataset from its version-1 B-tree, undoing the
+        filter pipeline on each chunk."""
         b = self.b
         out = np.zeros(shape, dtype=dt)
         ksize = 8 + 8 * (rank + 1)
@@ -423,9 +531,13 @@ class _Reader:
                 if level > 0:
                     walk(child)
                     continue
-                if fmask:
-                    raise NotImplementedError("filtered chunks")
-                blk = np.frombuffer(b, dtype=dt, count=int(np.prod(chunk)), offset=self.addr(child)).reshape(chunk)
+                count = int(np.prod(chunk))
+                if filters:
+                    start = self.addr(child)
+                    raw = _decode_chunk(b[start:start + csize], filters, fmask, dt.itemsize)
+                    blk = np.frombuffer(raw, dtype=dt, count=count).reshape(chunk)
+                else:
+                    blk = np.frombuffer(b, dtype=dt, count=count, offset=self.addr(child)).reshape(chunk)
                 sl = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, chunk, shape))
                 out[sl] = blk[tuple(slice(0, s.stop - s.start) for s in sl)]
 
@@ -437,6 +549,7 @@ class _Reader:
         b = self.b
         dt = shape = None
         layout = None
+        filters = []
         attrs = {}
         for t, off, sz in self.messages(addr):
             if t == MSG_DATASPACE:
@@ -446,9 +559,7 @@ class _Reader:
             elif t == MSG_LAYOUT:
                 layout = off
             elif t == MSG_FILTERS:
-                nfilt = b[off + 1]
-                if nfilt:
-                    raise NotImplementedError("filtered (compressed) datasets")
+                filters = _parse_filters(b, off)
             elif t == MSG_ATTRIBUTE:
                 k, v = self.attribute(off)
                 attrs[k] = v
@@ -459,6 +570,8 @@ class _Reader:
         if version != 3:
             raise NotImplementedError(f"layout message version {version}")
         count = int(np.prod(shape)) if shape else 1
+        if filters and cls != 2:
+            raise ValueError("a filter pipeline on a dataset that is not chunked")
         if cls == 1:
             data_addr, size = struct.unpack_from("<QQ", b, layout + 2)
             if data_addr == UNDEF:
@@ -472,7 +585,7 @@ class _Reader:
             nd = b[layout + 2]
             bt = struct.unpack_from("<Q", b, layout + 3)[0]
             dims = struct.unpack_from("<" + "I" * nd, b, layout + 11)
-            arr = self.chunks(bt, nd - 1, dt, shape, dims[:-1])
+            arr = self.chunks(bt, nd - 1, dt, shape, dims[:-1], filters)
         else:
             raise NotImplementedError(f"layout class {cls}")
         return arr, attrs

@@ -211,3 +211,27 @@ def test_legacy_file_is_the_same_simulation(name, tmp_path):
     b = OracleSimulation(direct, np.float64).run()["p"]
     e = float(np.linalg.norm(a - b) / np.linalg.norm(b))
     assert a.shape == b.shape and e <= 1e-5, e
+
+
+@pytest.mark.parametrize("name", ["ivp_3D_simulation", "tvsp_doppler_effect", "ivp_heterogeneous_medium"])
+def test_compressed_legacy_file(name, tmp_path):
+    """``hdf_compression_level`` deflates the grids and many-row signals
+    (kwave/utils/io.py:78-106); the values, and so the checksums, stay those
+    of MATLAB's file, and the file shrinks."""
+    inp, opts, expected = _load(name)
+    kgrid, medium, source, sensor = _objects(inp)
+    sizes = {}
+    for level in (0, 6):
+        so = NS(save_to_disk=True, save_to_disk_exit=True, data_path=str(tmp_path), input_filename=f"z{level}.h5",
+                hdf_compression_level=level, **opts)
+        (backend.kspaceFirstOrder2DC if kgrid.dim == 2 else backend.kspaceFirstOrder3DC)(kgrid, source, sensor,
+                                                                                          medium, so)
+        sizes[level] = (tmp_path / f"z{level}.h5").stat().st_size
+    got = _summary(tmp_path / "z6.h5")
+    for k, want in expected.items():
+        if k != "root":
+            assert got[k]["checksum8"] == want["checksum8"] and got[k]["shape"] == want["shape"], k
+    assert sizes[6] < 0.5 * sizes[0], sizes
+    with pytest.raises(ValueError, match="hdf_compression_level"):
+        (backend.kspaceFirstOrder2DC if kgrid.dim == 2 else backend.kspaceFirstOrder3DC)(
+            kgrid, source, sensor, medium, NS(save_to_disk=True, data_path=str(tmp_path), hdf_compression_level=12))
