@@ -125,7 +125,9 @@ def _legacy_cpp(ndim_expected, name):
         cpp_io.write_input_file(path, prob, legacy=True, compression_level=int(level))
         if getattr(simulation_options, "save_to_disk_exit", False):
             return None
-        return cpp_io.run_input_file(path, scaled_sources=True)
+        # the sensor's record list and start index, which the reference hands to the binary as flags
+        return cpp_io.run_input_file(path, scaled_sources=True, record=getattr(sensor, "record", None),
+                                     record_start_index=getattr(sensor, "record_start_index", None))
 
     run.__name__ = run.__qualname__ = name
     run.__doc__ = (f"{name}(kgrid, source, sensor, medium, simulation_options, execution_options): the legacy "

@@ -458,9 +458,15 @@ def _rows_to_c_order(rows, idx, shape):
     return rows[np.argsort(c, kind="stable")]
 
 
-def problem_from_input_file(path, scaled_sources=False):
+def problem_from_input_file(path, scaled_sources=False, record=None, record_start_index=None):
     """Problem dict of the native solver's time loop for an input file (PML
-    inside the grid, p0 used as stored, ``p`` recorded).  ``scaled_sources``:
+    inside the grid, p0 used as stored).  It records ``p``, as the C++ binary
+    does by default, or the ``record`` list of a sensor, whose flags the
+    binary takes on its command line
+    (kwave/options/simulation_execution_options.py:276-305); the binary's
+    whole-grid aggregates (``*_all``) are not recorded by the time loop and
+    are refused.  ``record_start_index`` is the binary's ``-s``.
+    ``scaled_sources``:
     the file's source signals carry the legacy route's scaling (files of
     MATLAB k-Wave and of kspaceFirstOrder2DC/3DC with ``save_to_disk``, see
     :func:`legacy_source_factors`), which is divided out again; files of
@@ -512,6 +518,15 @@ def problem_from_input_file(path, scaled_sources=False):
     prob["sensor_mask"] = _mask_from_index(ds["sensor_mask_index"], shape)
     if scaled_sources:
         _unscale_sources(prob, ds)
+    if record is not None:
+        rec = (record,) if isinstance(record, str) else tuple(record)
+        whole = [k for k in rec if k.endswith("_all")]
+        if whole:
+            raise NotImplementedError(f"{whole}: whole-grid aggregates of the C++ binary are not recorded by the "
+                                      "time loop")
+        prob["record"] = rec
+    if record_start_index is not None:
+        prob["record_start_index"] = int(record_start_index)
     return prob
 
 
@@ -535,14 +550,16 @@ def _unscale_sources(prob, ds):
         prob[field] = (rows / f[:, None]).astype(np.float32)
 
 
-def run_input_file(path, stream=None, scaled_sources=False):
+def run_input_file(path, stream=None, scaled_sources=False, record=None, record_start_index=None):
     """Run an input file of the C++ binary on the GB300 time loop; returns
     the result dict of the native solver (``p`` as (n_sensor, Nt) with the
-    sensor points in C order).  ``scaled_sources`` as for
-    :func:`problem_from_input_file`."""
+    sensor points in C order).  ``scaled_sources``, ``record`` and
+    ``record_start_index`` as for :func:`problem_from_input_file`."""
     from .solver import Simulation
 
-    sim = Simulation.from_problem(problem_from_input_file(path, scaled_sources=scaled_sources), stream=stream)
+    prob = problem_from_input_file(path, scaled_sources=scaled_sources, record=record,
+                                   record_start_index=record_start_index)
+    sim = Simulation.from_problem(prob, stream=stream)
     try:
         return sim.run()
     finally:

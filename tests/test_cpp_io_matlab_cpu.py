@@ -235,3 +235,16 @@ def test_compressed_legacy_file(name, tmp_path):
     with pytest.raises(ValueError, match="hdf_compression_level"):
         (backend.kspaceFirstOrder2DC if kgrid.dim == 2 else backend.kspaceFirstOrder3DC)(
             kgrid, source, sensor, medium, NS(save_to_disk=True, data_path=str(tmp_path), hdf_compression_level=12))
+
+
+def test_record_flags_of_the_run(tmp_path):
+    """The sensor's record list and start index reach the problem the file
+    runs as (the binary's command-line flags); by default ``p`` alone, as the
+    binary records; whole-grid aggregates are refused."""
+    path, _, _ = _write("ivp_homogeneous_medium", tmp_path)
+    assert cpp_io.problem_from_input_file(path)["record"] == ("p",)
+    prob = cpp_io.problem_from_input_file(path, record=["p", "p_max", "u_final"], record_start_index=5)
+    assert prob["record"] == ("p", "p_max", "u_final") and prob["record_start_index"] == 5
+    assert cpp_io.problem_from_input_file(path, record="p_final")["record"] == ("p_final",)
+    with pytest.raises(NotImplementedError, match="p_max_all"):
+        cpp_io.problem_from_input_file(path, record=["p", "p_max_all"])
