@@ -49,8 +49,23 @@ def _enabled(x) -> bool:
     if x is None:
         return False
     if hasattr(x, "__len__"):
-        return bool(np.any(np.asarray(x)))  # any non-zero (NaN included), without a temporary mask
+        # any non-zero (NaN included), without a temporary mask; grids in slabs on the pool
+        return bool(_par_reduce(np.asarray(x), np.any, any))
     return x != 0
+
+
+_PAR_MIN = 1 << 20  # elements below which a reduction runs on the calling thread
+
+
+def _par_reduce(arr, fn, combine):
+    """``fn`` over ``arr`` as ``combine`` of ``fn`` over slabs along axis 0
+    on the worker pool (exact for max, min, any: no rounding involved)."""
+    if arr.ndim == 0 or arr.size < _PAR_MIN or arr.shape[0] < 2:
+        return fn(arr)
+    n0 = arr.shape[0]
+    nslab = min(n0, 4 * (_pool()._max_workers))
+    bounds = [(i * n0 // nslab, (i + 1) * n0 // nslab) for i in range(nslab)]
+    return combine(_pool().map(lambda ab: fn(arr[ab[0]:ab[1]]), [ab for ab in bounds if ab[1] > ab[0]]))
 
 
 def grid_of(kgrid):
@@ -385,7 +400,7 @@ def build_setup(prob, derive_on_device=False) -> Setup:
 
     c0_32 = f32(c0)
     # c_ref = max(c0) of the FP32-cast medium (kspace_solver.py:228-231)
-    c_ref = float(np.float32(c0_32)) if isinstance(c0_32, float) else float(np.max(c0_32))
+    c_ref = float(np.float32(c0_32)) if isinstance(c0_32, float) else float(_par_reduce(c0_32, np.max, max))
     if prob.get("c_ref") is not None:
         # held fixed by the sound-speed gradient (the reference has no such
         # input: c_ref is always max(c0)), so that PML and kappa do not move with c0
